@@ -1,0 +1,220 @@
+/*
+ * mf.h -- C ABI of the GB300 magnetization-and-force library (libmfgb.so).
+ *
+ * Drop-in boundary for the reference's solver class
+ *   Libo::cuda_magnet_cgOptimizer   magnetic_solver/magnetic_force.cuh:36-174
+ *                                   magnetic_solver/magnetic_force.cu:608-1410
+ * and for the FMMTL direct evaluation of its two pair kernels
+ *   fmmtl::direct                   fmmtl_minimum/fmmtl/Direct.hpp:62-74
+ *   DipoleBKernel                   fmmtl_minimum/kernel/Dipole_B.kern:13-134
+ *   DipoleHessianKernel             fmmtl_minimum/kernel/Dipole_hessian.kern:19-278
+ *
+ * Plain C: pointers, sizes and status codes only.  Every call returns an
+ * mf_status; mf_last_error() gives a message for the calling thread's last
+ * failure.  A handle is used by one host thread at a time.  All device work
+ * of a handle runs on the handle's stream (mf_set_stream; default: the
+ * legacy default stream).  Calls that hand results to host memory return
+ * after the copy has completed.
+ *
+ * Layouts.  Host arrays passed to the solver are AoS float [n][3] (the
+ * reference's std::vector<float3>) unless MF_LAYOUT_SOA is given, in which
+ * case x[n], y[n], z[n] follow one another.  Published results (MF_Q_*) live
+ * on the device as SoA float arrays, like the reference's
+ * cuda_abstract_vector members (dev_x, dev_y, dev_z).
+ */
+#ifndef MF_GB300_H
+#define MF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MF_ABI_VERSION 1
+
+typedef enum mf_status {
+  MF_OK = 0,
+  MF_ERR_INVALID_ARG = 1,   /* bad pointer, size, NaN/Inf input, unknown key */
+  MF_ERR_OOM = 2,           /* device allocation failed */
+  MF_ERR_NOT_CONVERGED = 3, /* solver hit its iteration cap above tolerance */
+  MF_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+  MF_ERR_TIMEOUT = 5,       /* a kernel's bounded wait ran out (device error word set) */
+  MF_ERR_BUDGET = 6,        /* admission refused: over the HBM budget */
+  MF_ERR_UNSUPPORTED = 7,   /* no CUDA device / feature not available */
+  MF_ERR_BUSY = 8           /* serving queue full */
+} mf_status;
+
+typedef enum mf_layout { MF_LAYOUT_AOS = 0, MF_LAYOUT_SOA = 1 } mf_layout;
+typedef enum mf_where { MF_HOST = 0, MF_DEVICE = 1 } mf_where;
+typedef enum mf_precision { MF_FP32 = 0, MF_FP64 = 1 } mf_precision;
+
+/* Quantities a solver publishes (the reference's public members). */
+typedef enum mf_quantity {
+  MF_Q_POSITIONS = 0, /* xyz                 magnetic_force.cuh:136 */
+  MF_Q_M = 1,         /* M = V chi/(1+chi) b magnetic_force.cuh:140 */
+  MF_Q_B_OVER_MU0 = 2,/* total_B_over_mu0   magnetic_force.cuh:141 */
+  MF_Q_HEXT = 3,      /* Hext               magnetic_force.cuh:138 */
+  MF_Q_FORCE = 4,     /* magnetic_bodyforce magnetic_force.cuh:152 */
+  MF_Q_DHEXTDX = 5,   /* dHextdx            magnetic_force.cuh:148 */
+  MF_Q_DHEXTDY = 6,   /* dHextdy            magnetic_force.cuh:149 */
+  MF_Q_DHEXTDZ = 7,   /* dHextdz            magnetic_force.cuh:150 */
+  MF_Q_VELOCITY = 8   /* harness state of mf_advance (not in the reference) */
+} mf_quantity;
+
+/* Solver algorithms. */
+typedef enum mf_solver_kind {
+  /* The reference's least-squares nonlinear CG: 3 field products per
+   * iteration, absolute RMS tolerance, stop on error increase, restart every
+   * 10 iterations (magnetic_force.cu:874-1095, :1275-1315).  Default. */
+  MF_SOLVER_NLCG = 0,
+  /* Conjugate gradients on (I - c G) b = Hext (symmetric positive definite),
+   * one field product per iteration, FP64 inner products, stop on relative
+   * residual |r|/|Hext| < rel_tol. */
+  MF_SOLVER_CG = 1
+} mf_solver_kind;
+
+/* Option keys for mf_set_option / mf_get_option. */
+typedef enum mf_option {
+  MF_OPT_TOLERANCE = 0,     /* NLCG absolute RMS tolerance (reference default 0.1) */
+  MF_OPT_MAX_ITERATION = 1, /* NLCG iteration cap (reference default 80) */
+  MF_OPT_NAIVE = 2,         /* 1: reproduce the reference's naive CUDA path:
+                               external sources use h (not ext_mag_h) and the
+                               external force term gets an extra mu0
+                               (magnetic_force.cu:1118, :589-600) */
+  MF_OPT_SOLVER = 3,        /* mf_solver_kind */
+  MF_OPT_REL_TOL = 4,       /* CG relative residual tolerance (default 1e-6 FP32, 1e-8 FP64) */
+  MF_OPT_CG_MAX_ITER = 5,   /* CG iteration cap (default 500) */
+  MF_OPT_CRIT_SIZE = 6,     /* accepted for compatibility (crit_size, :647); unused */
+  MF_OPT_CHECK_INTERVAL = 7 /* CG: iterations launched between host convergence checks (default 4) */
+} mf_option;
+
+/* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
+typedef struct mf_params {
+  int64_t num_particles;
+  float h;
+  float ext_mag_h;
+  float volume;
+  float chi;
+  float const_ext_field[3];
+  const float* target_pos;     /* host AoS [num_particles][3] */
+  const float* ext_source_pos; /* host AoS [n_ext][3], may be NULL if n_ext == 0 */
+  const float* ext_source_M;   /* host AoS [n_ext][3] */
+  int64_t n_ext;
+  int32_t precision;           /* mf_precision */
+  int32_t device;              /* CUDA device ordinal */
+} mf_params;
+
+typedef struct mf_solver mf_solver;
+
+/* Status text and the calling thread's last error message. */
+const char* mf_status_string(mf_status s);
+const char* mf_last_error(void);
+int mf_abi_version(void);
+
+/* Constructor / destructor.
+ * Replaces cuda_magnet_cgOptimizer::cuda_magnet_cgOptimizer(CtorParam)
+ * (magnetic_force.cu:608-703) and ~cuda_magnet_cgOptimizer. */
+mf_status mf_create(const mf_params* p, mf_solver** out);
+mf_status mf_destroy(mf_solver* s);
+
+/* Stream all of the handle's work is issued on (cudaStream_t as void*). */
+mf_status mf_set_stream(mf_solver* s, void* stream);
+
+/* setTargetpos(const std::vector<float3>&) (magnetic_force.cu:806-871), with
+ * Resize (magnetic_force.cu:706-743): a new particle count keeps the first
+ * min(old, new) entries of total_B_over_mu0 as the warm start (new entries
+ * start at zero).  `where` says whether xyz is host or device memory. */
+mf_status mf_set_positions(mf_solver* s, const float* xyz, int64_t n, int32_t layout, int32_t where);
+
+/* setHext(const setHextParams&) (magnetic_force.cu:746-803). */
+mf_status mf_set_external(mf_solver* s, const float H0[3], const float* src_pos, const float* src_M,
+                          int64_t n_src, float ext_mag_h);
+
+/* solve(size_t niter) (magnetic_force.cu:874-888).  Runs the configured
+ * solver; *iters (may be NULL) gets the iterations run and *final_err the
+ * last error (NLCG: 0.5|r|^2 as in total_error; CG: |r|/|Hext|).
+ * NLCG returns MF_OK whenever it stops as the reference would; CG returns
+ * MF_ERR_NOT_CONVERGED if it reached its cap above tolerance. */
+mf_status mf_solve(mf_solver* s, int64_t niter, int64_t* iters, double* final_err);
+
+/* The NLCG error history of the last solve (total_error, magnetic_force.cuh:116).
+ * Copies min(cap, len) doubles into dst and returns the length in *len. */
+mf_status mf_get_error_history(mf_solver* s, double* dst, int64_t cap, int64_t* len);
+
+/* evaluate_fitted_near_foece() (magnetic_force.cu:890-997): M = c b, then the
+ * Kelvin force F_i = (Rext_i + sum_j T_ij) m_i into MF_Q_FORCE. */
+mf_status mf_eval_force(mf_solver* s);
+
+/* Copy a published quantity (n x 3 floats) to dst in the given layout.
+ * where == MF_DEVICE copies device-to-device. */
+mf_status mf_get(mf_solver* s, int32_t quantity, float* dst, int32_t layout, int32_t where);
+/* Same for FP64 solvers' full-precision values (FP32 solvers convert). */
+mf_status mf_get_f64(mf_solver* s, int32_t quantity, double* dst, int32_t layout, int32_t where);
+
+/* Device SoA pointers of a published quantity (the reference's public
+ * members' dev_x / dev_y / dev_z).  Valid until the next call that changes
+ * the particle count. */
+mf_status mf_device_soa(mf_solver* s, int32_t quantity, float** x, float** y, float** z);
+
+mf_status mf_num_particles(mf_solver* s, int64_t* n);
+
+mf_status mf_set_option(mf_solver* s, int32_t key, double value);
+mf_status mf_get_option(mf_solver* s, int32_t key, double* value);
+
+/* export_data / export_force (magnetic_force.cu:1318-1410): one line per
+ * particle, "i x y z v0 v1 v2 H0 H1 H2", v = total_B_over_mu0 / force. */
+mf_status mf_export_data(mf_solver* s, const char* path);
+mf_status mf_export_force(mf_solver* s, const char* path);
+
+/* One timestep of the benchmark harness, all on the device: solve (warm
+ * start), force, then symplectic Euler v += dt F / (rho V), x += dt v with
+ * unit density.  Not part of the reference (its caller moves the particles). */
+mf_status mf_advance(mf_solver* s, double dt, int64_t niter, int64_t* iters);
+
+/* Counters: field products, force passes and pair interactions issued by
+ * this handle since creation (or the last reset). */
+typedef struct mf_counters {
+  int64_t field_products;
+  int64_t force_passes;
+  double field_pairs;
+  double force_pairs;
+  int64_t kernel_launches;
+} mf_counters;
+mf_status mf_get_counters(mf_solver* s, mf_counters* c);
+mf_status mf_reset_counters(mf_solver* s);
+
+/* ---------------------------------------------------------------------- */
+/* Direct all-pairs evaluation of the reference's pair kernels on device    */
+/* buffers (AoS float [n][3] device arrays; results overwritten).           */
+/* ---------------------------------------------------------------------- */
+
+/* results_i = sum_j DipoleBKernel{h}(targets_i, sources_j) * charges_j
+ * Replaces fmmtl::direct(DipoleBKernel, ...) (Direct.hpp:62-74 ->
+ * S2T.hpp:57-79) and the naive cuda_Apply_G / cuda_ext_field_kernel bodies
+ * (magnetic_force.cu:8-237).  Allocates its scratch on first use. */
+mf_status mf_direct_field(const float* targets, int64_t nt, const float* sources, const float* charges,
+                          int64_t ns, float h, float* results, void* stream);
+
+/* results9_i = sum_j DipoleHessianKernel{h}(targets_i, sources_j) * charges_j,
+ * 3x3 per target in glm column-major order (results9[i*9 + c*3 + r]).
+ * Replaces fmmtl::direct(DipoleHessianKernel, ...) and
+ * cuda_ext_fitted_force_tensor_kernel (magnetic_force.cu:432-512). */
+mf_status mf_direct_force_tensor(const float* targets, int64_t nt, const float* sources,
+                                 const float* charges, int64_t ns, float h, float* results9, void* stream);
+
+/* F_i = (sum_j T(x_i - x_j; h) m_j) m_i over one particle set, plus
+ * Rext_i m_i when rext9 (device [n][9], may be NULL) is given: the force
+ * assembly of fitted_force_ofM_kernel / evaluate_fitted_near_foece
+ * (magnetic_force.cu:516-605, :968-980). */
+mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h, const float* rext9,
+                          int32_t naive_quirks, float* force, void* stream);
+
+/* Frees the scratch the mf_direct_* calls keep per device. */
+mf_status mf_release_scratch(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MF_GB300_H */

@@ -1,0 +1,308 @@
+// mf_allpairs.cu -- plans, scratch and launches of the all-pairs kernel.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <type_traits>
+
+#include "mf_internal.h"
+
+namespace mfgb {
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+mf_status fail(mf_status s, const std::string& msg) {
+  g_last_error = msg;
+  return s;
+}
+
+mf_status cuda_fail(cudaError_t e, const char* what) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s failed: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+  g_last_error = buf;
+  if (e == cudaErrorMemoryAllocation) return MF_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MF_ERR_UNSUPPORTED;
+  return MF_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// DevBuf / Scratch
+// ---------------------------------------------------------------------------
+mf_status DevBuf::reserve(size_t want, bool keep, bool zero) {
+  if (want == 0) want = 16;
+  if (want <= bytes) return MF_OK;
+  void* p = nullptr;
+  MF_CUDA_TRY(cudaMalloc(&p, want));
+  size_t kept = 0;
+  if (keep && ptr && bytes) {
+    cudaError_t e = cudaMemcpy(p, ptr, bytes, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return cuda_fail(e, "cudaMemcpy(grow)");
+    }
+    kept = bytes;
+  }
+  if (zero) {
+    cudaError_t e = cudaMemset(static_cast<char*>(p) + kept, 0, want - kept);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return cuda_fail(e, "cudaMemset(grow)");
+    }
+  }
+  release();
+  ptr = p;
+  bytes = want;
+  return MF_OK;
+}
+
+mf_status Scratch::ensure(size_t partial_doubles, size_t n_counters) {
+  MF_TRY(partials.reserve(partial_doubles * sizeof(double)));
+  MF_TRY(counters.reserve(n_counters * sizeof(int32_t), /*keep=*/true, /*zero=*/true));
+  MF_TRY(err.reserve(16, true, true));
+  return MF_OK;
+}
+
+mf_status Scratch::check(cudaStream_t st) {
+  if (!err.ptr) return MF_OK;
+  int32_t host = 0;
+  MF_CUDA_TRY(cudaMemcpyAsync(&host, err.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaStreamSynchronize(st));
+  if (host != 0) {
+    // Leave the scratch in its between-launches state again.
+    MF_CUDA_TRY(cudaMemsetAsync(err.ptr, 0, err.bytes, st));
+    if (counters.ptr) MF_CUDA_TRY(cudaMemsetAsync(counters.ptr, 0, counters.bytes, st));
+    MF_CUDA_TRY(cudaStreamSynchronize(st));
+    char buf[128];
+    snprintf(buf, sizeof(buf), "kernel wait ran out (device error %d); results of that launch are invalid",
+             int(host));
+    return fail(MF_ERR_TIMEOUT, buf);
+  }
+  return MF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device facts
+// ---------------------------------------------------------------------------
+int current_device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d;
+}
+
+int device_sms(int device) {
+  static std::mutex mu;
+  static int cache[64] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (device < 0 || device >= 64) return 1;
+  if (!cache[device]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+    cache[device] = v > 0 ? v : 1;
+  }
+  return cache[device];
+}
+
+// ---------------------------------------------------------------------------
+// Kernel selection
+// ---------------------------------------------------------------------------
+template <class Real, Body B>
+struct BodyOf;
+template <class Real>
+struct BodyOf<Real, Body::Field> {
+  using type = FieldBody<Real>;
+};
+template <class Real>
+struct BodyOf<Real, Body::Force> {
+  using type = ForceBody<Real>;
+};
+template <class Real>
+struct BodyOf<Real, Body::Tensor> {
+  using type = TensorBody<Real>;
+};
+
+template <class Real, Body B>
+struct Launcher {
+  using C = KCfg<Real, B>;
+  using BT = typename BodyOf<Real, B>::type;
+  static constexpr int TBT = C::TPB * C::TPT;
+  static constexpr size_t kSmem = size_t(C::STAGES) * StageLayout<Real, C::TILE>::kBytes;
+
+  static auto kernel() { return allpairs_kernel<Real, BT, C::TPB, C::TPT, C::TILE, C::STAGES>; }
+
+  // Resident CTAs per device (occupancy x SMs); sets the smem attribute once per device.
+  static int max_grid(int device) {
+    static std::mutex mu;
+    static int cache[64] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (device < 0 || device >= 64) device = 0;
+    if (!cache[device]) {
+      auto k = kernel();
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmem));
+      int per_sm = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, C::TPB, kSmem);
+      if (per_sm < 1) per_sm = 1;
+      cache[device] = per_sm * device_sms(device);
+    }
+    return cache[device];
+  }
+
+  static mf_status launch(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials,
+                          int32_t* counters, int32_t* err, cudaStream_t st) {
+    if (plan.total_steps <= 0) return MF_OK;
+    const int dev = current_device();
+    const int64_t g = std::min<int64_t>(plan.total_steps, max_grid(dev));
+    AllPairsArgs<Real> a;
+    memset(&a, 0, sizeof(a));
+    a.scenes = plan.d_scenes.template as<SceneDesc<Real>>();
+    a.n_scenes = plan.n_scenes;
+    a.total_steps = plan.total_steps;
+    a.tpos = io.tpos;
+    a.tmom = io.tmom;
+    a.spos = io.spos;
+    a.smom = io.smom;
+    for (int k = 0; k < 9; ++k) {
+      a.out[k] = io.out[k];
+      a.rext[k] = io.rext[k];
+    }
+    a.out4 = io.out4;
+    a.add4 = io.add4;
+    a.add4b = io.add4b;
+    a.naive_quirks = io.naive_quirks;
+    a.done_flags = io.done_flags;
+    a.done_stride = io.done_stride;
+    a.partials = partials;
+    a.counters = counters;
+    a.err = err;
+    kernel()<<<unsigned(g), C::TPB, kSmem, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "allpairs_kernel launch");
+    return MF_OK;
+  }
+
+  static void needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
+    const int64_t g = std::min<int64_t>(plan.total_steps, max_grid(current_device()));
+    *pd = size_t(g) * 2 * TBT * C::kOut;
+    *nc = size_t(plan.total_tb);
+  }
+};
+
+template <class Real>
+static void cfg_of(Body b, int* tile, int* tbt) {
+  switch (b) {
+    case Body::Field:
+      *tile = KCfg<Real, Body::Field>::TILE;
+      *tbt = KCfg<Real, Body::Field>::TPB * KCfg<Real, Body::Field>::TPT;
+      break;
+    case Body::Force:
+      *tile = KCfg<Real, Body::Force>::TILE;
+      *tbt = KCfg<Real, Body::Force>::TPB * KCfg<Real, Body::Force>::TPT;
+      break;
+    default:
+      *tile = KCfg<Real, Body::Tensor>::TILE;
+      *tbt = KCfg<Real, Body::Tensor>::TPB * KCfg<Real, Body::Tensor>::TPT;
+      break;
+  }
+}
+
+template <class Real>
+static void fill_coefs(const SceneSpec& s, SceneDesc<Real>& d) {
+  d.pc = make_pair_consts<Real>(s.h);
+  d.scale = Real(s.scale);
+  d.coef_add = Real(s.coef_add);
+  d.coef_add2 = Real(s.coef_add2);
+  for (int k = 0; k < 3; ++k) d.cvec[k] = Real(s.cvec[k]);
+}
+
+template <class Real>
+mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan) {
+  int tile = 0, tbt = 0;
+  cfg_of<Real>(body, &tile, &tbt);
+  plan.body = body;
+  plan.host.clear();
+  plan.host.reserve(specs.size());
+  int64_t step = 0, tbo = 0;
+  double pairs = 0;
+  for (const SceneSpec& s : specs) {
+    if (s.nt <= 0 || s.ns <= 0) return fail(MF_ERR_INVALID_ARG, "build_plan: empty scene");
+    if (!(s.h > 0.0)) return fail(MF_ERR_INVALID_ARG, "build_plan: smoothing length must be > 0");
+    SceneDesc<Real> d;
+    memset(&d, 0, sizeof(d));
+    d.t_off = s.t_off;
+    d.nt = s.nt;
+    d.s_off = s.s_off;
+    d.ns = s.ns;
+    d.n_tiles = int32_t((s.ns + tile - 1) / tile);
+    d.n_tb = int32_t((s.nt + tbt - 1) / tbt);
+    d.step_off = step;
+    d.tb_off = tbo;
+    fill_coefs(s, d);
+    step += int64_t(d.n_tiles) * d.n_tb;
+    tbo += d.n_tb;
+    pairs += double(s.nt) * double(s.ns);
+    plan.host.push_back(d);
+  }
+  plan.total_steps = step;
+  plan.total_tb = tbo;
+  plan.n_scenes = int32_t(plan.host.size());
+  plan.pairs = pairs;
+  const size_t bytes = plan.host.size() * sizeof(SceneDesc<Real>);
+  MF_TRY(plan.d_scenes.reserve(bytes));
+  if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
+  return MF_OK;
+}
+
+template <class Real>
+mf_status refresh_plan_coefs(const std::vector<SceneSpec>& specs, Plan<Real>& plan) {
+  if (specs.size() != plan.host.size()) return fail(MF_ERR_INVALID_ARG, "refresh_plan_coefs: size");
+  for (size_t i = 0; i < specs.size(); ++i) fill_coefs(specs[i], plan.host[i]);
+  const size_t bytes = plan.host.size() * sizeof(SceneDesc<Real>);
+  if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
+  return MF_OK;
+}
+
+template <class Real>
+void plan_scratch_needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
+  switch (plan.body) {
+    case Body::Field: Launcher<Real, Body::Field>::needs(plan, pd, nc); break;
+    case Body::Force: Launcher<Real, Body::Force>::needs(plan, pd, nc); break;
+    default: Launcher<Real, Body::Tensor>::needs(plan, pd, nc); break;
+  }
+}
+
+template <class Real>
+mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials, int32_t* counters,
+                       int32_t* err, cudaStream_t st) {
+  switch (plan.body) {
+    case Body::Field: return Launcher<Real, Body::Field>::launch(plan, io, partials, counters, err, st);
+    case Body::Force: return Launcher<Real, Body::Force>::launch(plan, io, partials, counters, err, st);
+    default: return Launcher<Real, Body::Tensor>::launch(plan, io, partials, counters, err, st);
+  }
+}
+
+template <class Real>
+mf_status run_plan(const Plan<Real>& plan, const LaunchIO<Real>& io, Scratch& scratch, cudaStream_t st) {
+  size_t pd = 0, nc = 0;
+  plan_scratch_needs(plan, &pd, &nc);
+  MF_TRY(scratch.ensure(pd, nc));
+  return run_plan_raw(plan, io, scratch.partials.as<double>(), scratch.counters.as<int32_t>(),
+                      scratch.err.as<int32_t>(), st);
+}
+
+#define MF_INSTANTIATE(R)                                                                                  \
+  template mf_status build_plan<R>(Body, const std::vector<SceneSpec>&, Plan<R>&);                        \
+  template mf_status refresh_plan_coefs<R>(const std::vector<SceneSpec>&, Plan<R>&);                      \
+  template void plan_scratch_needs<R>(const Plan<R>&, size_t*, size_t*);                                  \
+  template mf_status run_plan<R>(const Plan<R>&, const LaunchIO<R>&, Scratch&, cudaStream_t);             \
+  template mf_status run_plan_raw<R>(const Plan<R>&, const LaunchIO<R>&, double*, int32_t*, int32_t*,     \
+                                     cudaStream_t);
+MF_INSTANTIATE(float)
+MF_INSTANTIATE(double)
+#undef MF_INSTANTIATE
+
+}  // namespace mfgb

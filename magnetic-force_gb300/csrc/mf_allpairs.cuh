@@ -1,0 +1,479 @@
+// mf_allpairs.cuh -- persistent all-pairs tile kernel for sm_103a.
+//
+// One launch evaluates sum_j K(x_i - y_j) * s_j for every target i of one or
+// more independent scenes (a scene = a contiguous target range and a
+// contiguous source range with its own smoothing length and epilogue scale).
+//
+// Work layout.  Each scene's targets are cut into target blocks of
+// TPB * TPT targets (TPT targets per thread, strided by TPB for coalescing)
+// and its sources into tiles of TILE sources.  The (target block, source tile)
+// pairs of all scenes form one flat "step" space that is split evenly over a
+// grid of resident CTAs, so every SM gets the same number of tile-steps
+// whatever the scene sizes are.  A CTA walks its contiguous step range:
+//   * source tiles are staged in shared memory by 1-D bulk copies
+//     (cp.async.bulk, completion on an mbarrier), STAGES deep, issued by one
+//     thread, no cluster multicast;
+//   * each thread keeps TPT targets in registers and sweeps the tile with
+//     broadcast shared-memory reads;
+//   * per target the tile's sum is formed in plain FP32 and folded into the
+//     running sum with two-sum compensation (FP64 kernels add directly);
+//   * a target block completely covered by one CTA is finished in place; the
+//     first and last target blocks of a CTA's range may be shared with a
+//     neighbour CTA, which write FP64 partials to scratch, and the last of
+//     them to arrive (atomic ticket) adds the partials in CTA order, so the
+//     result does not depend on scheduling.
+#pragma once
+#include <cstdint>
+
+#include "mf_device.cuh"
+#include "mf_pair.cuh"
+
+namespace mfgb {
+
+template <class Real>
+struct SceneDesc {
+  int64_t t_off, nt;     // target index range
+  int64_t s_off, ns;     // source index range
+  int64_t step_off;      // first flat step of this scene
+  int64_t tb_off;        // first global target-block index of this scene
+  int32_t n_tiles;       // ceil(ns / TILE)
+  int32_t n_tb;          // ceil(nt / (TPB*TPT))
+  PairConsts<Real> pc;
+  // Field epilogue: out = scale * value + coef_add * add4 + coef_add2 * add4b + cvec.
+  // Force / tensor epilogues use scale only.
+  Real scale;
+  Real coef_add;
+  Real coef_add2;
+  Real cvec[3];
+};
+
+template <class Real>
+struct AllPairsArgs {
+  using R4 = typename Vec4T<Real>::type;
+  const SceneDesc<Real>* scenes;
+  int32_t n_scenes;
+  int64_t total_steps;
+  const R4* tpos;
+  const R4* tmom;  // target dipoles (force kernel)
+  const R4* spos;
+  const R4* smom;
+  Real* out[9];        // SoA outputs
+  R4* out4;            // packed output (field kernel), optional
+  const R4* add4;      // field epilogue addends (packed), optional
+  const R4* add4b;
+  const Real* rext[9]; // force epilogue: external gradient tensor (SoA), optional
+  int32_t naive_quirks;
+  // Optional per-scene stop flags (solver scalar rows): a scene whose flag is
+  // non-zero is skipped (its outputs are left as they are).
+  const double* done_flags;
+  int32_t done_stride;
+  double* partials;    // [grid][2][TPB*TPT][kOut]
+  int32_t* counters;   // [total target blocks], zero between launches
+  int32_t* err;        // device error word
+};
+
+// ----------------------------------------------------------------------------
+// Bodies: what a pair adds and how a target's result is written.
+// ----------------------------------------------------------------------------
+template <class Real>
+struct FieldBody {
+  using R4 = typename Vec4T<Real>::type;
+  static constexpr int kAcc = 6;
+  static constexpr int kOut = 3;
+  struct TData {
+    Real x, y, z;
+  };
+  __device__ static void load(const AllPairsArgs<Real>& a, int64_t i, TData& t) {
+    R4 p = a.tpos[i];
+    t.x = p.x;
+    t.y = p.y;
+    t.z = p.z;
+  }
+  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
+                              Real* acc) {
+    field_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc, acc + 3);
+  }
+  __device__ static void tile_out(const Real* acc, Real* o) {
+    const Real c = Real(kInv4Pi);
+    o[0] = (Real(3) * acc[0] - acc[3]) * c;
+    o[1] = (Real(3) * acc[1] - acc[4]) * c;
+    o[2] = (Real(3) * acc[2] - acc[5]) * c;
+  }
+  __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
+                                  const TData&, const double* v) {
+    Real o[3];
+    for (int k = 0; k < 3; ++k) o[k] = Real(v[k]) * sc.scale + sc.cvec[k];
+    if (a.add4) {
+      R4 q = a.add4[i];
+      o[0] += sc.coef_add * q.x;
+      o[1] += sc.coef_add * q.y;
+      o[2] += sc.coef_add * q.z;
+    }
+    if (a.add4b) {
+      R4 q = a.add4b[i];
+      o[0] += sc.coef_add2 * q.x;
+      o[1] += sc.coef_add2 * q.y;
+      o[2] += sc.coef_add2 * q.z;
+    }
+    if (a.out[0]) {
+      a.out[0][i] = o[0];
+      a.out[1][i] = o[1];
+      a.out[2][i] = o[2];
+    }
+    if (a.out4) {
+      R4 w;
+      w.x = o[0];
+      w.y = o[1];
+      w.z = o[2];
+      w.w = Real(0);
+      a.out4[i] = w;
+    }
+  }
+};
+
+template <class Real>
+struct ForceBody {
+  using R4 = typename Vec4T<Real>::type;
+  static constexpr int kAcc = 3;
+  static constexpr int kOut = 3;
+  struct TData {
+    Real x, y, z, mx, my, mz;
+  };
+  __device__ static void load(const AllPairsArgs<Real>& a, int64_t i, TData& t) {
+    R4 p = a.tpos[i];
+    R4 m = a.tmom[i];
+    t.x = p.x;
+    t.y = p.y;
+    t.z = p.z;
+    t.mx = m.x;
+    t.my = m.y;
+    t.mz = m.z;
+  }
+  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
+                              Real* acc) {
+    force_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc);
+  }
+  __device__ static void tile_out(const Real* acc, Real* o) {
+    const Real c = Real(kForceK);
+    o[0] = acc[0] * c;
+    o[1] = acc[1] * c;
+    o[2] = acc[2] * c;
+  }
+  // F = (sum_j T_ij) m_i + external part (magnetic_force.cu:968-980 by default;
+  // :583-603 with the naive path's extra mu0 when naive_quirks is set).
+  __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
+                                  const TData& t, const double* v) {
+    double f[3] = {v[0], v[1], v[2]};
+    if (a.rext[0]) {
+      // rext[c*3 + r] = column c, row r; the tensor is symmetric.
+      const double m[3] = {double(t.mx), double(t.my), double(t.mz)};
+      double e[3];
+      for (int r = 0; r < 3; ++r) {
+        e[r] = 0.0;
+        for (int c = 0; c < 3; ++c) e[r] += double(a.rext[c * 3 + r][i]) * m[c];
+      }
+      const double s = a.naive_quirks ? kMu0 : 1.0;
+      for (int r = 0; r < 3; ++r) f[r] += s * e[r];
+    }
+    a.out[0][i] = Real(f[0] * double(sc.scale));
+    a.out[1][i] = Real(f[1] * double(sc.scale));
+    a.out[2][i] = Real(f[2] * double(sc.scale));
+  }
+};
+
+template <class Real>
+struct TensorBody {
+  using R4 = typename Vec4T<Real>::type;
+  static constexpr int kAcc = 6;
+  static constexpr int kOut = 6;
+  struct TData {
+    Real x, y, z;
+  };
+  __device__ static void load(const AllPairsArgs<Real>& a, int64_t i, TData& t) {
+    R4 p = a.tpos[i];
+    t.x = p.x;
+    t.y = p.y;
+    t.z = p.z;
+  }
+  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
+                              Real* acc) {
+    tensor_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc);
+  }
+  __device__ static void tile_out(const Real* acc, Real* o) {
+    const Real c = Real(kForceK);
+    for (int k = 0; k < 6; ++k) o[k] = acc[k] * c;
+  }
+  // Writes the 3x3 in the reference's layout: out[c*3 + r] = T(row r, col c).
+  __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
+                                  const TData&, const double* v) {
+    const Real s = sc.scale;
+    const Real xx = Real(v[0]) * s, yy = Real(v[1]) * s, zz = Real(v[2]) * s;
+    const Real xy = Real(v[3]) * s, xz = Real(v[4]) * s, yz = Real(v[5]) * s;
+    a.out[0][i] = xx;
+    a.out[1][i] = xy;
+    a.out[2][i] = xz;
+    a.out[3][i] = xy;
+    a.out[4][i] = yy;
+    a.out[5][i] = yz;
+    a.out[6][i] = xz;
+    a.out[7][i] = yz;
+    a.out[8][i] = zz;
+  }
+};
+
+// ----------------------------------------------------------------------------
+// Step-space helpers.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ int64_t step_start(int64_t T, int64_t G, int64_t b) { return (T * b) / G; }
+// The CTA whose range holds step x: largest b with start(b) <= x.
+__device__ __forceinline__ int64_t step_owner(int64_t T, int64_t G, int64_t x) { return ((x + 1) * G - 1) / T; }
+
+template <class Real>
+__device__ __forceinline__ int find_scene(const SceneDesc<Real>* sc, int n, int64_t step) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (sc[mid].step_off <= step) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class Real, int TILE>
+struct StageLayout {
+  using R4 = typename Vec4T<Real>::type;
+  static constexpr int kBytes = 2 * TILE * int(sizeof(R4));
+};
+
+// ----------------------------------------------------------------------------
+// The kernel.
+// ----------------------------------------------------------------------------
+template <class Real, class Body, int TPB, int TPT, int TILE, int STAGES>
+__global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> a) {
+  using R4 = typename Vec4T<Real>::type;
+  constexpr int TBT = TPB * TPT;
+  constexpr int kAcc = Body::kAcc;
+  constexpr int kOut = Body::kOut;
+  constexpr bool kComp = sizeof(Real) == 4;  // compensate FP32 running sums
+
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ int s_flag;
+
+  const int tid = threadIdx.x;
+  const int64_t T = a.total_steps;
+  const int64_t G = gridDim.x;
+  const int64_t b = blockIdx.x;
+  const int64_t k_begin = step_start(T, G, b);
+  const int64_t k_end = step_start(T, G, b + 1);
+  if (k_begin >= k_end) return;
+  // A single-scene launch whose solve has already stopped does nothing.
+  if (a.done_flags && a.n_scenes == 1 && a.done_flags[0] != 0.0) return;
+
+  R4* stage_pos[STAGES];
+  R4* stage_mom[STAGES];
+#pragma unroll
+  for (int s = 0; s < STAGES; ++s) {
+    stage_pos[s] = reinterpret_cast<R4*>(smem_raw + s * StageLayout<Real, TILE>::kBytes);
+    stage_mom[s] = stage_pos[s] + TILE;
+  }
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full_bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // Producer (thread 0): stage the source tile of step k into stage s.
+  auto issue = [&](int64_t k, int s) {
+    const int si = find_scene(a.scenes, a.n_scenes, k);
+    const SceneDesc<Real>& sc = a.scenes[si];
+    const int64_t local = k - sc.step_off;
+    const int tile = int(local % sc.n_tiles);
+    const int64_t first = sc.s_off + int64_t(tile) * TILE;
+    const int64_t rem = sc.ns - int64_t(tile) * TILE;
+    const uint32_t cnt = uint32_t(rem < TILE ? rem : TILE);
+    const uint32_t bytes = cnt * uint32_t(sizeof(R4));
+    mbar_arrive_expect_tx(&full_bar[s], 2 * bytes);
+    bulk_g2s(stage_pos[s], a.spos + first, bytes, &full_bar[s]);
+    bulk_g2s(stage_mom[s], a.smom + first, bytes, &full_bar[s]);
+  };
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES && k_begin + s < k_end; ++s) issue(k_begin + s, s);
+  }
+
+  // Walk state.
+  int si = find_scene(a.scenes, a.n_scenes, k_begin);
+  int64_t local = k_begin - a.scenes[si].step_off;
+  int tb = int(local / a.scenes[si].n_tiles);
+  int tile = int(local % a.scenes[si].n_tiles);
+  bool seg_from_start = (tile == 0);
+  bool first_tb_of_cta = true;
+
+  typename Body::TData td[TPT];
+  Real run[TPT][kOut];
+  Real cmp[TPT][kOut];
+
+  auto load_targets = [&](const SceneDesc<Real>& sc, int tbl) {
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+      int64_t li = int64_t(tbl) * TBT + t * TPB + tid;
+      if (li >= sc.nt) li = sc.nt - 1;
+      Body::load(a, sc.t_off + li, td[t]);
+#pragma unroll
+      for (int o = 0; o < kOut; ++o) {
+        run[t][o] = Real(0);
+        cmp[t][o] = Real(0);
+      }
+    }
+  };
+  load_targets(a.scenes[si], tb);
+
+  int64_t k_fail = -1;
+  for (int64_t k = k_begin; k < k_end; ++k) {
+    const int64_t u = k - k_begin;
+    const int s = int(u % STAGES);
+    const uint32_t parity = uint32_t((u / STAGES) & 1);
+    const SceneDesc<Real>& sc = a.scenes[si];
+    const PairConsts<Real> pc = sc.pc;
+
+    const bool ok = mbar_wait_bounded(&full_bar[s], parity);
+    if (__syncthreads_or(!ok)) {
+      k_fail = k;
+      break;
+    }
+    const bool skip_scene = a.done_flags && a.done_flags[int64_t(si) * a.done_stride] != 0.0;
+
+    // Sweep the tile.
+    if (!skip_scene) {
+      const int64_t rem = sc.ns - int64_t(tile) * TILE;
+      const int cnt = int(rem < TILE ? rem : TILE);
+      const R4* __restrict__ sp = stage_pos[s];
+      const R4* __restrict__ sm = stage_mom[s];
+      Real acc[TPT][kAcc];
+#pragma unroll
+      for (int t = 0; t < TPT; ++t)
+#pragma unroll
+        for (int q = 0; q < kAcc; ++q) acc[t][q] = Real(0);
+#pragma unroll 4
+      for (int j = 0; j < cnt; ++j) {
+        const R4 p = sp[j];
+        const R4 m = sm[j];
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) Body::pair(td[t], p, m, pc, acc[t]);
+      }
+#pragma unroll
+      for (int t = 0; t < TPT; ++t) {
+        Real o[kOut];
+        Body::tile_out(acc[t], o);
+#pragma unroll
+        for (int q = 0; q < kOut; ++q) {
+          if constexpr (kComp) comp_add(run[t][q], cmp[t][q], o[q]);
+          else run[t][q] += o[q];
+        }
+      }
+    }
+
+    __syncthreads();  // every thread is done with stage s
+    if (tid == 0 && k + STAGES < k_end) {
+      fence_proxy_async_smem();
+      issue(k + STAGES, s);
+    }
+
+    // Advance; flush when this target block's segment ends.
+    const bool last_tile = (tile == sc.n_tiles - 1);
+    const bool last_step = (k == k_end - 1);
+    if (last_tile || last_step) {
+      const int64_t gtb = sc.tb_off + tb;
+      const bool full = seg_from_start && last_tile;
+      if (skip_scene) {
+        // nothing to write for a stopped scene
+      } else if (full) {
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+          const int64_t li = int64_t(tb) * TBT + t * TPB + tid;
+          if (li < sc.nt) {
+            double v[kOut];
+#pragma unroll
+            for (int q = 0; q < kOut; ++q) v[q] = double(run[t][q]) + double(cmp[t][q]);
+            Body::epilogue(a, sc, sc.t_off + li, td[t], v);
+          }
+        }
+      } else {
+        const int slot = first_tb_of_cta ? 0 : 1;
+        double* part = a.partials + ((b * 2 + slot) * TBT) * kOut;
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+          const int li = t * TPB + tid;
+#pragma unroll
+          for (int q = 0; q < kOut; ++q) part[li * kOut + q] = double(run[t][q]) + double(cmp[t][q]);
+        }
+        __threadfence();
+        __syncthreads();
+        const int64_t sa = sc.step_off + int64_t(tb) * sc.n_tiles;
+        const int64_t se = sa + sc.n_tiles;
+        const int64_t b_first = step_owner(T, G, sa);
+        const int64_t b_last = step_owner(T, G, se - 1);
+        if (tid == 0) {
+          const int nseg = int(b_last - b_first + 1);
+          const int ticket = atomicAdd(&a.counters[gtb], 1);
+          s_flag = (ticket == nseg - 1);
+        }
+        __syncthreads();
+        if (s_flag) {
+          __threadfence();
+          const bool first_split = step_start(T, G, b_first) < sa;
+#pragma unroll
+          for (int t = 0; t < TPT; ++t) {
+            const int li = t * TPB + tid;
+            double v[kOut];
+#pragma unroll
+            for (int q = 0; q < kOut; ++q) v[q] = 0.0;
+            for (int64_t bb = b_first; bb <= b_last; ++bb) {
+              const int sl = (bb == b_first && first_split) ? 1 : 0;
+              const double* pp = a.partials + ((bb * 2 + sl) * TBT) * kOut;
+#pragma unroll
+              for (int q = 0; q < kOut; ++q) v[q] += __ldcg(&pp[li * kOut + q]);
+            }
+            const int64_t gi = int64_t(tb) * TBT + li;
+            if (gi < sc.nt) Body::epilogue(a, sc, sc.t_off + gi, td[t], v);
+          }
+          if (tid == 0) a.counters[gtb] = 0;
+        }
+      }
+      // Next target block (possibly in the next scene).
+      if (!last_step) {
+        first_tb_of_cta = false;
+        seg_from_start = true;
+        tile = 0;
+        ++tb;
+        if (tb == sc.n_tb) {
+          tb = 0;
+          ++si;
+        }
+        load_targets(a.scenes[si], tb);
+      }
+    } else {
+      ++tile;
+    }
+  }
+
+  if (k_fail >= 0) {
+    if (tid == 0) {
+      atomicExch(a.err, MF_DEVERR_STAGE_TIMEOUT);
+      // Copies in flight: steps k_fail .. min(k_end, k_fail + STAGES) - 1, one
+      // per stage.  Wait for each (bounded) before the CTA leaves.
+      const int64_t k_stop = (k_fail + STAGES < k_end) ? k_fail + STAGES : k_end;
+      bool drained = true;
+      for (int64_t kk = k_fail; kk < k_stop; ++kk) {
+        const int64_t uu = kk - k_begin;
+        if (!mbar_wait_bounded(&full_bar[uu % STAGES], uint32_t((uu / STAGES) & 1))) drained = false;
+      }
+      if (!drained) atomicExch(a.err, MF_DEVERR_DRAIN_TIMEOUT);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace mfgb

@@ -1,0 +1,121 @@
+// mf_device.cuh -- sm_103a device helpers: bulk-copy staging through mbarriers,
+// approximate reciprocal square root, compensated summation.
+//
+// Every spin-wait here is bounded.  A wait that runs out returns false; the
+// caller records MF_DEVERR_* in the launch's error word and leaves the kernel
+// after draining its own copies, so a stuck copy can never hang the GPU.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mfgb {
+
+// Device-side error codes written to the error word a launch is given.
+enum : int {
+  MF_DEVERR_NONE = 0,
+  MF_DEVERR_STAGE_TIMEOUT = 1,   // a source tile never arrived in shared memory
+  MF_DEVERR_DRAIN_TIMEOUT = 2,   // copies still in flight when leaving after an error
+};
+
+// Try-wait iterations before a staging wait gives up.  Each try_wait blocks
+// for a hardware-defined slice (~microseconds), so this bounds a wait at well
+// under a second.
+constexpr uint32_t kWaitLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Make mbarrier initialisation visible to the async (bulk-copy) proxy.
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion signalled on `bar` as tx bytes.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// rsqrt.approx.ftz.f32: hardware reciprocal square root (MUFU), relative error
+// below 2^-22 per the PTX ISA.  rsqrt(+0) = +inf, which callers never feed
+// into a product that survives (near pairs take the exact branch).
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Knuth's two-sum: s + e == a + b exactly (round-to-nearest, no FMA
+// contraction: the intrinsics pin each operation to one rounding).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Running compensated accumulator: adds one block-sum `x` to (s, c).
+__device__ __forceinline__ void comp_add(float& s, float& c, float x) {
+  float t, e;
+  two_sum(s, x, t, e);
+  s = t;
+  c = __fadd_rn(c, e);
+}
+
+// Packed 4-wide particle record (x, y, z, pad): 16 B for FP32, 32 B for FP64,
+// so a tile of them is one contiguous, 16-byte-aligned bulk copy.
+struct alignas(32) dbl4 {
+  double x, y, z, w;
+};
+template <class Real>
+struct Vec4T;
+template <>
+struct Vec4T<float> {
+  using type = float4;
+};
+template <>
+struct Vec4T<double> {
+  using type = dbl4;
+};
+
+}  // namespace mfgb

@@ -1,0 +1,1025 @@
+// mf_engine.cu -- the solver object behind the C ABI (include/mf.h).
+//
+// Engine<Real> owns one object's particle state on one device and runs the
+// reference's magnetization-and-force step on it:
+//   eval_hext   magnetic_force.cu:1102-1192   external field + gradient tensor
+//   solve       magnetic_force.cu:874-1095    NLCG (reference) or CG
+//   force       magnetic_force.cu:890-997     Kelvin force
+// Hot products go through the all-pairs kernel (mf_allpairs.cuh); vector
+// updates and FP64 inner products through mf_vec.cuh.  Published results are
+// device SoA float arrays like the reference's cuda_abstract_vector members.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "mf_internal.h"
+#include "mf_vec.cuh"
+
+namespace mfgb {
+
+const char* last_error_cstr();
+
+// ---------------------------------------------------------------------------
+// Elementwise kernels
+// ---------------------------------------------------------------------------
+template <class Real, class R4>
+__global__ void k_pack_positions(const float* __restrict__ src, int layout, int64_t n, R4* __restrict__ pos4,
+                                 float* __restrict__ xf, float* __restrict__ yf, float* __restrict__ zf,
+                                 int32_t* __restrict__ bad) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    float x, y, z;
+    if (layout == MF_LAYOUT_AOS) {
+      x = src[3 * i];
+      y = src[3 * i + 1];
+      z = src[3 * i + 2];
+    } else {
+      x = src[i];
+      y = src[n + i];
+      z = src[2 * n + i];
+    }
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicExch(bad, 1);
+    R4 p;
+    p.x = Real(x);
+    p.y = Real(y);
+    p.z = Real(z);
+    p.w = Real(0);
+    pos4[i] = p;
+    if (xf) {
+      xf[i] = x;
+      yf[i] = y;
+      zf[i] = z;
+    }
+  }
+}
+
+template <class Real, class R4>
+__global__ void k_fill_hext(int64_t n, Real hx, Real hy, Real hz, R4* __restrict__ hext4, Real* __restrict__ ox,
+                            Real* __restrict__ oy, Real* __restrict__ oz) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    R4 v;
+    v.x = hx;
+    v.y = hy;
+    v.z = hz;
+    v.w = Real(0);
+    hext4[i] = v;
+    ox[i] = hx;
+    oy[i] = hy;
+    oz[i] = hz;
+  }
+}
+
+// total_B_over_mu0 = b, M = c b (SoA), and the packed dipoles of the force pass.
+template <class Real, class R4>
+__global__ void k_publish_b(int64_t n, Real c, const R4* __restrict__ b4, Real* __restrict__ bx,
+                            Real* __restrict__ by, Real* __restrict__ bz, Real* __restrict__ mx,
+                            Real* __restrict__ my, Real* __restrict__ mz, R4* __restrict__ mom4) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const R4 b = b4[i];
+    bx[i] = b.x;
+    by[i] = b.y;
+    bz[i] = b.z;
+    R4 m;
+    m.x = c * b.x;
+    m.y = c * b.y;
+    m.z = c * b.z;
+    m.w = Real(0);
+    mx[i] = m.x;
+    my[i] = m.y;
+    mz[i] = m.z;
+    mom4[i] = m;
+  }
+}
+
+// Symplectic Euler: v += dt F / m_p ; x += dt v   (unit density, m_p = V).
+template <class Real, class R4>
+__global__ void k_integrate(int64_t n, Real dt, Real inv_mass, const Real* __restrict__ fx,
+                            const Real* __restrict__ fy, const Real* __restrict__ fz, R4* __restrict__ vel4,
+                            R4* __restrict__ pos4, float* __restrict__ xf, float* __restrict__ yf,
+                            float* __restrict__ zf) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    R4 v = vel4[i];
+    R4 p = pos4[i];
+    v.x += dt * fx[i] * inv_mass;
+    v.y += dt * fy[i] * inv_mass;
+    v.z += dt * fz[i] * inv_mass;
+    p.x += dt * v.x;
+    p.y += dt * v.y;
+    p.z += dt * v.z;
+    vel4[i] = v;
+    pos4[i] = p;
+    xf[i] = float(p.x);
+    yf[i] = float(p.y);
+    zf[i] = float(p.z);
+  }
+}
+
+template <class Real>
+__global__ void k_to_float(int64_t n, const Real* __restrict__ src, float* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    dst[i] = float(src[i]);
+}
+
+template <class R4>
+__global__ void k_copy4(int64_t n, const R4* __restrict__ src, R4* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+}
+
+__global__ void k_init_row(double* row, double tol, double maxit) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    for (int k = 0; k < kScal; ++k) row[k] = 0.0;
+    row[S_TOL] = tol;
+    row[S_MAXIT] = maxit;
+  }
+}
+
+__global__ void k_set_scalar(double* row, int idx, double v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) row[idx] = v;
+}
+
+static inline unsigned grid_1d(int64_t n, int sms) {
+  int64_t g = (n + 255) / 256;
+  const int64_t cap = int64_t(sms) * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return unsigned(g);
+}
+
+// ---------------------------------------------------------------------------
+// Engine interface (type-erased for the C ABI)
+// ---------------------------------------------------------------------------
+struct EngineBase {
+  virtual ~EngineBase() = default;
+  virtual mf_status init(const mf_params& p) = 0;
+  virtual mf_status set_positions(const float* xyz, int64_t n, int layout, int where) = 0;
+  virtual mf_status set_external(const float* H0, const float* sp, const float* sm, int64_t ns, float hext) = 0;
+  virtual mf_status solve(int64_t niter, int64_t* iters, double* err) = 0;
+  virtual mf_status eval_force() = 0;
+  virtual mf_status advance(double dt, int64_t niter, int64_t* iters) = 0;
+  virtual mf_status get(int q, void* dst, int layout, int where, bool f64) = 0;
+  virtual mf_status device_soa(int q, float** x, float** y, float** z) = 0;
+  virtual mf_status set_option(int key, double v) = 0;
+  virtual mf_status get_option(int key, double* v) = 0;
+  virtual int64_t np() const = 0;
+  virtual const std::vector<double>& history() const = 0;
+  virtual mf_counters& counters() = 0;
+  virtual void set_stream(cudaStream_t s) = 0;
+  virtual cudaStream_t stream() const = 0;
+  int device = 0;
+};
+
+template <class Real>
+class Engine final : public EngineBase {
+  using R4 = typename Vec4T<Real>::type;
+  static constexpr bool kF32 = sizeof(Real) == 4;
+
+ public:
+  ~Engine() override {
+    if (pinned_) cudaFreeHost(pinned_);
+  }
+
+  mf_status init(const mf_params& p) override {
+    if (p.num_particles <= 0) return fail(MF_ERR_INVALID_ARG, "num_particles must be > 0");
+    if (!p.target_pos) return fail(MF_ERR_INVALID_ARG, "target_pos is NULL");
+    if (!(p.h > 0.f) || !std::isfinite(p.h)) return fail(MF_ERR_INVALID_ARG, "h must be finite and > 0");
+    if (!(p.volume > 0.f) || !std::isfinite(p.volume)) return fail(MF_ERR_INVALID_ARG, "volume must be > 0");
+    if (!std::isfinite(p.chi) || p.chi <= -1.f) return fail(MF_ERR_INVALID_ARG, "chi must be finite and > -1");
+    if (p.n_ext < 0) return fail(MF_ERR_INVALID_ARG, "n_ext < 0");
+    h_ = p.h;
+    ext_h_ = p.ext_mag_h;
+    volume_ = p.volume;
+    chi_ = p.chi;
+    for (int k = 0; k < 3; ++k) H0_[k] = p.const_ext_field[k];
+    rel_tol_ = kF32 ? 1e-6 : 1e-8;
+    sms_ = device_sms(device);
+    MF_CUDA_TRY(cudaMallocHost(&pinned_, 4096));
+    MF_TRY(scal_.reserve(kScal * sizeof(double), false, true));
+    MF_TRY(red_part_.reserve(size_t(sms_) * 8 * 4 * sizeof(double)));
+    MF_TRY(red_ticket_.reserve(64, false, true));
+    MF_TRY(range_.reserve(sizeof(VecRange)));
+    MF_TRY(bad_.reserve(16, false, true));
+    MF_TRY(set_positions(p.target_pos, p.num_particles, MF_LAYOUT_AOS, MF_HOST));
+    MF_TRY(set_external(p.const_ext_field, p.ext_source_pos, p.ext_source_M, p.n_ext, p.ext_mag_h));
+    return MF_OK;
+  }
+
+  void set_stream(cudaStream_t s) override { st_ = s; }
+  cudaStream_t stream() const override { return st_; }
+  int64_t np() const override { return np_; }
+  const std::vector<double>& history() const override { return history_; }
+  mf_counters& counters() override { return ctr_; }
+
+  // ---- setTargetpos / Resize ---------------------------------------------
+  mf_status set_positions(const float* xyz, int64_t n, int layout, int where) override {
+    if (n <= 0) return fail(MF_ERR_INVALID_ARG, "particle count must be > 0");
+    if (!xyz) return fail(MF_ERR_INVALID_ARG, "positions pointer is NULL");
+    if (layout != MF_LAYOUT_AOS && layout != MF_LAYOUT_SOA) return fail(MF_ERR_INVALID_ARG, "bad layout");
+    if (where != MF_HOST && where != MF_DEVICE) return fail(MF_ERR_INVALID_ARG, "bad memory kind");
+    if (where == MF_HOST) {
+      for (int64_t i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(xyz[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
+    }
+    const int64_t old = np_;
+    MF_TRY(resize(n));
+    const float* src = xyz;
+    if (where == MF_HOST) {
+      MF_TRY(staging_.reserve(size_t(3 * n) * sizeof(float)));
+      MF_CUDA_TRY(cudaMemcpyAsync(staging_.ptr, xyz, size_t(3 * n) * sizeof(float), cudaMemcpyHostToDevice, st_));
+      src = staging_.template as<float>();
+    }
+    MF_CUDA_TRY(cudaMemsetAsync(bad_.ptr, 0, sizeof(int32_t), st_));
+    k_pack_positions<Real, R4><<<grid_1d(n, sms_), 256, 0, st_>>>(src, layout, n, pos4(), pubf(MF_Q_POSITIONS, 0),
+                                                                    pubf(MF_Q_POSITIONS, 1),
+                                                                    pubf(MF_Q_POSITIONS, 2), bad_.template as<int32_t>());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    if (where == MF_DEVICE) {
+      int32_t bad = 0;
+      MF_CUDA_TRY(cudaMemcpyAsync(&bad, bad_.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+      MF_CUDA_TRY(cudaStreamSynchronize(st_));
+      if (bad) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
+    }
+    if (old != n || !plans_ready_) {
+      MF_TRY(build_plans());
+      // Resize keeps the warm start visible in total_B_over_mu0 (magnetic_force.cu:735-741).
+      MF_TRY(publish_b());
+    }
+    return MF_OK;
+  }
+
+  // ---- setHext -------------------------------------------------------------
+  mf_status set_external(const float* H0, const float* sp, const float* sm, int64_t ns, float hext) override {
+    if (ns < 0) return fail(MF_ERR_INVALID_ARG, "n_src < 0");
+    if (ns > 0 && (!sp || !sm)) return fail(MF_ERR_INVALID_ARG, "external sources are NULL");
+    if (H0)
+      for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(H0[k])) return fail(MF_ERR_INVALID_ARG, "non-finite external field");
+        H0_[k] = H0[k];
+      }
+    if (ns > 0 && !(hext > 0.f)) return fail(MF_ERR_INVALID_ARG, "ext_mag_h must be > 0");
+    for (int64_t i = 0; i < 3 * ns; ++i)
+      if (!std::isfinite(sp[i]) || !std::isfinite(sm[i])) return fail(MF_ERR_INVALID_ARG, "non-finite source");
+    ext_h_ = hext;
+    n_ext_ = ns;
+    if (ns > 0) {
+      MF_TRY(ext_pos4_.reserve(size_t(ns) * sizeof(R4)));
+      MF_TRY(ext_mom4_.reserve(size_t(ns) * sizeof(R4)));
+      MF_TRY(ext_soa_.reserve(size_t(6 * ns) * sizeof(float)));
+      MF_TRY(staging_.reserve(size_t(3 * ns) * sizeof(float)));
+      MF_CUDA_TRY(cudaMemcpyAsync(staging_.ptr, sp, size_t(3 * ns) * sizeof(float), cudaMemcpyHostToDevice, st_));
+      k_pack_positions<Real, R4><<<grid_1d(ns, sms_), 256, 0, st_>>>(
+          staging_.template as<float>(), MF_LAYOUT_AOS, ns, ext_pos4_.template as<R4>(), ext_soa_.template as<float>(),
+          ext_soa_.template as<float>() + ns, ext_soa_.template as<float>() + 2 * ns, bad_.template as<int32_t>());
+      MF_CUDA_TRY(cudaGetLastError());
+      MF_CUDA_TRY(cudaStreamSynchronize(st_));
+      MF_CUDA_TRY(cudaMemcpyAsync(staging_.ptr, sm, size_t(3 * ns) * sizeof(float), cudaMemcpyHostToDevice, st_));
+      k_pack_positions<Real, R4><<<grid_1d(ns, sms_), 256, 0, st_>>>(
+          staging_.template as<float>(), MF_LAYOUT_AOS, ns, ext_mom4_.template as<R4>(), ext_soa_.template as<float>() + 3 * ns,
+          ext_soa_.template as<float>() + 4 * ns, ext_soa_.template as<float>() + 5 * ns, bad_.template as<int32_t>());
+      MF_CUDA_TRY(cudaGetLastError());
+      MF_CUDA_TRY(cudaStreamSynchronize(st_));
+      ctr_.kernel_launches += 2;
+    }
+    if (np_ > 0) MF_TRY(build_ext_plans());
+    return MF_OK;
+  }
+
+  // ---- eval_hext -------------------------------------------------------------
+  mf_status eval_hext() {
+    if (n_ext_ == 0) {
+      k_fill_hext<Real, R4><<<grid_1d(np_, sms_), 256, 0, st_>>>(np_, Real(H0_[0]), Real(H0_[1]), Real(H0_[2]),
+                                                                  hext4(), pubr(MF_Q_HEXT, 0), pubr(MF_Q_HEXT, 1),
+                                                                  pubr(MF_Q_HEXT, 2));
+      MF_CUDA_TRY(cudaGetLastError());
+      ++ctr_.kernel_launches;
+      rext_zero_ = true;
+    } else {
+      LaunchIO<Real> io;
+      io.tpos = pos4();
+      io.spos = ext_pos4_.template as<R4>();
+      io.smom = ext_mom4_.template as<R4>();
+      for (int k = 0; k < 3; ++k) io.out[k] = pubr(MF_Q_HEXT, k);
+      io.out4 = hext4();
+      MF_TRY(run(plan_ext_field_, io));
+      LaunchIO<Real> it;
+      it.tpos = pos4();
+      it.spos = ext_pos4_.template as<R4>();
+      it.smom = ext_mom4_.template as<R4>();
+      for (int k = 0; k < 9; ++k) it.out[k] = rext(k);
+      MF_TRY(run(plan_ext_tensor_, it));
+      rext_zero_ = false;
+    }
+    if (rext_zero_)
+      for (int q = MF_Q_DHEXTDX; q <= MF_Q_DHEXTDZ; ++q)
+        MF_CUDA_TRY(cudaMemsetAsync(pub_r_[q].ptr, 0, size_t(3 * np_) * sizeof(Real), st_));
+    if (!kF32) {
+      publish_f(MF_Q_HEXT);
+      for (int q = MF_Q_DHEXTDX; q <= MF_Q_DHEXTDZ; ++q) publish_f(q);
+    }
+    return MF_OK;
+  }
+
+  // ---- solve -----------------------------------------------------------------
+  mf_status solve(int64_t niter, int64_t* iters, double* err) override {
+    if (niter < 0) return fail(MF_ERR_INVALID_ARG, "niter < 0");
+    history_.clear();
+    MF_TRY(eval_hext());
+    mf_status st = (solver_ == MF_SOLVER_CG) ? solve_cg(niter, iters, err) : solve_nlcg(niter, iters, err);
+    if (st != MF_OK && st != MF_ERR_NOT_CONVERGED) return st;
+    MF_TRY(publish_b());
+    MF_TRY(scr_.check(st_));
+    return st;
+  }
+
+  // ---- evaluate_fitted_near_foece ----------------------------------------------
+  mf_status eval_force() override {
+    MF_TRY(publish_b());  // M = c b (magnetic_force.cu:899, :915)
+    LaunchIO<Real> io;
+    io.tpos = pos4();
+    io.tmom = mom4();
+    io.spos = pos4();
+    io.smom = mom4();
+    for (int k = 0; k < 3; ++k) io.out[k] = pubr(MF_Q_FORCE, k);
+    if (!rext_zero_)
+      for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
+    io.naive_quirks = naive_ ? 1 : 0;
+    MF_TRY(run(plan_force_, io));
+    ctr_.force_passes += 1;
+    ctr_.force_pairs += plan_force_.pairs;
+    if (!kF32) publish_f(MF_Q_FORCE);
+    MF_TRY(scr_.check(st_));
+    return MF_OK;
+  }
+
+  mf_status advance(double dt, int64_t niter, int64_t* iters) override {
+    if (!std::isfinite(dt)) return fail(MF_ERR_INVALID_ARG, "dt must be finite");
+    mf_status s = solve(niter, iters, nullptr);
+    if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
+    MF_TRY(eval_force());
+    k_integrate<Real, R4><<<grid_1d(np_, sms_), 256, 0, st_>>>(
+        np_, Real(dt), Real(1.0 / volume_), pubr(MF_Q_FORCE, 0), pubr(MF_Q_FORCE, 1), pubr(MF_Q_FORCE, 2),
+        vel4(), pos4(), pubf(MF_Q_POSITIONS, 0), pubf(MF_Q_POSITIONS, 1), pubf(MF_Q_POSITIONS, 2));
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    return s;
+  }
+
+  // ---- results -----------------------------------------------------------------
+  mf_status get(int q, void* dst, int layout, int where, bool f64) override {
+    if (q < 0 || q > MF_Q_VELOCITY) return fail(MF_ERR_INVALID_ARG, "unknown quantity");
+    if (!dst) return fail(MF_ERR_INVALID_ARG, "dst is NULL");
+    if (layout != MF_LAYOUT_AOS && layout != MF_LAYOUT_SOA) return fail(MF_ERR_INVALID_ARG, "bad layout");
+    if (where != MF_HOST && where != MF_DEVICE) return fail(MF_ERR_INVALID_ARG, "bad memory kind");
+    const int64_t n = np_;
+    // Gather the three SoA components into a device staging buffer first.
+    const size_t esz = f64 ? sizeof(double) : sizeof(float);
+    MF_TRY(staging_.reserve(size_t(3 * n) * sizeof(double)));
+    MF_TRY(staging2_.reserve(size_t(3 * n) * sizeof(double)));
+    char* soa = staging2_.template as<char>();
+    for (int k = 0; k < 3; ++k) MF_TRY(component_to(q, k, soa + size_t(k * n) * esz, f64));
+    void* dev_out = staging_.ptr;
+    if (layout == MF_LAYOUT_SOA) {
+      dev_out = soa;
+    } else {
+      // SoA -> AoS on the device.
+      if (f64)
+        MF_TRY(soa_to_aos<double>(reinterpret_cast<const double*>(soa), staging_.template as<double>(), n));
+      else
+        MF_TRY(soa_to_aos<float>(reinterpret_cast<const float*>(soa), staging_.template as<float>(), n));
+    }
+    const size_t bytes = size_t(3 * n) * esz;
+    MF_CUDA_TRY(cudaMemcpyAsync(dst, dev_out, bytes,
+                                where == MF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st_));
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    return MF_OK;
+  }
+
+  mf_status device_soa(int q, float** x, float** y, float** z) override {
+    if (q < 0 || q > MF_Q_DHEXTDZ) return fail(MF_ERR_INVALID_ARG, "unknown quantity");
+    if (x) *x = pubf(q, 0);
+    if (y) *y = pubf(q, 1);
+    if (z) *z = pubf(q, 2);
+    return MF_OK;
+  }
+
+  mf_status set_option(int key, double v) override {
+    if (!std::isfinite(v)) return fail(MF_ERR_INVALID_ARG, "option value must be finite");
+    switch (key) {
+      case MF_OPT_TOLERANCE: tolerance_ = v; return MF_OK;
+      case MF_OPT_MAX_ITERATION:
+        if (v < 0) return fail(MF_ERR_INVALID_ARG, "max_iteration < 0");
+        max_iteration_ = int64_t(v);
+        return MF_OK;
+      case MF_OPT_NAIVE: {
+        const bool nv = v != 0.0;
+        if (nv != naive_) {
+          naive_ = nv;
+          MF_TRY(build_ext_plans());
+        }
+        return MF_OK;
+      }
+      case MF_OPT_SOLVER:
+        if (v != MF_SOLVER_NLCG && v != MF_SOLVER_CG) return fail(MF_ERR_INVALID_ARG, "unknown solver");
+        solver_ = int(v);
+        return MF_OK;
+      case MF_OPT_REL_TOL:
+        if (!(v > 0)) return fail(MF_ERR_INVALID_ARG, "rel_tol must be > 0");
+        rel_tol_ = v;
+        return MF_OK;
+      case MF_OPT_CG_MAX_ITER:
+        if (v < 0) return fail(MF_ERR_INVALID_ARG, "cg max iterations < 0");
+        cg_max_iter_ = int64_t(v);
+        return MF_OK;
+      case MF_OPT_CRIT_SIZE: crit_size_ = int(v); return MF_OK;
+      case MF_OPT_CHECK_INTERVAL:
+        if (v < 1) return fail(MF_ERR_INVALID_ARG, "check interval must be >= 1");
+        check_interval_ = int(v);
+        return MF_OK;
+      default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
+    }
+  }
+
+  mf_status get_option(int key, double* v) override {
+    if (!v) return fail(MF_ERR_INVALID_ARG, "value pointer is NULL");
+    switch (key) {
+      case MF_OPT_TOLERANCE: *v = tolerance_; return MF_OK;
+      case MF_OPT_MAX_ITERATION: *v = double(max_iteration_); return MF_OK;
+      case MF_OPT_NAIVE: *v = naive_ ? 1.0 : 0.0; return MF_OK;
+      case MF_OPT_SOLVER: *v = solver_; return MF_OK;
+      case MF_OPT_REL_TOL: *v = rel_tol_; return MF_OK;
+      case MF_OPT_CG_MAX_ITER: *v = double(cg_max_iter_); return MF_OK;
+      case MF_OPT_CRIT_SIZE: *v = crit_size_; return MF_OK;
+      case MF_OPT_CHECK_INTERVAL: *v = check_interval_; return MF_OK;
+      default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
+    }
+  }
+
+ private:
+  // Buffers ---------------------------------------------------------------
+  // Packed vectors (R4 x np): positions, velocities, solver vectors.
+  enum Vec4Id { V_POS, V_VEL, V_B, V_HEXT, V_MOM, V_R, V_P, V_Q, V_G, V_GOLD, V_D, V_DOLD, V_DD, kVec4 };
+  DevBuf vec4_[kVec4];
+  // Published SoA quantities in Real (9 x np for the tensors, 3 x np else).
+  DevBuf pub_r_[MF_Q_VELOCITY + 1];
+  // FP64 engines keep float copies of the published quantities.
+  DevBuf pub_f_[MF_Q_VELOCITY + 1];
+  DevBuf ext_pos4_, ext_mom4_, ext_soa_;
+  DevBuf staging_, staging2_;
+  DevBuf scal_, red_part_, red_ticket_, range_, bad_;
+  Scratch scr_;
+  Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_;
+  bool plans_ready_ = false;
+  bool rext_zero_ = true;
+
+  R4* v4(int id) const { return vec4_[id].template as<R4>(); }
+  R4* pos4() const { return v4(V_POS); }
+  R4* vel4() const { return v4(V_VEL); }
+  R4* hext4() const { return v4(V_HEXT); }
+  R4* mom4() const { return v4(V_MOM); }
+  Real* pubr(int q, int k) const {
+    return pub_r_[q].template as<Real>() ? pub_r_[q].template as<Real>() + size_t(k) * size_t(np_) : nullptr;
+  }
+  Real* rext(int k) const {  // k = c*3 + r, 9 SoA arrays in pub_r_[MF_Q_DHEXTDX..DZ]
+    return pubr(MF_Q_DHEXTDX + k / 3, k % 3);
+  }
+  float* pubf(int q, int k) const {
+    if (q == MF_Q_POSITIONS) return pub_f_[q].template as<float>() + size_t(k) * size_t(np_);
+    if constexpr (kF32) return reinterpret_cast<float*>(pubr(q, k));
+    return pub_f_[q].template as<float>() + size_t(k) * size_t(np_);
+  }
+
+  mf_status resize(int64_t n) {
+    if (n == np_) return MF_OK;
+    const int64_t old = np_;
+    const int64_t keep_n = old < n ? old : n;
+    // Warm start: keep the first min(old, n) entries of b (magnetic_force.cu:735-741).
+    DevBuf nb;
+    MF_TRY(nb.reserve(size_t(n) * sizeof(R4), false, true));
+    if (keep_n > 0 && vec4_[V_B].ptr)
+      MF_CUDA_TRY(cudaMemcpyAsync(nb.ptr, vec4_[V_B].ptr, size_t(keep_n) * sizeof(R4), cudaMemcpyDeviceToDevice, st_));
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    vec4_[V_B] = std::move(nb);
+    for (int id = 0; id < kVec4; ++id) {
+      if (id == V_B) continue;
+      vec4_[id].release();
+      MF_TRY(vec4_[id].reserve(size_t(n) * sizeof(R4), false, true));
+    }
+    for (int q = 0; q <= MF_Q_VELOCITY; ++q) {
+      pub_r_[q].release();
+      pub_f_[q].release();
+      const bool tensor_part = (q >= MF_Q_DHEXTDX && q <= MF_Q_DHEXTDZ);
+      (void)tensor_part;
+      if (q != MF_Q_POSITIONS && q != MF_Q_VELOCITY) MF_TRY(pub_r_[q].reserve(size_t(3 * n) * sizeof(Real), false, true));
+      if (q == MF_Q_POSITIONS || !kF32) MF_TRY(pub_f_[q].reserve(size_t(3 * n) * sizeof(float), false, true));
+    }
+    np_ = n;
+    VecRange rg{0, n};
+    MF_CUDA_TRY(cudaMemcpy(range_.ptr, &rg, sizeof(rg), cudaMemcpyHostToDevice));
+    plans_ready_ = false;
+    return MF_OK;
+  }
+
+  double c_coef() const { return double(volume_) * double(chi_) / (double(chi_) + 1.0); }
+
+  mf_status build_plans() {
+    const double c = c_coef();
+    SceneSpec base;
+    base.t_off = 0;
+    base.nt = np_;
+    base.s_off = 0;
+    base.ns = np_;
+    base.h = h_;
+    // residual r = c G(b) + Hext - b   (magnetic_force.cu:1016-1017)
+    SceneSpec s = base;
+    s.scale = c;
+    s.coef_add = 1.0;
+    s.coef_add2 = -1.0;
+    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_resid_));
+    // gradient g = c G(r) - r            (D_transpose, :1281-1284)
+    // D(d) = c G(d) - d                  (D, :1275-1278)
+    s = base;
+    s.scale = c;
+    s.coef_add = -1.0;
+    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_grad_));
+    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_dd_));
+    // CG: q = p - c G(p)
+    s = base;
+    s.scale = -c;
+    s.coef_add = 1.0;
+    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_cgq_));
+    s = base;
+    MF_TRY(build_plan<Real>(Body::Force, {s}, plan_force_));
+    MF_TRY(build_ext_plans());
+    plans_ready_ = true;
+    return MF_OK;
+  }
+
+  mf_status build_ext_plans() {
+    if (np_ <= 0 || n_ext_ == 0) return MF_OK;
+    // The naive path evaluates external sources with the object's h
+    // (magnetic_force.cu:1118, :1129); the default path with ext_mag_h (:693, :697).
+    const double hs = naive_ ? h_ : ext_h_;
+    SceneSpec s;
+    s.t_off = 0;
+    s.nt = np_;
+    s.s_off = 0;
+    s.ns = n_ext_;
+    s.h = hs;
+    s.scale = 1.0;
+    for (int k = 0; k < 3; ++k) s.cvec[k] = H0_[k];
+    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_ext_field_));
+    SceneSpec t = s;
+    for (int k = 0; k < 3; ++k) t.cvec[k] = 0.0;
+    MF_TRY(build_plan<Real>(Body::Tensor, {t}, plan_ext_tensor_));
+    return MF_OK;
+  }
+
+  mf_status run(const Plan<Real>& plan, const LaunchIO<Real>& io) {
+    MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+    ++ctr_.kernel_launches;
+    return MF_OK;
+  }
+
+  mf_status field(Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4, const R4* add4b,
+                  const double* done = nullptr) {
+    LaunchIO<Real> io;
+    io.tpos = pos4();
+    io.spos = pos4();
+    io.smom = src_mom;
+    io.out4 = out4;
+    io.add4 = add4;
+    io.add4b = add4b;
+    io.done_flags = done;
+    io.done_stride = kScal;
+    MF_TRY(run(plan, io));
+    ctr_.field_products += 1;
+    ctr_.field_pairs += plan.pairs;
+    return MF_OK;
+  }
+
+  template <class Op>
+  mf_status reduce(const Op& op) {
+    const int64_t gx = grid_1d(np_, sms_) > unsigned(sms_ * 2) ? sms_ * 2 : grid_1d(np_, sms_);
+    dim3 grid(unsigned(gx), 1);
+    reduce_kernel<Op><<<grid, 256, 0, st_>>>(op, range_.template as<VecRange>(), scal_.template as<double>(),
+                                             red_part_.template as<double>(), red_ticket_.template as<int32_t>());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    return MF_OK;
+  }
+
+  mf_status read_scalars(double* dst, int first, int count) {
+    MF_CUDA_TRY(cudaMemcpyAsync(pinned_, scal_.template as<double>() + first, sizeof(double) * count,
+                                cudaMemcpyDeviceToHost, st_));
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    memcpy(dst, pinned_, sizeof(double) * count);
+    return MF_OK;
+  }
+
+  // The reference's nonlinear CG, control flow on the host as in
+  // magnetic_force.cu:874-888 (solve), :1008-1040 (start), :1043-1095 (step_iteration).
+  mf_status solve_nlcg(int64_t niter, int64_t* iters_out, double* err_out) {
+    const double inv_np = 1.0 / double(np_);
+    int64_t steps = 0;
+    k_init_row<<<1, 32, 0, st_>>>(scal_.template as<double>(), 0.0, 0.0);
+    MF_CUDA_TRY(cudaGetLastError());
+    // start()
+    MF_TRY(field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B)));
+    MF_TRY(reduce(NlErr<R4>{v4(V_R)}));
+    double err = 0;
+    MF_TRY(read_scalars(&err, S_ERR, 1));
+    history_.push_back(err);
+    if (!(std::sqrt(err * inv_np) < tolerance_)) {
+      MF_TRY(field(plan_grad_, v4(V_R), v4(V_G), v4(V_R), nullptr));
+      MF_TRY(reduce(NlDirection<Real, R4>{v4(V_G), v4(V_DOLD), v4(V_D), true}));
+      MF_TRY(alpha_and_step());
+      int64_t i_step = 0;
+      for (int64_t it = 0; it < niter && it < max_iteration_; ++it) {
+        ++steps;
+        std::swap(vec4_[V_G], vec4_[V_GOLD]);  // old_gradient = gradient
+        std::swap(vec4_[V_D], vec4_[V_DOLD]);  // old_step_dir = step_dir
+        MF_TRY(field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B)));
+        MF_TRY(reduce(NlErr<R4>{v4(V_R)}));
+        MF_TRY(read_scalars(&err, S_ERR, 1));
+        history_.push_back(err);
+        if (std::sqrt(err * inv_np) < tolerance_) break;
+        if (err > history_[history_.size() - 2]) break;
+        ++i_step;
+        MF_TRY(field(plan_grad_, v4(V_R), v4(V_G), v4(V_R), nullptr));
+        k_set_scalar<<<1, 32, 0, st_>>>(scal_.template as<double>(), S_RESET, (i_step % 10 == 0) ? 1.0 : 0.0);
+        MF_CUDA_TRY(cudaGetLastError());
+        MF_TRY(reduce(NlBeta<R4>{v4(V_G), v4(V_GOLD), v4(V_DOLD)}));
+        MF_TRY(reduce(NlDirection<Real, R4>{v4(V_G), v4(V_DOLD), v4(V_D), false}));
+        MF_TRY(alpha_and_step());
+      }
+    }
+    if (iters_out) *iters_out = steps;
+    if (err_out) *err_out = err;
+    return MF_OK;
+  }
+
+  // calc_alpha (magnetic_force.cu:1287-1302), then b += alpha d (:1037, :1092).
+  mf_status alpha_and_step() {
+    MF_TRY(field(plan_dd_, v4(V_D), v4(V_DD), v4(V_D), nullptr));
+    MF_TRY(reduce(NlAlpha<R4>{v4(V_DD), v4(V_R)}));
+    MF_TRY(reduce(NlStep<Real, R4>{v4(V_B), v4(V_D)}));
+    return MF_OK;
+  }
+
+  // CG on (I - c G) b = Hext, scalar steps on the device, the host checking
+  // the stop flag every check_interval iterations.
+  mf_status solve_cg(int64_t niter, int64_t* iters_out, double* err_out) {
+    const int64_t cap = cg_max_iter_ < niter ? cg_max_iter_ : niter;
+    k_init_row<<<1, 32, 0, st_>>>(scal_.template as<double>(), rel_tol_, double(cap));
+    MF_CUDA_TRY(cudaGetLastError());
+    double* done = scal_.template as<double>() + S_DONE;
+    MF_TRY(field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B)));
+    MF_TRY(reduce(CgStart<R4>{v4(V_R), v4(V_P), hext4()}));
+    double row[kScal];
+    MF_TRY(read_scalars(row, 0, kScal));
+    int64_t launched = 0;
+    while (row[S_DONE] == 0.0 && launched < cap) {
+      for (int k = 0; k < check_interval_ && launched < cap; ++k, ++launched) {
+        MF_TRY(field(plan_cgq_, v4(V_P), v4(V_Q), v4(V_P), nullptr, done));
+        MF_TRY(reduce(CgPq<R4>{v4(V_P), v4(V_Q)}));
+        MF_TRY(reduce(CgUpdate<Real, R4>{v4(V_B), v4(V_R), v4(V_P), v4(V_Q)}));
+        MF_TRY(reduce(CgDirection<Real, R4>{v4(V_R), v4(V_P)}));
+      }
+      MF_TRY(read_scalars(row, 0, kScal));
+    }
+    // Skipped launches after the stop did no field work; count executed products only.
+    const int64_t executed = int64_t(row[S_ITERS]);
+    ctr_.field_products -= (launched - executed);
+    ctr_.field_pairs -= double(launched - executed) * plan_cgq_.pairs;
+    if (iters_out) *iters_out = executed;
+    if (err_out) *err_out = row[S_RELRES];
+    history_.push_back(row[S_RELRES]);
+    if (row[S_RELRES] < rel_tol_) return MF_OK;
+    char buf[160];
+    snprintf(buf, sizeof(buf), "CG stopped at relative residual %.3e after %lld iterations (tolerance %.3e)",
+             row[S_RELRES], (long long)executed, rel_tol_);
+    return fail(MF_ERR_NOT_CONVERGED, buf);
+  }
+
+  mf_status publish_b() {
+    const Real c = Real(c_coef());
+    k_publish_b<Real, R4><<<grid_1d(np_, sms_), 256, 0, st_>>>(np_, c, v4(V_B), pubr(MF_Q_B_OVER_MU0, 0),
+                                                                pubr(MF_Q_B_OVER_MU0, 1), pubr(MF_Q_B_OVER_MU0, 2),
+                                                                pubr(MF_Q_M, 0), pubr(MF_Q_M, 1), pubr(MF_Q_M, 2),
+                                                                mom4());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    if (!kF32) {
+      publish_f(MF_Q_B_OVER_MU0);
+      publish_f(MF_Q_M);
+    }
+    return MF_OK;
+  }
+
+  void publish_f(int q) {
+    if constexpr (!kF32) {
+      k_to_float<Real><<<grid_1d(3 * np_, sms_), 256, 0, st_>>>(3 * np_, pub_r_[q].template as<Real>(), pub_f_[q].template as<float>());
+      ++ctr_.kernel_launches;
+    }
+  }
+
+  template <class T>
+  mf_status soa_to_aos(const T* soa, T* aos, int64_t n);
+
+  // Component k of quantity q into dst (device), as float or double.
+  mf_status component_to(int q, int k, void* dst, bool f64) {
+    const int64_t n = np_;
+    if (q == MF_Q_POSITIONS) {
+      if (!f64) {
+        MF_CUDA_TRY(cudaMemcpyAsync(dst, pubf(q, k), size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+      } else {
+        MF_TRY(gather_r4(pos4(), k, static_cast<double*>(dst), n));
+      }
+      return MF_OK;
+    }
+    if (q == MF_Q_VELOCITY) {
+      if (f64) MF_TRY(gather_r4(vel4(), k, static_cast<double*>(dst), n));
+      else MF_TRY(gather_r4f(vel4(), k, static_cast<float*>(dst), n));
+      return MF_OK;
+    }
+    if (f64) {
+      if constexpr (kF32) {
+        MF_TRY(widen(pubr(q, k), static_cast<double*>(dst), n));
+      } else {
+        MF_CUDA_TRY(cudaMemcpyAsync(dst, pubr(q, k), size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+      }
+    } else {
+      MF_CUDA_TRY(cudaMemcpyAsync(dst, pubf(q, k), size_t(n) * sizeof(float), cudaMemcpyDeviceToDevice, st_));
+    }
+    return MF_OK;
+  }
+
+  mf_status gather_r4(const R4* src, int k, double* dst, int64_t n);
+  mf_status gather_r4f(const R4* src, int k, float* dst, int64_t n);
+  mf_status widen(const Real* src, double* dst, int64_t n);
+
+  // State -----------------------------------------------------------------
+  int64_t np_ = 0;
+  int64_t n_ext_ = 0;
+  double h_ = 0, ext_h_ = 0, volume_ = 0, chi_ = 0;
+  double H0_[3] = {0, 0, 0};
+  double tolerance_ = 0.1;       // magnetic_force.cu:626
+  int64_t max_iteration_ = 80;   // magnetic_force.cu:627
+  bool naive_ = false;           // magnetic_force.cu:702
+  int crit_size_ = 384;          // magnetic_force.cu:647
+  int solver_ = MF_SOLVER_NLCG;
+  double rel_tol_ = 1e-6;
+  int64_t cg_max_iter_ = 500;
+  int check_interval_ = 4;
+  int sms_ = 1;
+  cudaStream_t st_ = nullptr;
+  void* pinned_ = nullptr;
+  std::vector<double> history_;
+  mf_counters ctr_ = {};
+};
+
+template <class T>
+__global__ void k_soa_to_aos(int64_t n, const T* __restrict__ soa, T* __restrict__ aos) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    aos[3 * i] = soa[i];
+    aos[3 * i + 1] = soa[n + i];
+    aos[3 * i + 2] = soa[2 * n + i];
+  }
+}
+
+template <class R4, class T>
+__global__ void k_gather_r4(int64_t n, const R4* __restrict__ src, int k, T* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const R4 v = src[i];
+    dst[i] = T(k == 0 ? v.x : (k == 1 ? v.y : v.z));
+  }
+}
+
+template <class S>
+__global__ void k_widen(int64_t n, const S* __restrict__ src, double* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    dst[i] = double(src[i]);
+}
+
+template <class Real>
+template <class T>
+mf_status Engine<Real>::soa_to_aos(const T* soa, T* aos, int64_t n) {
+  k_soa_to_aos<T><<<grid_1d(n, sms_), 256, 0, st_>>>(n, soa, aos);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+template <class Real>
+mf_status Engine<Real>::gather_r4(const R4* src, int k, double* dst, int64_t n) {
+  k_gather_r4<R4, double><<<grid_1d(n, sms_), 256, 0, st_>>>(n, src, k, dst);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+template <class Real>
+mf_status Engine<Real>::gather_r4f(const R4* src, int k, float* dst, int64_t n) {
+  k_gather_r4<R4, float><<<grid_1d(n, sms_), 256, 0, st_>>>(n, src, k, dst);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+template <class Real>
+mf_status Engine<Real>::widen(const Real* src, double* dst, int64_t n) {
+  k_widen<Real><<<grid_1d(n, sms_), 256, 0, st_>>>(n, src, dst);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+
+template class Engine<float>;
+template class Engine<double>;
+
+}  // namespace mfgb
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace mfgb;
+
+struct mf_solver {
+  std::unique_ptr<EngineBase> eng;
+  int device = 0;
+};
+
+namespace {
+// Runs `fn` with the handle's device current; converts exceptions to statuses.
+template <class F>
+mf_status guarded(mf_solver* s, F&& fn) {
+  if (!s || !s->eng) return fail(MF_ERR_INVALID_ARG, "NULL solver handle");
+  try {
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return fn(*s->eng);
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  } catch (...) {
+    return fail(MF_ERR_CUDA, "unexpected exception");
+  }
+}
+}  // namespace
+
+extern "C" {
+
+const char* mf_status_string(mf_status s) {
+  switch (s) {
+    case MF_OK: return "MF_OK";
+    case MF_ERR_INVALID_ARG: return "MF_ERR_INVALID_ARG";
+    case MF_ERR_OOM: return "MF_ERR_OOM";
+    case MF_ERR_NOT_CONVERGED: return "MF_ERR_NOT_CONVERGED";
+    case MF_ERR_CUDA: return "MF_ERR_CUDA";
+    case MF_ERR_TIMEOUT: return "MF_ERR_TIMEOUT";
+    case MF_ERR_BUDGET: return "MF_ERR_BUDGET";
+    case MF_ERR_UNSUPPORTED: return "MF_ERR_UNSUPPORTED";
+    case MF_ERR_BUSY: return "MF_ERR_BUSY";
+  }
+  return "MF_UNKNOWN_STATUS";
+}
+
+const char* mf_last_error(void) { return last_error_cstr(); }
+int mf_abi_version(void) { return MF_ABI_VERSION; }
+
+mf_status mf_create(const mf_params* p, mf_solver** out) {
+  if (!p || !out) return fail(MF_ERR_INVALID_ARG, "NULL argument");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(MF_ERR_UNSUPPORTED, "no CUDA device available");
+  if (p->device < 0 || p->device >= ndev) return fail(MF_ERR_INVALID_ARG, "bad device ordinal");
+  if (p->precision != MF_FP32 && p->precision != MF_FP64) return fail(MF_ERR_INVALID_ARG, "bad precision");
+  try {
+    e = cudaSetDevice(p->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    std::unique_ptr<mf_solver> s(new mf_solver);
+    s->device = p->device;
+    if (p->precision == MF_FP64) s->eng.reset(new Engine<double>());
+    else s->eng.reset(new Engine<float>());
+    s->eng->device = p->device;
+    mf_status st = s->eng->init(*p);
+    if (st != MF_OK) return st;
+    *out = s.release();
+    return MF_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  }
+}
+
+mf_status mf_destroy(mf_solver* s) {
+  if (!s) return MF_OK;
+  cudaSetDevice(s->device);
+  if (s->eng) cudaStreamSynchronize(s->eng->stream());
+  delete s;
+  return MF_OK;
+}
+
+mf_status mf_set_stream(mf_solver* s, void* stream) {
+  return guarded(s, [&](EngineBase& e) {
+    e.set_stream(static_cast<cudaStream_t>(stream));
+    return MF_OK;
+  });
+}
+
+mf_status mf_set_positions(mf_solver* s, const float* xyz, int64_t n, int32_t layout, int32_t where) {
+  return guarded(s, [&](EngineBase& e) { return e.set_positions(xyz, n, layout, where); });
+}
+
+mf_status mf_set_external(mf_solver* s, const float H0[3], const float* sp, const float* sm, int64_t ns,
+                          float ext_mag_h) {
+  return guarded(s, [&](EngineBase& e) { return e.set_external(H0, sp, sm, ns, ext_mag_h); });
+}
+
+mf_status mf_solve(mf_solver* s, int64_t niter, int64_t* iters, double* final_err) {
+  return guarded(s, [&](EngineBase& e) { return e.solve(niter, iters, final_err); });
+}
+
+mf_status mf_get_error_history(mf_solver* s, double* dst, int64_t cap, int64_t* len) {
+  return guarded(s, [&](EngineBase& e) {
+    const auto& h = e.history();
+    if (len) *len = int64_t(h.size());
+    if (dst)
+      for (int64_t i = 0; i < cap && i < int64_t(h.size()); ++i) dst[i] = h[size_t(i)];
+    return MF_OK;
+  });
+}
+
+mf_status mf_eval_force(mf_solver* s) {
+  return guarded(s, [&](EngineBase& e) { return e.eval_force(); });
+}
+
+mf_status mf_get(mf_solver* s, int32_t q, float* dst, int32_t layout, int32_t where) {
+  return guarded(s, [&](EngineBase& e) { return e.get(q, dst, layout, where, false); });
+}
+
+mf_status mf_get_f64(mf_solver* s, int32_t q, double* dst, int32_t layout, int32_t where) {
+  return guarded(s, [&](EngineBase& e) { return e.get(q, dst, layout, where, true); });
+}
+
+mf_status mf_device_soa(mf_solver* s, int32_t q, float** x, float** y, float** z) {
+  return guarded(s, [&](EngineBase& e) { return e.device_soa(q, x, y, z); });
+}
+
+mf_status mf_num_particles(mf_solver* s, int64_t* n) {
+  return guarded(s, [&](EngineBase& e) {
+    if (!n) return fail(MF_ERR_INVALID_ARG, "NULL");
+    *n = e.np();
+    return MF_OK;
+  });
+}
+
+mf_status mf_set_option(mf_solver* s, int32_t key, double value) {
+  return guarded(s, [&](EngineBase& e) { return e.set_option(key, value); });
+}
+
+mf_status mf_get_option(mf_solver* s, int32_t key, double* value) {
+  return guarded(s, [&](EngineBase& e) { return e.get_option(key, value); });
+}
+
+static mf_status export_common(mf_solver* s, const char* path, int q) {
+  return guarded(s, [&](EngineBase& e) {
+    if (!path) return fail(MF_ERR_INVALID_ARG, "NULL path");
+    const int64_t n = e.np();
+    std::vector<float> pos(size_t(3 * n)), v(size_t(3 * n)), he(size_t(3 * n));
+    MF_TRY(e.get(MF_Q_POSITIONS, pos.data(), MF_LAYOUT_AOS, MF_HOST, false));
+    MF_TRY(e.get(q, v.data(), MF_LAYOUT_AOS, MF_HOST, false));
+    MF_TRY(e.get(MF_Q_HEXT, he.data(), MF_LAYOUT_AOS, MF_HOST, false));
+    std::ofstream out(path);
+    if (!out) return fail(MF_ERR_INVALID_ARG, std::string("cannot open ") + path);
+    // Same record as magnetic_force.cu:1348-1351 (default ostream formatting).
+    for (int64_t i = 0; i < n; ++i) {
+      out << i << " ";
+      out << pos[3 * i] << " " << pos[3 * i + 1] << " " << pos[3 * i + 2] << " ";
+      out << v[3 * i] << " " << v[3 * i + 1] << " " << v[3 * i + 2] << " ";
+      out << he[3 * i] << " " << he[3 * i + 1] << " " << he[3 * i + 2] << std::endl;
+    }
+    return MF_OK;
+  });
+}
+
+mf_status mf_export_data(mf_solver* s, const char* path) { return export_common(s, path, MF_Q_B_OVER_MU0); }
+mf_status mf_export_force(mf_solver* s, const char* path) { return export_common(s, path, MF_Q_FORCE); }
+
+mf_status mf_advance(mf_solver* s, double dt, int64_t niter, int64_t* iters) {
+  return guarded(s, [&](EngineBase& e) { return e.advance(dt, niter, iters); });
+}
+
+mf_status mf_get_counters(mf_solver* s, mf_counters* c) {
+  return guarded(s, [&](EngineBase& e) {
+    if (!c) return fail(MF_ERR_INVALID_ARG, "NULL");
+    *c = e.counters();
+    return MF_OK;
+  });
+}
+
+mf_status mf_reset_counters(mf_solver* s) {
+  return guarded(s, [&](EngineBase& e) {
+    e.counters() = mf_counters{};
+    return MF_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,179 @@
+// mf_internal.h -- shared declarations of the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mf.h"
+#include "mf_allpairs.cuh"
+
+namespace mfgb {
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+void set_last_error(const std::string& msg);
+mf_status fail(mf_status s, const std::string& msg);
+mf_status cuda_fail(cudaError_t e, const char* what);
+
+#define MF_CUDA_TRY(expr)                                       \
+  do {                                                          \
+    cudaError_t _e = (expr);                                    \
+    if (_e != cudaSuccess) return ::mfgb::cuda_fail(_e, #expr); \
+  } while (0)
+
+#define MF_TRY(expr)            \
+  do {                          \
+    mf_status _s = (expr);      \
+    if (_s != MF_OK) return _s; \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Device buffer (owning, growable)
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : ptr(o.ptr), bytes(o.bytes) {
+    o.ptr = nullptr;
+    o.bytes = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      ptr = o.ptr;
+      bytes = o.bytes;
+      o.ptr = nullptr;
+      o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  // Ensure at least `want` bytes.  keep: preserve the old contents on growth;
+  // zero: clear bytes beyond the preserved prefix.
+  mf_status reserve(size_t want, bool keep = false, bool zero = false);
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(ptr);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// All-pairs launch configurations.
+// ---------------------------------------------------------------------------
+enum class Body { Field = 0, Force = 1, Tensor = 2 };
+
+template <class Real, Body B>
+struct KCfg;
+// FP32: 256 threads x 2 targets, 256-source tiles, 3 stages (24 KB of smem).
+template <>
+struct KCfg<float, Body::Field> {
+  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 3;
+};
+template <>
+struct KCfg<float, Body::Force> {
+  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 3;
+};
+template <>
+struct KCfg<float, Body::Tensor> {
+  static constexpr int TPB = 128, TPT = 1, TILE = 256, STAGES = 3, kOut = 6;
+};
+// FP64: 128 threads x 1 target, 128-source tiles of 32-byte records.
+template <>
+struct KCfg<double, Body::Field> {
+  static constexpr int TPB = 128, TPT = 1, TILE = 128, STAGES = 3, kOut = 3;
+};
+template <>
+struct KCfg<double, Body::Force> {
+  static constexpr int TPB = 128, TPT = 1, TILE = 128, STAGES = 3, kOut = 3;
+};
+template <>
+struct KCfg<double, Body::Tensor> {
+  static constexpr int TPB = 128, TPT = 1, TILE = 128, STAGES = 3, kOut = 6;
+};
+
+// One scene of a launch before it is laid out in step space.  nt > 0, ns > 0.
+struct SceneSpec {
+  int64_t t_off, nt, s_off, ns;
+  double h;
+  double scale = 1.0;
+  double coef_add = 0.0;   // field: coefficient of add4
+  double coef_add2 = 0.0;  // field: coefficient of add4b
+  double cvec[3] = {0.0, 0.0, 0.0};
+};
+
+// A laid-out launch: device scene table plus its step-space totals.
+template <class Real>
+struct Plan {
+  Body body = Body::Field;
+  int64_t total_steps = 0;
+  int64_t total_tb = 0;
+  int32_t n_scenes = 0;
+  double pairs = 0.0;  // sum over scenes of nt * ns
+  DevBuf d_scenes;
+  std::vector<SceneDesc<Real>> host;  // the table as uploaded
+};
+
+// Build (and synchronously upload) a plan.  Empty scenes are rejected.
+template <class Real>
+mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan);
+// Re-upload a plan whose per-scene coefficients (scale, coef_add*, cvec) changed.
+template <class Real>
+mf_status refresh_plan_coefs(const std::vector<SceneSpec>& specs, Plan<Real>& plan);
+
+// Scratch of all-pairs launches: FP64 partials, tickets, error word.
+struct Scratch {
+  DevBuf partials;
+  DevBuf counters;
+  DevBuf err;
+  mf_status ensure(size_t partial_doubles, size_t n_counters);
+  // Read and clear the device error word (synchronises `st`).
+  mf_status check(cudaStream_t st);
+};
+
+// Pointers of one launch.
+template <class Real>
+struct LaunchIO {
+  using R4 = typename Vec4T<Real>::type;
+  const R4* tpos = nullptr;
+  const R4* tmom = nullptr;
+  const R4* spos = nullptr;
+  const R4* smom = nullptr;
+  Real* out[9] = {};
+  R4* out4 = nullptr;
+  const R4* add4 = nullptr;
+  const R4* add4b = nullptr;
+  const Real* rext[9] = {};
+  int naive_quirks = 0;
+  const double* done_flags = nullptr;
+  int done_stride = 0;
+};
+
+// Scratch sizes a plan needs.
+template <class Real>
+void plan_scratch_needs(const Plan<Real>& plan, size_t* partial_doubles, size_t* n_counters);
+
+// Launch a plan on `st`.  Grows `scratch` if needed (allocation happens only
+// outside stream capture; a captured launch must have been sized before).
+template <class Real>
+mf_status run_plan(const Plan<Real>& plan, const LaunchIO<Real>& io, Scratch& scratch, cudaStream_t st);
+
+// Same, with caller-provided scratch pointers (no allocation at all).
+template <class Real>
+mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials,
+                       int32_t* counters, int32_t* err, cudaStream_t st);
+
+int device_sms(int device);
+int current_device();
+
+}  // namespace mfgb

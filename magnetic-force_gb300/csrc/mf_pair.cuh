@@ -1,0 +1,221 @@
+// mf_pair.cuh -- pair arithmetic of the SPH-smoothed dipole kernels.
+//
+// Field (B/mu0) of a source dipole s at offset d = target - source:
+//   fmmtl_minimum/kernel/Dipole_B.kern:46-104, magnetic_force.cu:63-98
+//   K_B(d) s = rhat (rhat.s)(w_avr - w_dens) - (w_avr/3 - w_dens) s.
+// Written here as  (1/4pi) * (3 d (d.s) alpha - s beta)  with
+//   far  (q >= 2):  alpha = r^-5,  beta = r^-3        (w_dens = 0)
+//   near (q <  2):  alpha = 4pi (w_avr - w_dens) / (3 r^2),  beta = 4pi (w_avr/3 - w_dens)
+// so the common far pair costs one rsqrt and a handful of FMAs.  At r = 0 the
+// d-term vanishes and beta carries the self term, as in the reference.
+//
+// Force tensor of a source dipole s, contracted with the target dipole m:
+//   fmmtl_minimum/kernel/Dipole_hessian.kern:53-253, magnetic_force.cu:239-427.
+// The reference builds a rotated frame (xi, eta, zeta = rhat) and forms
+// M U M^T.  Expanding that product with an orthonormal frame gives the
+// frame-free form used here,
+//   T_ab = P (ds delta_ab + s_a d_b + d_a s_b) + Q ds d_a d_b,   ds = d.s,
+//   far  (q >  4):  P = K r^-5,            Q = -5 K r^-7,   K = 3 mu0 / (4 pi)
+//   near (0<q<=4):  P = C1(q) / (h^4 r),   Q = (C2(q) - 3 C1(q)) / (h^4 r^3)
+//   q == 0:         T = 0  (overlapping particles exert no force, :101-104)
+// and F = T m = P (ds m + dm s + sm d) + Q ds dm d  with dm = d.m, sm = s.m.
+// The far branch is the reference's analytic tensor term for term
+// (A = mu0 w_avr / r^2, dAdr, dBdr of :168-206).
+#pragma once
+#include "mf_device.cuh"
+
+namespace mfgb {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kMu0 = 1.25663706e-6;              // Dipole_hessian.kern:170
+constexpr double kForceK = 3.0 * kMu0 / (4.0 * kPi);  // far-field force prefactor
+constexpr double kInv4Pi = 1.0 / (4.0 * kPi);
+
+// Per-scene constants derived from the smoothing length.
+template <class Real>
+struct PairConsts {
+  Real inv_h;        // 1/h
+  Real ih3;          // 1/h^3
+  Real ih4_over_k;   // 1/(h^4 K): scales the fitted curves into the K-free form
+  Real near2_field;  // (2h)^2: field pairs closer than this take the SPH branch
+  Real near2_force;  // (4h)^2: force pairs at or inside this take the fitted branch
+};
+
+template <class Real>
+__host__ __device__ inline PairConsts<Real> make_pair_consts(double h) {
+  PairConsts<Real> k;
+  k.inv_h = Real(1.0 / h);
+  k.ih3 = Real(1.0 / (h * h * h));
+  k.ih4_over_k = Real(1.0 / (h * h * h * h * kForceK));
+  k.near2_field = Real(4.0 * h * h);
+  k.near2_force = Real(16.0 * h * h);
+  return k;
+}
+
+template <class Real>
+__device__ __forceinline__ Real rsqrt_r(Real x);
+template <>
+__device__ __forceinline__ float rsqrt_r<float>(float x) {
+  return rsqrt_approx(x);
+}
+template <>
+__device__ __forceinline__ double rsqrt_r<double>(double x) {
+  return rsqrt(x);
+}
+
+// Near-field SPH weights of the field kernel (Dipole_B.kern:46-76), returned as
+// the (alpha, beta) pair of the form above.  Only reached for r < 2h.
+template <class Real>
+__device__ __noinline__ void field_near_coeffs(Real r2, const PairConsts<Real>& k, Real& alpha, Real& beta) {
+  Real r = sqrt(r2);
+  Real q = r * k.inv_h;
+  Real tmq = Real(2) - q;
+  Real tmq3 = tmq * tmq * tmq;
+  Real wa, wd;  // 4 pi h^3 w_avr, 4 pi h^3 w_dens
+  if (q >= Real(1)) {
+    Real q2 = q * q, q3 = q2 * q;
+    Real P = q3 * q3 / Real(6) - Real(6) * q3 * q2 / Real(5) + Real(3) * q2 * q2 - Real(8) * q3 / Real(3) +
+             Real(1) / Real(15);
+    wa = Real(-3) * P / q3;
+    wd = tmq3;
+  } else {
+    Real q2 = q * q;
+    Real omq = Real(1) - q;
+    wa = (Real(15) * q2 * q - Real(36) * q2 + Real(40)) / Real(10);
+    wd = tmq3 - Real(4) * omq * omq * omq;
+  }
+  beta = (wa / Real(3) - wd) * k.ih3;
+  alpha = (r2 > Real(0)) ? (wa - wd) * k.ih3 / (Real(3) * r2) : Real(0);
+}
+
+// One field pair: s1 += d (d.s) alpha, s2 += s beta.  Field = (3 s1 - s2) / 4pi.
+template <class Real>
+__device__ __forceinline__ void field_pair(Real dx, Real dy, Real dz, Real sx, Real sy, Real sz,
+                                           const PairConsts<Real>& k, Real* s1, Real* s2) {
+  Real r2 = dx * dx + dy * dy + dz * dz;
+  Real alpha, beta;
+  if (r2 >= k.near2_field) {
+    Real ri = rsqrt_r(r2);
+    Real ri2 = ri * ri;
+    beta = ri2 * ri;
+    alpha = beta * ri2;
+  } else {
+    field_near_coeffs(r2, k, alpha, beta);
+  }
+  Real t = (dx * sx + dy * sy + dz * sz) * alpha;
+  s1[0] += dx * t;
+  s1[1] += dy * t;
+  s1[2] += dz * t;
+  s2[0] += sx * beta;
+  s2[1] += sy * beta;
+  s2[2] += sz * beta;
+}
+
+// Fitted near-field curves C1(q), C2(q), q in (0, 4]
+// (Dipole_hessian.kern:53-85, magnetic_force.cu:301-330).
+template <class Real>
+__device__ __forceinline__ void fitted_curves(Real q, Real& c1, Real& c2) {
+#define MF_P4(a, b, c, d, e) (q * (q * (q * (q * Real(a) + Real(b)) + Real(c)) + Real(d)) + Real(e))
+  if (q <= Real(1)) {
+    c1 = MF_P4(9.97813616438174e-09, -2.97897856524718e-08, 2.38918644566813e-09, 4.53199938857366e-08,
+               2.44617454752747e-11);
+    c2 = MF_P4(6.69550479838731e-08, -1.61753307173877e-07, 1.68213714992711e-08, 1.34558143036838e-07,
+               1.10976027980100e-10);
+  } else if (q <= Real(2)) {
+    c1 = MF_P4(-2.76473728643294e-09, 2.86975546540539e-08, -9.94582836806651e-08, 1.25129924573675e-07,
+               -2.37010166723652e-08);
+    c2 = MF_P4(-3.08460139955194e-08, 2.29192245602275e-07, -5.88399621128587e-07, 5.61170054591844e-07,
+               -1.14421132829680e-07);
+  } else if (q <= Real(3)) {
+    c1 = MF_P4(-1.09679990621465e-09, 9.77055663264614e-09, -2.54781238661150e-08, 2.65020634884934e-09,
+               5.00787562417835e-08);
+    c2 = MF_P4(3.50477408060213e-09, -5.25956271895141e-08, 2.78876509535747e-07, -6.24199554212217e-07,
+               4.91807818904985e-07);
+  } else {
+    c1 = MF_P4(3.79927162333632e-10, -6.26368404962679e-09, 3.94760528277489e-08, -1.13580541622200e-07,
+               1.27491333574323e-07);
+    c2 = MF_P4(7.33485346367840e-10, -9.58855788627803e-09, 4.37085309763591e-08, -7.48004594092261e-08,
+               2.34161209605651e-08);
+  }
+#undef MF_P4
+}
+
+// (P, Q) of the force tensor for 0 <= r <= 4h, in units of K.
+template <class Real>
+__device__ __noinline__ void force_near_coeffs(Real r2, const PairConsts<Real>& k, Real& P, Real& Q) {
+  if (r2 == Real(0)) {
+    P = Real(0);
+    Q = Real(0);
+    return;
+  }
+  Real r = sqrt(r2);
+  Real q = r * k.inv_h;
+  q = q > Real(4) ? Real(4) : q;  // the branch test is on r^2; keep q on the fitted range
+  Real c1, c2;
+  fitted_curves(q, c1, c2);
+  Real ir = Real(1) / r;
+  Real s = k.ih4_over_k * ir;
+  P = c1 * s;
+  Q = (c2 - Real(3) * c1) * s * ir * ir;
+}
+
+// (P, Q) of the force tensor for any pair, in units of K.
+template <class Real>
+__device__ __forceinline__ void force_coeffs(Real r2, const PairConsts<Real>& k, Real& P, Real& Q) {
+  if (r2 > k.near2_force) {
+    Real ri = rsqrt_r(r2);
+    Real ri2 = ri * ri;
+    P = ri2 * ri2 * ri;
+    Q = Real(-5) * P * ri2;
+  } else {
+    force_near_coeffs(r2, k, P, Q);
+  }
+}
+
+// One force pair contracted with the target dipole m: f += T(d, s) m / K.
+template <class Real>
+__device__ __forceinline__ void force_pair(Real dx, Real dy, Real dz, Real sx, Real sy, Real sz, Real mx,
+                                           Real my, Real mz, const PairConsts<Real>& k, Real* f) {
+  Real r2 = dx * dx + dy * dy + dz * dz;
+  Real ds = dx * sx + dy * sy + dz * sz;
+  Real dm = dx * mx + dy * my + dz * mz;
+  Real sm = sx * mx + sy * my + sz * mz;
+  Real u, v, w;
+  if (r2 > k.near2_force) {
+    Real ri = rsqrt_r(r2);
+    Real ri2 = ri * ri;
+    Real ri5 = ri2 * ri2 * ri;
+    u = ds * ri5;
+    v = dm * ri5;
+    w = (Real(-5) * ri2 * ds) * v + sm * ri5;
+  } else {
+    Real P, Q;
+    force_near_coeffs(r2, k, P, Q);
+    u = P * ds;
+    v = P * dm;
+    w = P * sm + Q * ds * dm;
+  }
+  f[0] += dx * w + mx * u + sx * v;
+  f[1] += dy * w + my * u + sy * v;
+  f[2] += dz * w + mz * u + sz * v;
+}
+
+// One tensor pair (6 unique entries xx, yy, zz, xy, xz, yz): t += T(d, s) / K.
+template <class Real>
+__device__ __forceinline__ void tensor_pair(Real dx, Real dy, Real dz, Real sx, Real sy, Real sz,
+                                            const PairConsts<Real>& k, Real* t) {
+  Real r2 = dx * dx + dy * dy + dz * dz;
+  Real P, Q;
+  force_coeffs(r2, k, P, Q);
+  Real ds = dx * sx + dy * sy + dz * sz;
+  Real pd = P * ds, qd = Q * ds;
+  Real ax = P * sx, ay = P * sy, az = P * sz;
+  t[0] += pd + Real(2) * ax * dx + qd * dx * dx;
+  t[1] += pd + Real(2) * ay * dy + qd * dy * dy;
+  t[2] += pd + Real(2) * az * dz + qd * dz * dz;
+  t[3] += ax * dy + ay * dx + qd * dx * dy;
+  t[4] += ax * dz + az * dx + qd * dx * dz;
+  t[5] += ay * dz + az * dy + qd * dy * dz;
+}
+
+}  // namespace mfgb

@@ -1,0 +1,320 @@
+"""Python host binding of libmfgb.so (include/mf.h) over ctypes.
+
+``Solver`` mirrors the reference's ``Libo::cuda_magnet_cgOptimizer``
+(magnetic_solver/magnetic_force.cuh:36-174): the same constructor arguments,
+the same method names (``setTargetpos``, ``setHext``, ``solve``,
+``evaluate_fitted_near_foece``, ``export_data``, ``export_force``) and the
+same public results (``M``, ``total_B_over_mu0``, ``Hext``,
+``magnetic_bodyforce``, ``dHextdx/dy/dz``), returned here as numpy arrays
+of shape [n, 3].  Knobs ``tolerance``, ``max_iteration`` and ``naive`` are
+properties, as they are public members in the reference.
+
+``direct_field`` / ``direct_force_tensor`` / ``direct_force`` evaluate the
+reference's FMMTL pair kernels all-pairs on device buffers (torch CUDA
+tensors), the replacement of ``fmmtl::direct``.
+
+There is no CPU fallback: if the library or a CUDA device is missing the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmfgb.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "mf.h")
+
+MF_OK = 0
+STATUS = {
+    0: "MF_OK", 1: "MF_ERR_INVALID_ARG", 2: "MF_ERR_OOM", 3: "MF_ERR_NOT_CONVERGED", 4: "MF_ERR_CUDA",
+    5: "MF_ERR_TIMEOUT", 6: "MF_ERR_BUDGET", 7: "MF_ERR_UNSUPPORTED", 8: "MF_ERR_BUSY",
+}
+LAYOUT_AOS, LAYOUT_SOA = 0, 1
+HOST, DEVICE = 0, 1
+FP32, FP64 = 0, 1
+Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyforce": 4,
+     "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
+OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
+       "crit_size": 6, "check_interval": 7}
+SOLVER_NLCG, SOLVER_CG = 0, 1
+
+
+class MFError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class mf_params(ctypes.Structure):
+    _fields_ = [
+        ("num_particles", ctypes.c_int64), ("h", ctypes.c_float), ("ext_mag_h", ctypes.c_float),
+        ("volume", ctypes.c_float), ("chi", ctypes.c_float), ("const_ext_field", ctypes.c_float * 3),
+        ("target_pos", ctypes.c_void_p), ("ext_source_pos", ctypes.c_void_p), ("ext_source_M", ctypes.c_void_p),
+        ("n_ext", ctypes.c_int64), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+    ]
+
+
+class mf_counters(ctypes.Structure):
+    _fields_ = [("field_products", ctypes.c_int64), ("force_passes", ctypes.c_int64),
+                ("field_pairs", ctypes.c_double), ("force_pairs", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libmfgb.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: build it with magnetic-force_gb300/build.py")
+    lib = ctypes.CDLL(path)
+    i32, i64, vp, f32, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_float, ctypes.c_double
+    sig = {
+        "mf_status_string": (ctypes.c_char_p, [i32]),
+        "mf_last_error": (ctypes.c_char_p, []),
+        "mf_abi_version": (ctypes.c_int, []),
+        "mf_create": (i32, [ctypes.POINTER(mf_params), ctypes.POINTER(vp)]),
+        "mf_destroy": (i32, [vp]),
+        "mf_set_stream": (i32, [vp, vp]),
+        "mf_set_positions": (i32, [vp, vp, i64, i32, i32]),
+        "mf_set_external": (i32, [vp, vp, vp, vp, i64, f32]),
+        "mf_solve": (i32, [vp, i64, ctypes.POINTER(i64), ctypes.POINTER(f64)]),
+        "mf_get_error_history": (i32, [vp, vp, i64, ctypes.POINTER(i64)]),
+        "mf_eval_force": (i32, [vp]),
+        "mf_get": (i32, [vp, i32, vp, i32, i32]),
+        "mf_get_f64": (i32, [vp, i32, vp, i32, i32]),
+        "mf_device_soa": (i32, [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]),
+        "mf_num_particles": (i32, [vp, ctypes.POINTER(i64)]),
+        "mf_set_option": (i32, [vp, i32, f64]),
+        "mf_get_option": (i32, [vp, i32, ctypes.POINTER(f64)]),
+        "mf_export_data": (i32, [vp, ctypes.c_char_p]),
+        "mf_export_force": (i32, [vp, ctypes.c_char_p]),
+        "mf_advance": (i32, [vp, f64, i64, ctypes.POINTER(i64)]),
+        "mf_get_counters": (i32, [vp, ctypes.POINTER(mf_counters)]),
+        "mf_reset_counters": (i32, [vp]),
+        "mf_direct_field": (i32, [vp, i64, vp, vp, i64, f32, vp, vp]),
+        "mf_direct_force_tensor": (i32, [vp, i64, vp, vp, i64, f32, vp, vp]),
+        "mf_direct_force": (i32, [vp, vp, i64, f32, vp, i32, vp, vp]),
+        "mf_release_scratch": (i32, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Function names declared in include/*.h (for the export check)."""
+    names = set()
+    hdir = os.path.dirname(header)
+    for fn in sorted(os.listdir(hdir)):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(hdir, fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names.update(re.findall(r"\b(mf_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def check(status: int) -> None:
+    if status != MF_OK:
+        msg = load().mf_last_error()
+        raise MFError(status, msg.decode() if msg else "")
+
+
+def _f32(a, cols=3) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, cols))
+
+
+class Solver:
+    """``Libo::cuda_magnet_cgOptimizer`` on libmfgb.so."""
+
+    def __init__(self, num_particles, h, ext_mag_h, volume, chi, const_ext_field, ext_source_pos,
+                 ext_source_M, target_pos, precision: str = "fp32", device: int = 0):
+        lib = load()
+        tp = _f32(target_pos)
+        if len(tp) != num_particles:
+            raise ValueError("target_pos does not have num_particles rows")
+        esp = _f32(ext_source_pos) if ext_source_pos is not None and len(ext_source_pos) else np.zeros((0, 3), np.float32)
+        esm = _f32(ext_source_M) if ext_source_M is not None and len(ext_source_M) else np.zeros((0, 3), np.float32)
+        p = mf_params()
+        p.num_particles = int(num_particles)
+        p.h, p.ext_mag_h, p.volume, p.chi = float(h), float(ext_mag_h), float(volume), float(chi)
+        for k in range(3):
+            p.const_ext_field[k] = float(const_ext_field[k])
+        p.target_pos = tp.ctypes.data
+        p.ext_source_pos = esp.ctypes.data if len(esp) else None
+        p.ext_source_M = esm.ctypes.data if len(esm) else None
+        p.n_ext = len(esp)
+        p.precision = FP64 if precision == "fp64" else FP32
+        p.device = int(device)
+        self._keep = (tp, esp, esm)
+        h_ = ctypes.c_void_p()
+        check(lib.mf_create(ctypes.byref(p), ctypes.byref(h_)))
+        self._h = h_
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().mf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- methods of the reference class -------------------------------------
+    def setTargetpos(self, pos):
+        a = _f32(pos)
+        check(load().mf_set_positions(self._h, a.ctypes.data, len(a), LAYOUT_AOS, HOST))
+
+    def set_positions_device(self, ptr: int, n: int, layout: int = LAYOUT_AOS):
+        check(load().mf_set_positions(self._h, ctypes.c_void_p(ptr), n, layout, DEVICE))
+
+    def setHext(self, const_ext_field, ext_source_pos, ext_source_M, ext_mag_h):
+        H = np.ascontiguousarray(const_ext_field, dtype=np.float32)
+        sp = _f32(ext_source_pos) if ext_source_pos is not None and len(ext_source_pos) else np.zeros((0, 3), np.float32)
+        sm = _f32(ext_source_M) if ext_source_M is not None and len(ext_source_M) else np.zeros((0, 3), np.float32)
+        check(load().mf_set_external(self._h, H.ctypes.data, sp.ctypes.data if len(sp) else None,
+                                     sm.ctypes.data if len(sm) else None, len(sp), float(ext_mag_h)))
+
+    def solve(self, niter: int = 100):
+        it = ctypes.c_int64(0)
+        err = ctypes.c_double(0)
+        st = load().mf_solve(self._h, int(niter), ctypes.byref(it), ctypes.byref(err))
+        if st not in (MF_OK, 3):
+            check(st)
+        self.last_status = st
+        return it.value, err.value
+
+    def evaluate_fitted_near_foece(self):
+        check(load().mf_eval_force(self._h))
+
+    def advance(self, dt: float, niter: int = 100) -> int:
+        it = ctypes.c_int64(0)
+        st = load().mf_advance(self._h, float(dt), int(niter), ctypes.byref(it))
+        if st not in (MF_OK, 3):
+            check(st)
+        return it.value
+
+    def export_data(self, path: str):
+        check(load().mf_export_data(self._h, path.encode()))
+
+    def export_force(self, path: str):
+        check(load().mf_export_force(self._h, path.encode()))
+
+    def set_stream(self, stream_ptr: int):
+        check(load().mf_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    # -- results ---------------------------------------------------------------
+    @property
+    def np(self) -> int:
+        n = ctypes.c_int64(0)
+        check(load().mf_num_particles(self._h, ctypes.byref(n)))
+        return n.value
+
+    def get(self, quantity: str, f64: bool = False) -> np.ndarray:
+        n = self.np
+        out = np.empty((n, 3), dtype=np.float64 if f64 else np.float32)
+        fn = load().mf_get_f64 if f64 else load().mf_get
+        check(fn(self._h, Q[quantity], out.ctypes.data, LAYOUT_AOS, HOST))
+        return out
+
+    def get_into_device(self, quantity: str, ptr: int, f64: bool = False, layout: int = LAYOUT_AOS):
+        fn = load().mf_get_f64 if f64 else load().mf_get
+        check(fn(self._h, Q[quantity], ctypes.c_void_p(ptr), layout, DEVICE))
+
+    def device_soa(self, quantity: str):
+        x, y, z = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        check(load().mf_device_soa(self._h, Q[quantity], ctypes.byref(x), ctypes.byref(y), ctypes.byref(z)))
+        return x.value, y.value, z.value
+
+    def error_history(self) -> np.ndarray:
+        n = ctypes.c_int64(0)
+        check(load().mf_get_error_history(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        check(load().mf_get_error_history(self._h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def counters(self) -> dict:
+        c = mf_counters()
+        check(load().mf_get_counters(self._h, ctypes.byref(c)))
+        return {f: getattr(c, f) for f, _ in mf_counters._fields_}
+
+    def reset_counters(self):
+        check(load().mf_reset_counters(self._h))
+
+    def set_option(self, key: str, value: float):
+        check(load().mf_set_option(self._h, OPT[key], float(value)))
+
+    def get_option(self, key: str) -> float:
+        v = ctypes.c_double(0)
+        check(load().mf_get_option(self._h, OPT[key], ctypes.byref(v)))
+        return v.value
+
+    M = property(lambda self: self.get("M"))
+    total_B_over_mu0 = property(lambda self: self.get("total_B_over_mu0"))
+    Hext = property(lambda self: self.get("Hext"))
+    magnetic_bodyforce = property(lambda self: self.get("magnetic_bodyforce"))
+    dHextdx = property(lambda self: self.get("dHextdx"))
+    dHextdy = property(lambda self: self.get("dHextdy"))
+    dHextdz = property(lambda self: self.get("dHextdz"))
+    xyz = property(lambda self: self.get("positions"))
+
+    tolerance = property(lambda self: self.get_option("tolerance"), lambda self, v: self.set_option("tolerance", v))
+    max_iteration = property(lambda self: int(self.get_option("max_iteration")),
+                             lambda self, v: self.set_option("max_iteration", v))
+    naive = property(lambda self: bool(self.get_option("naive")), lambda self, v: self.set_option("naive", 1 if v else 0))
+
+
+# -- direct evaluation on device buffers (torch CUDA tensors) -----------------
+def _dev(t):
+    import torch
+    assert t.is_cuda and t.dtype == torch.float32 and t.is_contiguous()
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def direct_field(targets, sources, charges, h):
+    import torch
+    out = torch.empty((targets.shape[0], 3), dtype=torch.float32, device=targets.device)
+    check(load().mf_direct_field(_dev(targets), targets.shape[0], _dev(sources), _dev(charges), sources.shape[0],
+                                 float(h), _dev(out), _stream()))
+    return out
+
+
+def direct_force_tensor(targets, sources, charges, h):
+    import torch
+    out = torch.empty((targets.shape[0], 9), dtype=torch.float32, device=targets.device)
+    check(load().mf_direct_force_tensor(_dev(targets), targets.shape[0], _dev(sources), _dev(charges),
+                                        sources.shape[0], float(h), _dev(out), _stream()))
+    return out
+
+
+def direct_force(pos, mom, h, rext9=None, naive_quirks=False):
+    import torch
+    out = torch.empty((pos.shape[0], 3), dtype=torch.float32, device=pos.device)
+    check(load().mf_direct_force(_dev(pos), _dev(mom), pos.shape[0], float(h),
+                                 _dev(rext9) if rext9 is not None else None, 1 if naive_quirks else 0,
+                                 _dev(out), _stream()))
+    return out

@@ -1,0 +1,155 @@
+"""GPU parity: the all-pairs kernels through the C ABI against the oracle and
+the reference's own outputs.
+
+Tolerances: FP32 kernels vs the FP64 oracle at relative L2 <= 1e-5 (the
+stated bar), which also holds against the reference's FP32 golden outputs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "golden_kernels.npz")
+TOL = 1e-5
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def dev(torch, a, cols=3):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1, cols))).cuda()
+
+
+def cases():
+    z = np.load(GOLD)
+    return z, sorted({k.split("/")[0] for k in z.files})
+
+
+@pytest.mark.parametrize("name", cases()[1])
+def test_golden_field(mf, cuda, name):
+    z, _ = cases()
+    t, s, m, h = z[f"{name}/targets"], z[f"{name}/sources"], z[f"{name}/charges"], float(z[f"{name}/h"])
+    out = mf.direct_field(dev(cuda, t), dev(cuda, s), dev(cuda, m), h).cpu().numpy()
+    assert rel(out, z[f"{name}/field"]) < TOL
+
+
+@pytest.mark.parametrize("name", cases()[1])
+def test_golden_tensor(mf, cuda, name, oracle):
+    z, _ = cases()
+    t, s, m, h = z[f"{name}/targets"], z[f"{name}/sources"], z[f"{name}/charges"], float(z[f"{name}/h"])
+    out = mf.direct_force_tensor(dev(cuda, t), dev(cuda, s), dev(cuda, m), h).cpu().numpy()
+    ref = z[f"{name}/tensor"]
+    if name == "boundary":
+        qd = np.linalg.norm(t.astype(np.float64), axis=1) / h
+        for i in range(len(t)):
+            amb = np.min(np.abs(qd[i] - np.array([1.0, 2.0, 3.0, 4.0]))) < 1e-5
+            e = rel(out[i], ref[i])
+            assert e < (0.05 if amb else 2e-5), (i, qd[i], e)
+    else:
+        assert rel(out, ref) < 2 * TOL
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 255, 256, 257, 511, 513, 1000, 4096])
+def test_field_sizes(mf, cuda, oracle, n):
+    rng = np.random.default_rng(n)
+    x = rng.random((n, 3)).astype(np.float32)
+    m = rng.normal(size=(n, 3)).astype(np.float32)
+    h = 0.125
+    got = mf.direct_field(dev(cuda, x), dev(cuda, x), dev(cuda, m), h).cpu().numpy()
+    assert rel(got, oracle.field(x, x, m, h)) < TOL
+
+
+@pytest.mark.parametrize("nt,ns", [(1, 7000), (700, 3), (5000, 1), (3000, 9000), (257, 1025)])
+def test_field_rectangular(mf, cuda, oracle, nt, ns):
+    rng = np.random.default_rng(nt * 7 + ns)
+    t = rng.random((nt, 3)).astype(np.float32)
+    s = (rng.random((ns, 3)) * 1.4 - 0.2).astype(np.float32)
+    m = rng.normal(size=(ns, 3)).astype(np.float32)
+    got = mf.direct_field(dev(cuda, t), dev(cuda, s), dev(cuda, m), 0.09).cpu().numpy()
+    assert rel(got, oracle.field(t, s, m, 0.09)) < TOL
+
+
+@pytest.mark.parametrize("n", [2, 33, 513, 4096])
+def test_tensor_sizes(mf, cuda, oracle, n):
+    rng = np.random.default_rng(100 + n)
+    x = rng.random((n, 3)).astype(np.float32)
+    m = rng.normal(size=(n, 3)).astype(np.float32)
+    h = 0.05
+    got = mf.direct_force_tensor(dev(cuda, x), dev(cuda, x), dev(cuda, m), h).cpu().numpy()
+    assert rel(got, oracle.tensor_sum(x, x, m, h)) < 2 * TOL
+
+
+@pytest.mark.parametrize("n", [2, 64, 1000, 4096])
+@pytest.mark.parametrize("naive", [False, True])
+def test_force_with_external_tensor(mf, cuda, oracle, n, naive):
+    rng = np.random.default_rng(200 + n)
+    x = rng.random((n, 3)).astype(np.float32)
+    m = (rng.normal(size=(n, 3)) * 1e-3).astype(np.float32)
+    h = 0.06
+    ext_s = rng.random((5, 3)).astype(np.float32) * 2 - 0.5
+    ext_m = rng.normal(size=(5, 3)).astype(np.float32)
+    _, rext = oracle.ext(x, ext_s, ext_m, [0, 0, 1], 0.1)
+    rext32 = rext.astype(np.float32)
+    got = mf.direct_force(dev(cuda, x), dev(cuda, m), h, dev(cuda, rext32, 9), naive_quirks=naive).cpu().numpy()
+    want = oracle.force(x, m, h, rext32, naive_quirks=naive)
+    assert rel(got, want) < TOL
+
+
+def test_force_sums_to_zero(mf, cuda, oracle):
+    # internal forces are pairwise antisymmetric: sum_i F_i = 0
+    rng = np.random.default_rng(9)
+    n = 6000
+    x = rng.random((n, 3)).astype(np.float32)
+    m = (rng.normal(size=(n, 3)) * 1e-3).astype(np.float32)
+    F = mf.direct_force(dev(cuda, x), dev(cuda, m), 0.03).cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(F.sum(axis=0)) < 1e-5 * np.abs(F).sum()
+
+
+def test_coincident_particles(mf, cuda, oracle):
+    # distinct particles at the same position: field keeps the r = 0 term,
+    # the force tensor drops it; nothing is NaN
+    x = np.float32([[0.1, 0.2, 0.3]] * 3 + [[0.5, 0.5, 0.5]])
+    m = np.float32([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1]])
+    f = mf.direct_field(dev(cuda, x), dev(cuda, x), dev(cuda, m), 0.2).cpu().numpy()
+    T = mf.direct_force_tensor(dev(cuda, x), dev(cuda, x), dev(cuda, m), 0.2).cpu().numpy()
+    assert np.all(np.isfinite(f)) and np.all(np.isfinite(T))
+    assert rel(f, oracle.field(x, x, m, 0.2)) < TOL
+    assert rel(T, oracle.tensor_sum(x, x, m, 0.2)) < 2 * TOL
+
+
+def test_empty_and_invalid(mf, cuda):
+    t = dev(cuda, np.zeros((4, 3)))
+    s = cuda.empty((0, 3), dtype=cuda.float32, device="cuda")
+    out = mf.direct_field(t, s, s, 0.1).cpu().numpy()
+    assert np.all(out == 0)
+    with pytest.raises(mf.MFError) as e:
+        mf.direct_field(t, t, t, -1.0)
+    assert e.value.status == 1
+
+
+def test_deterministic(mf, cuda):
+    rng = np.random.default_rng(11)
+    x = dev(cuda, rng.random((20000, 3)))
+    m = dev(cuda, rng.normal(size=(20000, 3)))
+    a = mf.direct_field(x, x, m, 0.02).cpu().numpy()
+    b = mf.direct_field(x, x, m, 0.02).cpu().numpy()
+    assert np.array_equal(a, b)
+
+
+def test_large_subsample(mf, cuda, oracle):
+    # 65,536 particles: check 512 targets against the FP64 oracle
+    import scenes
+    sc = scenes.config_allpairs_65k()
+    rng = np.random.default_rng(12)
+    m = (rng.normal(size=(sc.n, 3)) * sc.volume).astype(np.float32)
+    x = dev(cuda, sc.pos)
+    got = mf.direct_field(x, x, dev(cuda, m), sc.h).cpu().numpy()
+    idx = rng.choice(sc.n, 512, replace=False)
+    want = oracle.field(sc.pos[idx], sc.pos, m, sc.h)
+    assert rel(got[idx], want) < TOL
