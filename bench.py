@@ -1,0 +1,421 @@
+#!/usr/bin/env python
+"""Pair interactions per second of the magnetization-and-force step on GB300.
+
+Workload (default): N = 65,536 particles, jittered cubic lattice (jitter
++-0.25 spacing, seed 1) filling a sphere of radius 0.5, h = 2 x spacing,
+chi = 2, H0 = (0,0,1), FP32 pair arithmetic with compensated accumulation,
+FP64 solver inner products.  One step = one timestep: CG solve of the
+magnetization (warm start, relative residual 1e-6), the Kelvin force, and a
+symplectic Euler update with dt = 1e-4, all on the device.
+
+Printed (rank 0, one JSON line):
+  value      executed pair interactions (field + force) / device time, inputs
+             resident in HBM; L2 flushed (256 MiB write) before every timed step
+  e2e        the same metric through the public API with host buffers: every
+             step uploads positions from pinned memory, solves, evaluates the
+             force, reads M, B/mu0 and F back and integrates on the host
+  roofline   FP32 FMA roofline of the dominant all-pairs kernel: algorithmic
+             FLOP (32 per field pair, 53 per force pair) / its event-timed
+             device time, against a dense-FFMA throughput measured in this run
+  cpu_baseline  the CPU restatement of the reference's pair kernels (FP32,
+             OpenMP over all host cores) on a bounded sample of the same step
+
+``--impl reference`` times that CPU implementation alone (see run_reference).
+Multi-GPU: one independent replica per rank (the step has no exchange), value
+summed over ranks, time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "magnetic-force_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+FLOP_FIELD_PAIR = 32.0  # minimal far-field form, FMA = 2, rsqrt = 1
+FLOP_FORCE_PAIR = 53.0
+METRIC = "pair interactions/s; p50/p99 step latency, served vs plain at 1e-5 rel err"
+UNIT = "pairs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dt", type=float, default=1e-4)
+    ap.add_argument("--n", type=int, default=65536)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_pair_rates(pos: np.ndarray, mom: np.ndarray, h: float, seconds: float):
+    """FP32 CPU restatement of the reference's DipoleBKernel / DipoleHessianKernel
+    (fmmtl::direct split over targets with OpenMP), timed on target chunks
+    against all sources.  Returns (field pairs/s, force pairs/s, sample text)."""
+    import oracle as orc
+    o = orc.Oracle()
+    n = len(pos)
+    rates = {}
+    done = {}
+    for kind in ("field", "force"):
+        budget = seconds / 2
+        pairs = 0.0
+        t_used = 0.0
+        start = 0
+        chunk = 1024 if kind == "field" else 256
+        while t_used < budget:
+            idx = np.arange(start, start + chunk) % n
+            t0 = time.perf_counter()
+            if kind == "field":
+                o.field(pos[idx], pos, mom, h, prec=32)
+            else:
+                o.tensor_sum(pos[idx], pos, mom, h, prec=32)
+            t_used += time.perf_counter() - t0
+            pairs += chunk * n
+            start += chunk
+        rates[kind] = pairs / t_used
+        done[kind] = (pairs, t_used)
+    sample = (f"field: {int(done['field'][0] / n)} targets x {n} sources in {done['field'][1]:.1f} s; "
+              f"force tensor: {int(done['force'][0] / n)} targets x {n} sources in {done['force'][1]:.1f} s")
+    return rates["field"], rates["force"], sample
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import mfgb
+    import scenes
+
+    torch.cuda.set_device(local)
+    sc = scenes.config_allpairs_65k() if args.n == 65536 else scenes.jittered_lattice(args.n, "sphere", 0.5, chi=2.0)
+    n = sc.n
+    s = mfgb.Solver(n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
+    s.set_option("solver", mfgb.SOLVER_CG)
+    s.set_option("rel_tol", 1e-6)
+    s.set_option("kernel_timing", 1)
+
+    # cold solve (reported) + warm-up steps
+    t0 = time.perf_counter()
+    cold_iters, cold_res = s.solve(500)
+    torch.cuda.synchronize()
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(args.warmup):
+        s.advance(args.dt, 500)
+    torch.cuda.synchronize()
+
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > 129 MB L2
+    s.reset_counters()
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms = []
+    iters = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        iters.append(s.advance(args.dt, 500))
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ctr = s.counters()
+    kf = s.kernel_stats("field")
+    kg = s.kernel_stats("force")
+    total_ms = sum(step_ms)
+    pairs = ctr["field_pairs"] + ctr["force_pairs"]
+    t_max = allreduce_max(total_ms, world)
+    pairs_all = allreduce_sum(pairs, world)
+    value = pairs_all / (t_max * 1e-3)
+
+    # dominant all-pairs kernel and its FP32 roofline
+    peak = mfgb.probe_fp32_peak()
+    kern = {}
+    for name, st, fpp in (("field", kf, FLOP_FIELD_PAIR), ("force", kg, FLOP_FORCE_PAIR)):
+        if st["launches"]:
+            kern[name] = {"launches": st["launches"], "total_ms": round(st["total_ms"], 4),
+                          "avg_ms": round(st["total_ms"] / st["launches"], 4),
+                          "pairs_per_launch": st["pairs"] / st["launches"],
+                          "tflops": fpp * st["pairs"] / (st["total_ms"] * 1e-3) / 1e12,
+                          "pairs_per_s": st["pairs"] / (st["total_ms"] * 1e-3)}
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    ach = kern[dom]["tflops"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(f"allpairs_{dom}_fp32_65536")
+    roofline = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": f"allpairs_kernel<{dom}>",
+                "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
+                "kernels": kern,
+                "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores; "
+                        "HBM traffic per launch is ~1 MB of particle records"}
+
+    # accuracy on a sample: fixed-point residual and force, FP64 oracle
+    errors = None
+    if rank == 0:
+        errors = sample_errors(s, sc)
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(s, sc, args, world)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        M = s.M
+        rf, rg, sample = cpu_pair_rates(sc.pos, M, sc.h, args.cpu_seconds)
+        fp = ctr["field_pairs"]
+        gp = ctr["force_pairs"]
+        cpu_time = fp / rf + gp / rg
+        cpu = {"value": (fp + gp) / cpu_time, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+               "sample": sample + "; value = the timed step's field/force pair mix at these rates",
+               "field_pairs_per_s": rf, "force_pairs_per_s": rg}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered-lattice sphere (the reference ships no dataset)",
+            "config": {"workload": f"allpairs_fp32_{n}: jittered lattice sphere r=0.5, N={n}, h=2*spacing="
+                                   f"{sc.h:.5f}, chi=2, H0=(0,0,1), dt={args.dt}, CG rel tol 1e-6",
+                       "N": n, "step": "one timestep: warm-started CG solve + Kelvin force + symplectic Euler",
+                       "l2": "flushed before every timed step (256 MiB write, not timed)",
+                       "parallelism": f"replicas x{world}"},
+            "field_pairs": ctr["field_pairs"], "force_pairs": ctr["force_pairs"],
+            "solve_iters_per_step": iters, "step_ms": [round(v, 4) for v in step_ms],
+            "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+            "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
+            "gpu_launches": ctr["kernel_launches"],
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "errors": errors, "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    s.close()
+
+
+def sample_errors(s, sc, k: int = 256):
+    """Relative fixed-point residual |b - Hext - c G b| / |Hext| and force
+    error on k sample particles, both with FP64 oracle sums over all N."""
+    import oracle as orc
+    o = orc.Oracle()
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(sc.n, size=min(k, sc.n), replace=False))
+    pos = s.xyz.astype(np.float64)
+    b = s.get("total_B_over_mu0", f64=True)
+    M = s.get("M", f64=True)
+    Hext = s.get("Hext", f64=True)
+    F = s.get("magnetic_bodyforce", f64=True)
+    G = o.field(pos[idx], pos, M, sc.h)
+    r = b[idx] - Hext[idx] - G
+    T = o.tensor_sum(pos[idx], pos, M, sc.h).reshape(-1, 3, 3)  # [i][col][row]
+    Fo = np.einsum("icr,ic->ir", T, M[idx])
+    return {"sample": int(len(idx)),
+            "fixed_point_rel_residual": float(np.linalg.norm(r) / np.linalg.norm(Hext[idx])),
+            "force_rel_l2": float(np.linalg.norm(F[idx] - Fo) / np.linalg.norm(Fo))}
+
+
+def run_e2e(s, sc, args, world):
+    import torch
+    n = sc.n
+    pin = lambda: torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+    pos, F, B, M = pin(), pin(), pin(), pin()
+    pos[:] = s.xyz
+    vel = np.zeros((n, 3), np.float32)
+    s.reset_counters()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.setTargetpos(pos)                 # H2D
+        s.solve(500)
+        s.evaluate_fitted_near_foece()
+        s.get("magnetic_bodyforce", out=F)  # D2H
+        s.get("total_B_over_mu0", out=B)
+        s.get("M", out=M)
+        vel += np.float32(args.dt) * F / np.float32(sc.volume)
+        pos += np.float32(args.dt) * vel
+    torch.cuda.synchronize()
+    dt_s = time.perf_counter() - t0
+    ctr = s.counters()
+    dt_max = allreduce_max(dt_s, world)
+    pairs = allreduce_sum(ctr["field_pairs"] + ctr["force_pairs"], world)
+    return {"value": pairs / dt_max, "unit": UNIT, "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": 3 * n * 12,
+            "ms_per_step": dt_max * 1e3 / args.steps, "path": "mf_set_positions/mf_solve/mf_eval_force/mf_get"}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path for this step: its pair kernels evaluated all-
+    pairs on the host (the CPU restatement, FP32, OpenMP over every core).
+    The reference sources are not present where this runs, so the port stands
+    in for them (the port is bit-identical to the reference's FP32 field
+    kernel and within 2e-6 on the force tensor, pinned by tests/test_oracle.py).
+    Each step is a bounded sample: 1024 field targets and 128 force targets
+    against all N sources; value = executed pairs / wall time."""
+    if rank != 0:
+        return
+    import oracle as orc
+    import scenes
+    sc = scenes.config_allpairs_65k() if args.n == 65536 else scenes.jittered_lattice(args.n, "sphere", 0.5, chi=2.0)
+    o = orc.Oracle()
+    n = sc.n
+    rng = np.random.default_rng(1)
+    mom = (rng.normal(size=(n, 3)) * sc.volume).astype(np.float32)
+    nf, ng = 1024, 128
+
+    def step(k):
+        i0 = (k * nf) % n
+        idx = np.arange(i0, i0 + nf) % n
+        o.field(sc.pos[idx], sc.pos, mom, sc.h, prec=32)
+        jdx = np.arange(i0, i0 + ng) % n
+        o.tensor_sum(sc.pos[jdx], sc.pos, mom, sc.h, prec=32)
+        return (nf + ng) * n
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    pairs = 0.0
+    for k in range(args.steps):
+        pairs += step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = pairs / dt
+    cores = cpu_threads()
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+           "data": "synthetic: seeded jittered-lattice sphere (the reference ships no dataset)",
+           "config": {"workload": f"allpairs_fp32_{n}: jittered lattice sphere r=0.5, N={n}, chi=2, H0=(0,0,1)",
+                      "N": n, "step": f"sample: {nf} field targets + {ng} force-tensor targets x {n} sources"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{nf}+{ng} targets x {n} sources per step, FP32, OpenMP {cores} threads"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -87,7 +87,9 @@ typedef enum mf_option {
   MF_OPT_REL_TOL = 4,       /* CG relative residual tolerance (default 1e-6 FP32, 1e-8 FP64) */
   MF_OPT_CG_MAX_ITER = 5,   /* CG iteration cap (default 500) */
   MF_OPT_CRIT_SIZE = 6,     /* accepted for compatibility (crit_size, :647); unused */
-  MF_OPT_CHECK_INTERVAL = 7 /* CG: iterations launched between host convergence checks (default 4) */
+  MF_OPT_CHECK_INTERVAL = 7,/* CG: iterations launched between host convergence checks
+                               (default 1 for N >= 16384, else 4) */
+  MF_OPT_KERNEL_TIMING = 8  /* 1: time every all-pairs launch with CUDA events (mf_get_kernel_stats) */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -184,6 +186,23 @@ typedef struct mf_counters {
 } mf_counters;
 mf_status mf_get_counters(mf_solver* s, mf_counters* c);
 mf_status mf_reset_counters(mf_solver* s);
+
+/* Per-kernel device time of a handle's all-pairs launches, measured with
+ * CUDA events on the handle's stream while MF_OPT_KERNEL_TIMING is on.
+ * Launches that found their solve already stopped are not counted.
+ * Reset by mf_reset_counters.  Synchronises the handle's stream. */
+typedef enum mf_kernel_kind { MF_K_FIELD = 0, MF_K_FORCE = 1, MF_K_TENSOR = 2 } mf_kernel_kind;
+typedef struct mf_kernel_stats {
+  int64_t launches;
+  double total_ms;
+  double pairs;
+} mf_kernel_stats;
+mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out);
+
+/* Measured dense FP32 FMA throughput of the current device in TFLOP/s
+ * (independent FFMA chains on every SM, timed with CUDA events): the
+ * denominator of the all-pairs kernels' roofline.  Not in the reference. */
+mf_status mf_probe_fp32_peak(double* tflops);
 
 /* ---------------------------------------------------------------------- */
 /* Direct all-pairs evaluation of the reference's pair kernels on device    */

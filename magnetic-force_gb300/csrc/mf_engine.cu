@@ -170,6 +170,8 @@ struct EngineBase {
   virtual mf_counters& counters() = 0;
   virtual void set_stream(cudaStream_t s) = 0;
   virtual cudaStream_t stream() const = 0;
+  virtual mf_status kernel_stats(int kind, mf_kernel_stats* out) = 0;
+  virtual void reset_stats() = 0;
   int device = 0;
 };
 
@@ -180,6 +182,7 @@ class Engine final : public EngineBase {
 
  public:
   ~Engine() override {
+    reset_stats();
     if (pinned_) cudaFreeHost(pinned_);
   }
 
@@ -439,7 +442,9 @@ class Engine final : public EngineBase {
       case MF_OPT_CHECK_INTERVAL:
         if (v < 1) return fail(MF_ERR_INVALID_ARG, "check interval must be >= 1");
         check_interval_ = int(v);
+        check_interval_set_ = true;
         return MF_OK;
+      case MF_OPT_KERNEL_TIMING: timing_ = v != 0.0; return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -454,7 +459,8 @@ class Engine final : public EngineBase {
       case MF_OPT_REL_TOL: *v = rel_tol_; return MF_OK;
       case MF_OPT_CG_MAX_ITER: *v = double(cg_max_iter_); return MF_OK;
       case MF_OPT_CRIT_SIZE: *v = crit_size_; return MF_OK;
-      case MF_OPT_CHECK_INTERVAL: *v = check_interval_; return MF_OK;
+      case MF_OPT_CHECK_INTERVAL: *v = interval(); return MF_OK;
+      case MF_OPT_KERNEL_TIMING: *v = timing_ ? 1.0 : 0.0; return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -580,10 +586,64 @@ class Engine final : public EngineBase {
   }
 
   mf_status run(const Plan<Real>& plan, const LaunchIO<Real>& io) {
-    MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+    if (!timing_) {
+      MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+    } else {
+      // Grow the scratch before the first event so the bracket holds the kernel only.
+      size_t pd = 0, nc = 0;
+      plan_scratch_needs(plan, &pd, &nc);
+      MF_TRY(scr_.ensure(pd, nc));
+      TimedLaunch t;
+      t.body = int(plan.body);
+      t.pairs = plan.pairs;
+      MF_CUDA_TRY(cudaEventCreate(&t.start));
+      MF_CUDA_TRY(cudaEventCreate(&t.stop));
+      MF_CUDA_TRY(cudaEventRecord(t.start, st_));
+      MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+      MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
+      timed_.push_back(t);
+    }
     ++ctr_.kernel_launches;
     return MF_OK;
   }
+
+ public:
+  mf_status kernel_stats(int kind, mf_kernel_stats* out) override {
+    if (kind < 0 || kind > 2 || !out) return fail(MF_ERR_INVALID_ARG, "bad kernel kind");
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    for (TimedLaunch& t : timed_) {
+      float ms = 0.f;
+      MF_CUDA_TRY(cudaEventElapsedTime(&ms, t.start, t.stop));
+      agg_[t.body].launches += t.skipped ? 0 : 1;
+      agg_[t.body].total_ms += ms;
+      agg_[t.body].pairs += t.skipped ? 0.0 : t.pairs;
+      cudaEventDestroy(t.start);
+      cudaEventDestroy(t.stop);
+    }
+    timed_.clear();
+    *out = agg_[kind];
+    return MF_OK;
+  }
+  void reset_stats() override {
+    cudaStreamSynchronize(st_);
+    for (TimedLaunch& t : timed_) {
+      cudaEventDestroy(t.start);
+      cudaEventDestroy(t.stop);
+    }
+    timed_.clear();
+    for (auto& a : agg_) a = mf_kernel_stats{};
+  }
+
+ private:
+  struct TimedLaunch {
+    int body = 0;
+    double pairs = 0;
+    bool skipped = false;
+    cudaEvent_t start = nullptr, stop = nullptr;
+  };
+  std::vector<TimedLaunch> timed_;
+  mf_kernel_stats agg_[3] = {};
+  bool timing_ = false;
 
   mf_status field(Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4, const R4* add4b,
                   const double* done = nullptr) {
@@ -684,7 +744,7 @@ class Engine final : public EngineBase {
     MF_TRY(read_scalars(row, 0, kScal));
     int64_t launched = 0;
     while (row[S_DONE] == 0.0 && launched < cap) {
-      for (int k = 0; k < check_interval_ && launched < cap; ++k, ++launched) {
+      for (int k = 0; k < interval() && launched < cap; ++k, ++launched) {
         MF_TRY(field(plan_cgq_, v4(V_P), v4(V_Q), v4(V_P), nullptr, done));
         MF_TRY(reduce(CgPq<R4>{v4(V_P), v4(V_Q)}));
         MF_TRY(reduce(CgUpdate<Real, R4>{v4(V_B), v4(V_R), v4(V_P), v4(V_Q)}));
@@ -696,6 +756,14 @@ class Engine final : public EngineBase {
     const int64_t executed = int64_t(row[S_ITERS]);
     ctr_.field_products -= (launched - executed);
     ctr_.field_pairs -= double(launched - executed) * plan_cgq_.pairs;
+    if (timing_) {
+      int64_t to_mark = launched - executed;  // the last field launches of this solve
+      for (auto it = timed_.rbegin(); it != timed_.rend() && to_mark > 0; ++it)
+        if (it->body == int(Body::Field)) {
+          it->skipped = true;
+          --to_mark;
+        }
+    }
     if (iters_out) *iters_out = executed;
     if (err_out) *err_out = row[S_RELRES];
     history_.push_back(row[S_RELRES]);
@@ -776,6 +844,8 @@ class Engine final : public EngineBase {
   double rel_tol_ = 1e-6;
   int64_t cg_max_iter_ = 500;
   int check_interval_ = 4;
+  bool check_interval_set_ = false;
+  int interval() const { return check_interval_set_ ? check_interval_ : (np_ >= 16384 ? 1 : 4); }
   int sms_ = 1;
   cudaStream_t st_ = nullptr;
   void* pinned_ = nullptr;
@@ -834,6 +904,56 @@ mf_status Engine<Real>::widen(const Real* src, double* dst, int64_t n) {
 
 template class Engine<float>;
 template class Engine<double>;
+
+// Dense FFMA throughput: 8 independent chains per thread, 8 CTAs of 256
+// threads per SM, 2 FLOP per FFMA.  The values stay bounded (|a| < 1) and a
+// never-true store keeps the chains alive.
+__global__ void __launch_bounds__(256) k_ffma_probe(float* sink, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1e-3f, x2 = x0 + 2e-3f, x3 = x0 + 3e-3f;
+  float x4 = x0 + 4e-3f, x5 = x0 + 5e-3f, x6 = x0 + 6e-3f, x7 = x0 + 7e-3f;
+#pragma unroll 4
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b);
+    x1 = fmaf(x1, a, b);
+    x2 = fmaf(x2, a, b);
+    x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b);
+    x5 = fmaf(x5, a, b);
+    x6 = fmaf(x6, a, b);
+    x7 = fmaf(x7, a, b);
+  }
+  const float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == -1.2345f) sink[0] = s;
+}
+
+mf_status probe_fp32_peak(double* tflops) {
+  const int dev = current_device();
+  const int sms = device_sms(dev);
+  DevBuf sink;
+  MF_TRY(sink.reserve(16));
+  const int iters = 1 << 14;
+  const unsigned grid = unsigned(sms * 8);
+  cudaEvent_t e0, e1;
+  MF_CUDA_TRY(cudaEventCreate(&e0));
+  MF_CUDA_TRY(cudaEventCreate(&e1));
+  k_ffma_probe<<<grid, 256>>>(sink.as<float>(), iters, 0.999999f, 1e-7f);  // warm-up
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0);
+    k_ffma_probe<<<grid, 256>>>(sink.as<float>(), iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MF_CUDA_TRY(cudaGetLastError());
+  const double flops = 2.0 * 8.0 * double(iters) * double(grid) * 256.0;
+  *tflops = flops / (double(best) * 1e-3) / 1e12;
+  return MF_OK;
+}
 
 }  // namespace mfgb
 
@@ -1018,8 +1138,18 @@ mf_status mf_get_counters(mf_solver* s, mf_counters* c) {
 mf_status mf_reset_counters(mf_solver* s) {
   return guarded(s, [&](EngineBase& e) {
     e.counters() = mf_counters{};
+    e.reset_stats();
     return MF_OK;
   });
+}
+
+mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out) {
+  return guarded(s, [&](EngineBase& e) { return e.kernel_stats(kind, out); });
+}
+
+mf_status mf_probe_fp32_peak(double* tflops) {
+  if (!tflops) return fail(MF_ERR_INVALID_ARG, "NULL");
+  return mfgb::probe_fp32_peak(tflops);
 }
 
 }  // extern "C"

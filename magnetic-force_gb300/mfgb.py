@@ -39,7 +39,7 @@ FP32, FP64 = 0, 1
 Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyforce": 4,
      "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
-       "crit_size": 6, "check_interval": 7}
+       "crit_size": 6, "check_interval": 7, "kernel_timing": 8}
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
 
@@ -63,6 +63,12 @@ class mf_counters(ctypes.Structure):
                 ("field_pairs", ctypes.c_double), ("force_pairs", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64)]
 
+
+class mf_kernel_stats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int64), ("total_ms", ctypes.c_double), ("pairs", ctypes.c_double)]
+
+
+KERNEL = {"field": 0, "force": 1, "tensor": 2}
 
 _lib = None
 
@@ -103,6 +109,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_direct_force_tensor": (i32, [vp, i64, vp, vp, i64, f32, vp, vp]),
         "mf_direct_force": (i32, [vp, vp, i64, f32, vp, i32, vp, vp]),
         "mf_release_scratch": (i32, []),
+        "mf_get_kernel_stats": (i32, [vp, i32, ctypes.POINTER(mf_kernel_stats)]),
+        "mf_probe_fp32_peak": (i32, [ctypes.POINTER(f64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -229,9 +237,12 @@ class Solver:
         check(load().mf_num_particles(self._h, ctypes.byref(n)))
         return n.value
 
-    def get(self, quantity: str, f64: bool = False) -> np.ndarray:
+    def get(self, quantity: str, f64: bool = False, out: np.ndarray | None = None) -> np.ndarray:
         n = self.np
-        out = np.empty((n, 3), dtype=np.float64 if f64 else np.float32)
+        if out is None:
+            out = np.empty((n, 3), dtype=np.float64 if f64 else np.float32)
+        assert out.flags["C_CONTIGUOUS"] and out.size == 3 * n
+        assert out.dtype == (np.float64 if f64 else np.float32)
         fn = load().mf_get_f64 if f64 else load().mf_get
         check(fn(self._h, Q[quantity], out.ctypes.data, LAYOUT_AOS, HOST))
         return out
@@ -260,6 +271,11 @@ class Solver:
     def reset_counters(self):
         check(load().mf_reset_counters(self._h))
 
+    def kernel_stats(self, kind: str) -> dict:
+        st = mf_kernel_stats()
+        check(load().mf_get_kernel_stats(self._h, KERNEL[kind], ctypes.byref(st)))
+        return {"launches": st.launches, "total_ms": st.total_ms, "pairs": st.pairs}
+
     def set_option(self, key: str, value: float):
         check(load().mf_set_option(self._h, OPT[key], float(value)))
 
@@ -281,6 +297,13 @@ class Solver:
     max_iteration = property(lambda self: int(self.get_option("max_iteration")),
                              lambda self, v: self.set_option("max_iteration", v))
     naive = property(lambda self: bool(self.get_option("naive")), lambda self, v: self.set_option("naive", 1 if v else 0))
+
+
+def probe_fp32_peak() -> float:
+    """Measured dense FP32 FMA throughput of the current device, TFLOP/s."""
+    v = ctypes.c_double(0)
+    check(load().mf_probe_fp32_peak(ctypes.byref(v)))
+    return v.value
 
 
 # -- direct evaluation on device buffers (torch CUDA tensors) -----------------
