@@ -233,6 +233,22 @@ mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h
 /* Frees the scratch the mf_direct_* calls keep per device. */
 mf_status mf_release_scratch(void);
 
+/* mf_direct_field without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- hosts that
+ * have handed the device's whole memory budget to their own pool allocator,
+ * or loops that cannot take cudaMalloc's device-wide synchronisation.  All
+ * scratch (about 11.5 MiB: packed copies of the inputs, FP64 partial sums,
+ * tickets, an error word) lives in one static device array that every GPU
+ * loading the library holds until the process exits.  Same arguments and
+ * results as mf_direct_field; nt and ns must each be at most 65,536
+ * (MF_ERR_INVALID_ARG otherwise).  The first call on a device, with that
+ * device current, looks up the array's device address; make it before any
+ * stream capture.  Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  Returns after the results are
+ * written (synchronises `stream`). */
+mf_status mf_direct_field_noalloc(const float* targets, int64_t nt, const float* sources,
+                                  const float* charges, int64_t ns, float h, float* results, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
