@@ -125,6 +125,20 @@ template <class Real>
 struct BodyOf<Real, Body::Tensor> {
   using type = TensorBody<Real>;
 };
+template <>
+struct BodyOf<float, Body::FieldF2> {
+  using type = FieldF2Body;
+};
+template <>
+struct BodyOf<float, Body::ForceF2> {
+  using type = ForceF2Body;
+};
+
+// Packed two-source bodies exist in FP32 only.
+template <class Real>
+constexpr bool has_f2() {
+  return std::is_same<Real, float>::value;
+}
 
 template <class Real, Body B>
 struct Launcher {
@@ -176,6 +190,7 @@ struct Launcher {
     a.naive_quirks = io.naive_quirks;
     a.done_flags = io.done_flags;
     a.done_stride = io.done_stride;
+    a.corr4 = io.corr4;
     a.partials = partials;
     a.counters = counters;
     a.err = err;
@@ -203,9 +218,17 @@ static void cfg_of(Body b, int* tile, int* tbt) {
       *tile = KCfg<Real, Body::Force>::TILE;
       *tbt = KCfg<Real, Body::Force>::TPB * KCfg<Real, Body::Force>::TPT;
       break;
-    default:
+    case Body::Tensor:
       *tile = KCfg<Real, Body::Tensor>::TILE;
       *tbt = KCfg<Real, Body::Tensor>::TPB * KCfg<Real, Body::Tensor>::TPT;
+      break;
+    case Body::FieldF2:
+      *tile = KCfg<float, Body::FieldF2>::TILE;
+      *tbt = KCfg<float, Body::FieldF2>::TPB * KCfg<float, Body::FieldF2>::TPT;
+      break;
+    case Body::ForceF2:
+      *tile = KCfg<float, Body::ForceF2>::TILE;
+      *tbt = KCfg<float, Body::ForceF2>::TPB * KCfg<float, Body::ForceF2>::TPT;
       break;
   }
 }
@@ -271,7 +294,13 @@ void plan_scratch_needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
   switch (plan.body) {
     case Body::Field: Launcher<Real, Body::Field>::needs(plan, pd, nc); break;
     case Body::Force: Launcher<Real, Body::Force>::needs(plan, pd, nc); break;
-    default: Launcher<Real, Body::Tensor>::needs(plan, pd, nc); break;
+    case Body::Tensor: Launcher<Real, Body::Tensor>::needs(plan, pd, nc); break;
+    case Body::FieldF2:
+      if constexpr (has_f2<Real>()) Launcher<float, Body::FieldF2>::needs(plan, pd, nc);
+      break;
+    case Body::ForceF2:
+      if constexpr (has_f2<Real>()) Launcher<float, Body::ForceF2>::needs(plan, pd, nc);
+      break;
   }
 }
 
@@ -281,8 +310,15 @@ mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double*
   switch (plan.body) {
     case Body::Field: return Launcher<Real, Body::Field>::launch(plan, io, partials, counters, err, st);
     case Body::Force: return Launcher<Real, Body::Force>::launch(plan, io, partials, counters, err, st);
-    default: return Launcher<Real, Body::Tensor>::launch(plan, io, partials, counters, err, st);
+    case Body::Tensor: return Launcher<Real, Body::Tensor>::launch(plan, io, partials, counters, err, st);
+    case Body::FieldF2:
+      if constexpr (has_f2<Real>()) return Launcher<float, Body::FieldF2>::launch(plan, io, partials, counters, err, st);
+      break;
+    case Body::ForceF2:
+      if constexpr (has_f2<Real>()) return Launcher<float, Body::ForceF2>::launch(plan, io, partials, counters, err, st);
+      break;
   }
+  return fail(MF_ERR_UNSUPPORTED, "packed two-source kernels exist in FP32 only");
 }
 
 template <class Real>

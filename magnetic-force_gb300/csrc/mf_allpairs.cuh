@@ -67,6 +67,8 @@ struct AllPairsArgs {
   // non-zero is skipped (its outputs are left as they are).
   const double* done_flags;
   int32_t done_stride;
+  // Optional near-field correction per target (added before the epilogue's scale).
+  const R4* corr4;
   double* partials;    // [grid][2][TPB*TPT][kOut]
   int32_t* counters;   // [total target blocks], zero between launches
   int32_t* err;        // device error word
@@ -75,8 +77,41 @@ struct AllPairsArgs {
 // ----------------------------------------------------------------------------
 // Bodies: what a pair adds and how a target's result is written.
 // ----------------------------------------------------------------------------
+// Source tiles as one packed record per source: item j = record j.
 template <class Real>
-struct FieldBody {
+struct RecordItems {
+  using R4 = typename Vec4T<Real>::type;
+  struct Item {
+    R4 p, m;
+  };
+  __device__ static Item load_item(const R4* sp, const R4* sm, int j) { return Item{sp[j], sm[j]}; }
+  __device__ static int items(int cnt) { return cnt; }
+  __host__ __device__ static uint32_t tile_bytes(int cnt) { return uint32_t(cnt) * uint32_t(sizeof(R4)); }
+};
+
+// Per-target tile accumulator of kAcc scalars.
+template <class Real, int N>
+struct ScalarAcc {
+  Real v[N];
+  __device__ void zero() {
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = Real(0);
+  }
+};
+
+// Adds the near-field correction of target i (if the launch has one) to v.
+template <class Real>
+__device__ __forceinline__ void add_correction(const AllPairsArgs<Real>& a, int64_t i, double* v) {
+  if (a.corr4) {
+    const typename Vec4T<Real>::type c = a.corr4[i];
+    v[0] += double(c.x);
+    v[1] += double(c.y);
+    v[2] += double(c.z);
+  }
+}
+
+template <class Real>
+struct FieldBody : RecordItems<Real> {
   using R4 = typename Vec4T<Real>::type;
   static constexpr int kAcc = 6;
   static constexpr int kOut = 3;
@@ -89,18 +124,23 @@ struct FieldBody {
     t.y = p.y;
     t.z = p.z;
   }
-  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
-                              Real* acc) {
-    field_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc, acc + 3);
+  using Acc = ScalarAcc<Real, kAcc>;
+  __device__ static void pair(const TData& t, const typename RecordItems<Real>::Item& it,
+                              const PairConsts<Real>& pc, Acc& acc) {
+    const R4& sp = it.p;
+    const R4& sm = it.m;
+    field_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc.v, acc.v + 3);
   }
-  __device__ static void tile_out(const Real* acc, Real* o) {
+  __device__ static void tile_out(const Acc& acc, Real* o) {
     const Real c = Real(kInv4Pi);
-    o[0] = (Real(3) * acc[0] - acc[3]) * c;
-    o[1] = (Real(3) * acc[1] - acc[4]) * c;
-    o[2] = (Real(3) * acc[2] - acc[5]) * c;
+    o[0] = (Real(3) * acc.v[0] - acc.v[3]) * c;
+    o[1] = (Real(3) * acc.v[1] - acc.v[4]) * c;
+    o[2] = (Real(3) * acc.v[2] - acc.v[5]) * c;
   }
   __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
-                                  const TData&, const double* v) {
+                                  const TData&, const double* vin) {
+    double v[3] = {vin[0], vin[1], vin[2]};
+    add_correction(a, i, v);
     Real o[3];
     for (int k = 0; k < 3; ++k) o[k] = Real(v[k]) * sc.scale + sc.cvec[k];
     if (a.add4) {
@@ -132,7 +172,11 @@ struct FieldBody {
 };
 
 template <class Real>
-struct ForceBody {
+__device__ __forceinline__ void force_epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
+                                               double mx, double my, double mz, const double* v);
+
+template <class Real>
+struct ForceBody : RecordItems<Real> {
   using R4 = typename Vec4T<Real>::type;
   static constexpr int kAcc = 3;
   static constexpr int kOut = 3;
@@ -149,24 +193,36 @@ struct ForceBody {
     t.my = m.y;
     t.mz = m.z;
   }
-  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
-                              Real* acc) {
-    force_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc);
+  using Acc = ScalarAcc<Real, kAcc>;
+  __device__ static void pair(const TData& t, const typename RecordItems<Real>::Item& it,
+                              const PairConsts<Real>& pc, Acc& acc) {
+    const R4& sp = it.p;
+    const R4& sm = it.m;
+    force_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc.v);
   }
-  __device__ static void tile_out(const Real* acc, Real* o) {
+  __device__ static void tile_out(const Acc& acc, Real* o) {
     const Real c = Real(kForceK);
-    o[0] = acc[0] * c;
-    o[1] = acc[1] * c;
-    o[2] = acc[2] * c;
+    o[0] = acc.v[0] * c;
+    o[1] = acc.v[1] * c;
+    o[2] = acc.v[2] * c;
   }
-  // F = (sum_j T_ij) m_i + external part (magnetic_force.cu:968-980 by default;
-  // :583-603 with the naive path's extra mu0 when naive_quirks is set).
   __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
                                   const TData& t, const double* v) {
+    force_epilogue<Real>(a, sc, i, double(t.mx), double(t.my), double(t.mz), v);
+  }
+};
+
+// F = (sum_j T_ij) m_i + external part (magnetic_force.cu:968-980 by default;
+// :583-603 with the naive path's extra mu0 when naive_quirks is set).
+template <class Real>
+__device__ __forceinline__ void force_epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
+                                               double mx, double my, double mz, const double* v) {
+  {
     double f[3] = {v[0], v[1], v[2]};
+    add_correction(a, i, f);
     if (a.rext[0]) {
       // rext[c*3 + r] = column c, row r; the tensor is symmetric.
-      const double m[3] = {double(t.mx), double(t.my), double(t.mz)};
+      const double m[3] = {mx, my, mz};
       double e[3];
       for (int r = 0; r < 3; ++r) {
         e[r] = 0.0;
@@ -179,10 +235,10 @@ struct ForceBody {
     a.out[1][i] = Real(f[1] * double(sc.scale));
     a.out[2][i] = Real(f[2] * double(sc.scale));
   }
-};
+}
 
 template <class Real>
-struct TensorBody {
+struct TensorBody : RecordItems<Real> {
   using R4 = typename Vec4T<Real>::type;
   static constexpr int kAcc = 6;
   static constexpr int kOut = 6;
@@ -195,13 +251,16 @@ struct TensorBody {
     t.y = p.y;
     t.z = p.z;
   }
-  __device__ static void pair(const TData& t, const R4& sp, const R4& sm, const PairConsts<Real>& pc,
-                              Real* acc) {
-    tensor_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc);
+  using Acc = ScalarAcc<Real, kAcc>;
+  __device__ static void pair(const TData& t, const typename RecordItems<Real>::Item& it,
+                              const PairConsts<Real>& pc, Acc& acc) {
+    const R4& sp = it.p;
+    const R4& sm = it.m;
+    tensor_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc.v);
   }
-  __device__ static void tile_out(const Real* acc, Real* o) {
+  __device__ static void tile_out(const Acc& acc, Real* o) {
     const Real c = Real(kForceK);
-    for (int k = 0; k < 6; ++k) o[k] = acc[k] * c;
+    for (int k = 0; k < 6; ++k) o[k] = acc.v[k] * c;
   }
   // Writes the 3x3 in the reference's layout: out[c*3 + r] = T(row r, col c).
   __device__ static void epilogue(const AllPairsArgs<Real>& a, const SceneDesc<Real>& sc, int64_t i,
@@ -218,6 +277,98 @@ struct TensorBody {
     a.out[6][i] = xz;
     a.out[7][i] = yz;
     a.out[8][i] = zz;
+  }
+};
+
+// ----------------------------------------------------------------------------
+// Packed two-source bodies (FP32).  Source arrays are in pair layout: sources
+// 2p and 2p+1 share two float4 records (x_a, x_b, y_a, y_b), (z_a, z_b, 0, 0),
+// the same 16 bytes per source as the record layout, so tiles stage the same
+// way.  A scene's sources start at an even index; an odd scene ends with a
+// zero-dipole partner, which contributes exactly zero.  Every pair takes the
+// far form with r^2 clamped to the near radius; the near-field correction of
+// each target (mf_cells.cu) is added in the epilogue.
+// ----------------------------------------------------------------------------
+struct PairItems {
+  struct Item {
+    float2 x, y, z, mx, my, mz;
+  };
+  __device__ static Item load_item(const float4* sp, const float4* sm, int j) {
+    const float4 p0 = sp[2 * j], p1 = sp[2 * j + 1];
+    const float4 m0 = sm[2 * j], m1 = sm[2 * j + 1];
+    return Item{make_float2(p0.x, p0.y), make_float2(p0.z, p0.w), make_float2(p1.x, p1.y),
+                make_float2(m0.x, m0.y), make_float2(m0.z, m0.w), make_float2(m1.x, m1.y)};
+  }
+  __device__ static int items(int cnt) { return (cnt + 1) >> 1; }
+  __host__ __device__ static uint32_t tile_bytes(int cnt) { return uint32_t((cnt + 1) >> 1) * 32u; }
+};
+
+struct FieldF2Body : PairItems {
+  static constexpr int kOut = 3;
+  struct TData {
+    float2 x, y, z;
+  };
+  struct Acc {
+    float2 s1[3], s2[3];
+    __device__ void zero() {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s1[k] = s2[k] = make_float2(0.f, 0.f);
+    }
+  };
+  __device__ static void load(const AllPairsArgs<float>& a, int64_t i, TData& t) {
+    const float4 p = a.tpos[i];
+    t.x = f2_dup(p.x);
+    t.y = f2_dup(p.y);
+    t.z = f2_dup(p.z);
+  }
+  __device__ static void pair(const TData& t, const Item& it, const PairConsts<float>& pc, Acc& acc) {
+    field_pair2(t.x, t.y, t.z, it.x, it.y, it.z, it.mx, it.my, it.mz, pc.near2_field, acc.s1, acc.s2);
+  }
+  __device__ static void tile_out(const Acc& acc, float* o) {
+    const float c = float(kInv4Pi);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      o[k] = (3.f * (acc.s1[k].x + acc.s1[k].y) - (acc.s2[k].x + acc.s2[k].y)) * c;
+  }
+  __device__ static void epilogue(const AllPairsArgs<float>& a, const SceneDesc<float>& sc, int64_t i,
+                                  const TData&, const double* v) {
+    FieldBody<float>::epilogue(a, sc, i, FieldBody<float>::TData{}, v);
+  }
+};
+
+struct ForceF2Body : PairItems {
+  static constexpr int kOut = 3;
+  struct TData {
+    float2 x, y, z, mx, my, mz;
+  };
+  struct Acc {
+    float2 f[3];
+    __device__ void zero() {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) f[k] = make_float2(0.f, 0.f);
+    }
+  };
+  __device__ static void load(const AllPairsArgs<float>& a, int64_t i, TData& t) {
+    const float4 p = a.tpos[i];
+    const float4 m = a.tmom[i];
+    t.x = f2_dup(p.x);
+    t.y = f2_dup(p.y);
+    t.z = f2_dup(p.z);
+    t.mx = f2_dup(m.x);
+    t.my = f2_dup(m.y);
+    t.mz = f2_dup(m.z);
+  }
+  __device__ static void pair(const TData& t, const Item& it, const PairConsts<float>& pc, Acc& acc) {
+    force_pair2(t.x, t.y, t.z, t.mx, t.my, t.mz, it.x, it.y, it.z, it.mx, it.my, it.mz, pc.near2_force, acc.f);
+  }
+  __device__ static void tile_out(const Acc& acc, float* o) {
+    const float c = float(kForceK);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = (acc.f[k].x + acc.f[k].y) * c;
+  }
+  __device__ static void epilogue(const AllPairsArgs<float>& a, const SceneDesc<float>& sc, int64_t i,
+                                  const TData& t, const double* v) {
+    force_epilogue<float>(a, sc, i, double(t.mx.x), double(t.my.x), double(t.mz.x), v);
   }
 };
 
@@ -252,7 +403,6 @@ template <class Real, class Body, int TPB, int TPT, int TILE, int STAGES>
 __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> a) {
   using R4 = typename Vec4T<Real>::type;
   constexpr int TBT = TPB * TPT;
-  constexpr int kAcc = Body::kAcc;
   constexpr int kOut = Body::kOut;
   constexpr bool kComp = sizeof(Real) == 4;  // compensate FP32 running sums
 
@@ -270,13 +420,10 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
   // A single-scene launch whose solve has already stopped does nothing.
   if (a.done_flags && a.n_scenes == 1 && a.done_flags[0] != 0.0) return;
 
-  R4* stage_pos[STAGES];
-  R4* stage_mom[STAGES];
-#pragma unroll
-  for (int s = 0; s < STAGES; ++s) {
-    stage_pos[s] = reinterpret_cast<R4*>(smem_raw + s * StageLayout<Real, TILE>::kBytes);
-    stage_mom[s] = stage_pos[s] + TILE;
-  }
+  // Stage s: TILE source positions, then TILE source dipoles (computed, not
+  // tabulated, so a runtime stage index does not put the table in local memory).
+  auto stage_pos = [&](int s) { return reinterpret_cast<R4*>(smem_raw + s * StageLayout<Real, TILE>::kBytes); };
+  auto stage_mom = [&](int s) { return stage_pos(s) + TILE; };
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&full_bar[s], 1);
@@ -293,10 +440,10 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
     const int64_t first = sc.s_off + int64_t(tile) * TILE;
     const int64_t rem = sc.ns - int64_t(tile) * TILE;
     const uint32_t cnt = uint32_t(rem < TILE ? rem : TILE);
-    const uint32_t bytes = cnt * uint32_t(sizeof(R4));
+    const uint32_t bytes = Body::tile_bytes(cnt);
     mbar_arrive_expect_tx(&full_bar[s], 2 * bytes);
-    bulk_g2s(stage_pos[s], a.spos + first, bytes, &full_bar[s]);
-    bulk_g2s(stage_mom[s], a.smom + first, bytes, &full_bar[s]);
+    bulk_g2s(stage_pos(s), a.spos + first, bytes, &full_bar[s]);
+    bulk_g2s(stage_mom(s), a.smom + first, bytes, &full_bar[s]);
   };
 
   if (tid == 0) {
@@ -349,19 +496,17 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
     if (!skip_scene) {
       const int64_t rem = sc.ns - int64_t(tile) * TILE;
       const int cnt = int(rem < TILE ? rem : TILE);
-      const R4* __restrict__ sp = stage_pos[s];
-      const R4* __restrict__ sm = stage_mom[s];
-      Real acc[TPT][kAcc];
+      const R4* __restrict__ sp = stage_pos(s);
+      const R4* __restrict__ sm = stage_mom(s);
+      typename Body::Acc acc[TPT];
 #pragma unroll
-      for (int t = 0; t < TPT; ++t)
-#pragma unroll
-        for (int q = 0; q < kAcc; ++q) acc[t][q] = Real(0);
+      for (int t = 0; t < TPT; ++t) acc[t].zero();
+      const int n_items = Body::items(cnt);
 #pragma unroll 4
-      for (int j = 0; j < cnt; ++j) {
-        const R4 p = sp[j];
-        const R4 m = sm[j];
+      for (int j = 0; j < n_items; ++j) {
+        const typename Body::Item it = Body::load_item(sp, sm, j);
 #pragma unroll
-        for (int t = 0; t < TPT; ++t) Body::pair(td[t], p, m, pc, acc[t]);
+        for (int t = 0; t < TPT; ++t) Body::pair(td[t], it, pc, acc[t]);
       }
 #pragma unroll
       for (int t = 0; t < TPT; ++t) {

@@ -102,6 +102,32 @@ __device__ __forceinline__ void comp_add(float& s, float& c, float x) {
   c = __fadd_rn(c, e);
 }
 
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction applies
+// the operation to both halves, so the FMA pipe does the same work with half
+// the issue slots.  Rounding is round-to-nearest per half, as for FFMA.
+__device__ __forceinline__ unsigned long long f2_bits(float2 a) {
+  return (static_cast<unsigned long long>(__float_as_uint(a.y)) << 32) | __float_as_uint(a.x);
+}
+__device__ __forceinline__ float2 f2_from(unsigned long long r) {
+  return make_float2(__uint_as_float(unsigned(r & 0xffffffffull)), __uint_as_float(unsigned(r >> 32)));
+}
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)), "l"(f2_bits(c)));
+  return f2_from(r);
+}
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(r);
+}
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(r);
+}
+__device__ __forceinline__ float2 f2_dup(float v) { return make_float2(v, v); }
+
 // Packed 4-wide particle record (x, y, z, pad): 16 B for FP32, 32 B for FP64,
 // so a tile of them is one contiguous, 16-byte-aligned bulk copy.
 struct alignas(32) dbl4 {

@@ -38,25 +38,24 @@ unsigned grid_for(int64_t n) {
   return unsigned(g);
 }
 
+constexpr int kBodies = 5;
+
 struct DirectCtx {
   std::mutex mu;
-  DevBuf t4, s4, m4, tm4, soa, aux;
+  DevBuf t4, s4, m4, tm4, soa, aux, s2, m2, corr;
   Scratch scr;
-  Plan<float> plan[3];
-  bool plan_ok[3] = {false, false, false};
-  int64_t plan_nt[3] = {0, 0, 0}, plan_ns[3] = {0, 0, 0};
-  double plan_h[3] = {0, 0, 0};
+  CellList cells;
+  Plan<float> plan[kBodies];
+  bool plan_ok[kBodies] = {};
+  int64_t plan_nt[kBodies] = {}, plan_ns[kBodies] = {};
+  double plan_h[kBodies] = {};
   void release() {
-    t4.release();
-    s4.release();
-    m4.release();
-    tm4.release();
-    soa.release();
-    aux.release();
+    for (DevBuf* b : {&t4, &s4, &m4, &tm4, &soa, &aux, &s2, &m2, &corr}) b->release();
     scr.partials.release();
     scr.counters.release();
     scr.err.release();
-    for (int b = 0; b < 3; ++b) {
+    cells = CellList();
+    for (int b = 0; b < kBodies; ++b) {
       plan[b].d_scenes.release();
       plan_ok[b] = false;
     }
@@ -114,12 +113,39 @@ mf_status direct_impl(Body body, const float* targets, int64_t nt, const float* 
   k_pack_aos<<<grid_for(ns), 256, 0, st>>>(ns, sources, c.s4.as<float4>());
   k_pack_aos<<<grid_for(ns), 256, 0, st>>>(ns, charges, c.m4.as<float4>());
   MF_CUDA_TRY(cudaGetLastError());
-  const Plan<float>* plan = nullptr;
-  MF_TRY(get_plan(c, body, nt, ns, h, &plan));
   LaunchIO<float> io;
   io.tpos = c.t4.as<float4>();
   io.spos = c.s4.as<float4>();
   io.smom = c.m4.as<float4>();
+  // Field and force go through the packed two-source kernels: sources in pair
+  // layout, a cell list over the sources, and the near-field correction.
+  Body launch_body = body;
+  if (body == Body::Field || body == Body::Force) {
+    const size_t pair_bytes = size_t(ns + 1) * sizeof(float4);
+    MF_TRY(c.s2.reserve(pair_bytes));
+    MF_TRY(c.m2.reserve(pair_bytes));
+    MF_TRY(c.corr.reserve(size_t(nt) * sizeof(float4)));
+    to_pairs(c.s4.as<float4>(), c.s2.as<float4>(), ns, st);
+    to_pairs(c.m4.as<float4>(), c.m2.as<float4>(), ns, st);
+    MF_CUDA_TRY(cudaGetLastError());
+    MF_TRY(c.cells.build(c.s4.as<float4>(), {CellSceneSpec{0, ns, double(h)}}, st));
+    if (body == Body::Field) {
+      if (targets == sources && nt == ns)
+        MF_TRY(c.cells.field_correction(c.s4.as<float4>(), c.m4.as<float4>(), c.corr.as<float4>(), st));
+      else
+        MF_TRY(c.cells.field_correction_at(c.t4.as<float4>(), nt, c.s4.as<float4>(), c.m4.as<float4>(),
+                                           c.corr.as<float4>(), st));
+      launch_body = Body::FieldF2;
+    } else {
+      MF_TRY(c.cells.force_correction(c.s4.as<float4>(), c.m4.as<float4>(), c.corr.as<float4>(), st));
+      launch_body = Body::ForceF2;
+    }
+    io.spos = c.s2.as<float4>();
+    io.smom = c.m2.as<float4>();
+    io.corr4 = c.corr.as<float4>();
+  }
+  const Plan<float>* plan = nullptr;
+  MF_TRY(get_plan(c, launch_body, nt, ns, h, &plan));
   float* soa = c.soa.as<float>();
   for (int k = 0; k < kOut; ++k) io.out[k] = soa + int64_t(k) * nt;
   if (body == Body::Force) {

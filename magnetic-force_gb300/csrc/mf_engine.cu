@@ -247,6 +247,7 @@ class Engine final : public EngineBase {
       MF_CUDA_TRY(cudaStreamSynchronize(st_));
       if (bad) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
     }
+    positions_changed();
     if (old != n || !plans_ready_) {
       MF_TRY(build_plans());
       // Resize keeps the warm start visible in total_B_over_mu0 (magnetic_force.cu:735-741).
@@ -351,6 +352,7 @@ class Engine final : public EngineBase {
     if (!rext_zero_)
       for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
     io.naive_quirks = naive_ ? 1 : 0;
+    MF_TRY(prepare_packed(mom4(), true, io));
     MF_TRY(run(plan_force_, io));
     ctr_.force_passes += 1;
     ctr_.force_pairs += plan_force_.pairs;
@@ -369,6 +371,7 @@ class Engine final : public EngineBase {
         vel4(), pos4(), pubf(MF_Q_POSITIONS, 0), pubf(MF_Q_POSITIONS, 1), pubf(MF_Q_POSITIONS, 2));
     MF_CUDA_TRY(cudaGetLastError());
     ++ctr_.kernel_launches;
+    positions_changed();
     return s;
   }
 
@@ -478,6 +481,11 @@ class Engine final : public EngineBase {
   DevBuf staging_, staging2_;
   DevBuf scal_, red_part_, red_ticket_, range_, bad_;
   Scratch scr_;
+  // FP32 packed-kernel state: positions and the current product's dipoles in
+  // pair layout, the cell list, the near-field correction per target.
+  DevBuf pos2_, mom2_, corr_;
+  CellList cells_;
+  bool cells_dirty_ = true;
   Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_;
   bool plans_ready_ = false;
   bool rext_zero_ = true;
@@ -523,6 +531,15 @@ class Engine final : public EngineBase {
       if (q != MF_Q_POSITIONS && q != MF_Q_VELOCITY) MF_TRY(pub_r_[q].reserve(size_t(3 * n) * sizeof(Real), false, true));
       if (q == MF_Q_POSITIONS || !kF32) MF_TRY(pub_f_[q].reserve(size_t(3 * n) * sizeof(float), false, true));
     }
+    if constexpr (kF32) {
+      pos2_.release();
+      mom2_.release();
+      corr_.release();
+      MF_TRY(pos2_.reserve(size_t(n + 1) * sizeof(float4), false, true));
+      MF_TRY(mom2_.reserve(size_t(n + 1) * sizeof(float4), false, true));
+      MF_TRY(corr_.reserve(size_t(n) * sizeof(float4), false, true));
+      cells_dirty_ = true;
+    }
     np_ = n;
     VecRange rg{0, n};
     MF_CUDA_TRY(cudaMemcpy(range_.ptr, &rg, sizeof(rg), cudaMemcpyHostToDevice));
@@ -545,21 +562,24 @@ class Engine final : public EngineBase {
     s.scale = c;
     s.coef_add = 1.0;
     s.coef_add2 = -1.0;
-    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_resid_));
+    // FP32 uses the packed two-source kernels; FP64 the exact-branch kernels.
+    const Body fb = kF32 ? Body::FieldF2 : Body::Field;
+    const Body gb = kF32 ? Body::ForceF2 : Body::Force;
+    MF_TRY(build_plan<Real>(fb, {s}, plan_resid_));
     // gradient g = c G(r) - r            (D_transpose, :1281-1284)
     // D(d) = c G(d) - d                  (D, :1275-1278)
     s = base;
     s.scale = c;
     s.coef_add = -1.0;
-    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_grad_));
-    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_dd_));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_grad_));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_dd_));
     // CG: q = p - c G(p)
     s = base;
     s.scale = -c;
     s.coef_add = 1.0;
-    MF_TRY(build_plan<Real>(Body::Field, {s}, plan_cgq_));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_));
     s = base;
-    MF_TRY(build_plan<Real>(Body::Force, {s}, plan_force_));
+    MF_TRY(build_plan<Real>(gb, {s}, plan_force_));
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
     return MF_OK;
@@ -594,7 +614,10 @@ class Engine final : public EngineBase {
       plan_scratch_needs(plan, &pd, &nc);
       MF_TRY(scr_.ensure(pd, nc));
       TimedLaunch t;
-      t.body = int(plan.body);
+      // statistics per kernel kind: field (0), force (1), tensor (2)
+      t.body = (plan.body == Body::Field || plan.body == Body::FieldF2)   ? 0
+               : (plan.body == Body::Force || plan.body == Body::ForceF2) ? 1
+                                                                          : 2;
       t.pairs = plan.pairs;
       MF_CUDA_TRY(cudaEventCreate(&t.start));
       MF_CUDA_TRY(cudaEventCreate(&t.stop));
@@ -645,12 +668,48 @@ class Engine final : public EngineBase {
   mf_kernel_stats agg_[3] = {};
   bool timing_ = false;
 
+  // FP32: the packed two-source kernels need the sources in pair layout, the
+  // cell list of the current positions and the near-field correction of the
+  // current dipoles.
+  mf_status ensure_cells() {
+    if constexpr (kF32) {
+      if (cells_dirty_) {
+        MF_TRY(cells_.build(pos4(), {CellSceneSpec{0, np_, h_}}, st_));
+        ctr_.kernel_launches += 7;
+        cells_dirty_ = false;
+      }
+    }
+    return MF_OK;
+  }
+  mf_status prepare_packed(const R4* src_mom, bool force, LaunchIO<Real>& io) {
+    if constexpr (kF32) {
+      MF_TRY(ensure_cells());
+      to_pairs(src_mom, mom2_.template as<float4>(), np_, st_);
+      MF_CUDA_TRY(cudaGetLastError());
+      if (force) MF_TRY(cells_.force_correction(pos4(), src_mom, corr_.template as<float4>(), st_));
+      else MF_TRY(cells_.field_correction(pos4(), src_mom, corr_.template as<float4>(), st_));
+      ctr_.kernel_launches += 2;
+      io.spos = pos2_.template as<float4>();
+      io.smom = mom2_.template as<float4>();
+      io.corr4 = corr_.template as<float4>();
+    }
+    return MF_OK;
+  }
+  void positions_changed() {
+    if constexpr (kF32) {
+      to_pairs(pos4(), pos2_.template as<float4>(), np_, st_);
+      ++ctr_.kernel_launches;
+      cells_dirty_ = true;
+    }
+  }
+
   mf_status field(Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4, const R4* add4b,
                   const double* done = nullptr) {
     LaunchIO<Real> io;
     io.tpos = pos4();
     io.spos = pos4();
     io.smom = src_mom;
+    MF_TRY(prepare_packed(src_mom, false, io));
     io.out4 = out4;
     io.add4 = add4;
     io.add4b = add4b;
@@ -759,7 +818,7 @@ class Engine final : public EngineBase {
     if (timing_) {
       int64_t to_mark = launched - executed;  // the last field launches of this solve
       for (auto it = timed_.rbegin(); it != timed_.rend() && to_mark > 0; ++it)
-        if (it->body == int(Body::Field)) {
+        if (it->body == 0) {
           it->skipped = true;
           --to_mark;
         }

@@ -71,7 +71,11 @@ struct DevBuf {
 // ---------------------------------------------------------------------------
 // All-pairs launch configurations.
 // ---------------------------------------------------------------------------
-enum class Body { Field = 0, Force = 1, Tensor = 2 };
+// Field / Force / Tensor: one packed record per source, exact pair branches
+// (both precisions).  FieldF2 / ForceF2: FP32 pair-layout sources, two
+// sources per instruction, clamped far form plus a near-field correction
+// array (mf_cells.cu) added in the epilogue.
+enum class Body { Field = 0, Force = 1, Tensor = 2, FieldF2 = 3, ForceF2 = 4 };
 
 template <class Real, Body B>
 struct KCfg;
@@ -87,6 +91,14 @@ struct KCfg<float, Body::Force> {
 template <>
 struct KCfg<float, Body::Tensor> {
   static constexpr int TPB = 128, TPT = 1, TILE = 256, STAGES = 3, kOut = 6;
+};
+template <>
+struct KCfg<float, Body::FieldF2> {
+  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 3;
+};
+template <>
+struct KCfg<float, Body::ForceF2> {
+  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 3;
 };
 // FP64: 128 threads x 1 target, 128-source tiles of 32-byte records.
 template <>
@@ -157,6 +169,7 @@ struct LaunchIO {
   int naive_quirks = 0;
   const double* done_flags = nullptr;
   int done_stride = 0;
+  const R4* corr4 = nullptr;
 };
 
 // Scratch sizes a plan needs.
@@ -175,5 +188,54 @@ mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double*
 
 int device_sms(int device);
 int current_device();
+
+// ---------------------------------------------------------------------------
+// Uniform-grid cell lists and the near-field correction pass (mf_cells.cu)
+// ---------------------------------------------------------------------------
+struct CellGrid {
+  float ox, oy, oz, inv_cs;  // grid origin and 1 / cell size
+  int32_t nx, ny, nz;
+  int32_t reach_field;       // cells to scan each way for r < 2h
+  int32_t reach_force;       // cells to scan each way for r <= 4h
+  int32_t pad;
+  int64_t cell_off;          // first cell of this scene in the global arrays
+  int64_t p_off, n;          // particle range of the scene
+  int64_t k_off;             // particles of the scenes before this one
+  PairConsts<float> pc;
+};
+
+struct CellSceneSpec {
+  int64_t p_off, n;
+  double h;
+};
+
+class CellList {
+ public:
+  // Bins the particles of every scene into cells of edge >= 2h; particles of
+  // a cell are listed in increasing index order (deterministic sums).
+  // Synchronises `st` once (the bounding boxes are read on the host).
+  mf_status build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st);
+  // corr_i = sum over j within 2h (resp. 4h) of [exact pair term - the
+  // clamped far term the packed all-pairs loop gave that pair], in the
+  // all-pairs kernels' output units.  Targets = sources = the binned set.
+  mf_status field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const;
+  mf_status force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const;
+  // Field correction at separate targets tpos4[0..nt) (single-scene lists).
+  mf_status field_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
+                                float4* corr, cudaStream_t st) const;
+  int64_t particles() const { return n_total_; }
+  int64_t cells() const { return n_cells_; }
+  const std::vector<CellGrid>& grids() const { return host_grids_; }
+
+ private:
+  DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
+  std::vector<CellGrid> host_grids_;
+  int64_t n_total_ = 0, n_cells_ = 0;
+  int32_t n_scenes_ = 0;
+};
+
+// Packed records -> pair layout (sources 2p, 2p+1 as (x_a, x_b, y_a, y_b),
+// (z_a, z_b, 0, 0)); a missing partner (odd n) is written as zeros.
+void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st);
 
 }  // namespace mfgb

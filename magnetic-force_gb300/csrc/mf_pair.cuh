@@ -200,6 +200,158 @@ __device__ __forceinline__ void force_pair(Real dx, Real dy, Real dz, Real sx, R
   f[2] += dz * w + mz * u + sz * v;
 }
 
+// ---------------------------------------------------------------------------
+// Packed two-source forms (FP32).  Lanes .x / .y hold two different sources;
+// the target's values are duplicated into both lanes.  Every pair takes the
+// far form with r^2 clamped to the near radius: exact beyond it, finite inside
+// it (including r = 0).  The near-field correction pass (mf_cells.cu) adds,
+// for each pair inside the near radius, the exact term minus this clamped one.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 clamp_rsqrt2(float2 r2, float near2) {
+  return make_float2(rsqrt_approx(fmaxf(r2.x, near2)), rsqrt_approx(fmaxf(r2.y, near2)));
+}
+
+// s1 += d (d.m) r^-5, s2 += m r^-3 (field = (3 s1 - s2) / 4pi after the lanes are added).
+__device__ __forceinline__ void field_pair2(float2 tx, float2 ty, float2 tz, float2 sx, float2 sy, float2 sz,
+                                            float2 mx, float2 my, float2 mz, float near2, float2* s1, float2* s2) {
+  const float2 dx = f2_sub(tx, sx), dy = f2_sub(ty, sy), dz = f2_sub(tz, sz);
+  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+  const float2 ri = clamp_rsqrt2(r2, near2);
+  const float2 ri2 = f2_mul(ri, ri);
+  const float2 beta = f2_mul(ri2, ri);
+  const float2 alpha = f2_mul(beta, ri2);
+  const float2 dm = f2_fma(dz, mz, f2_fma(dy, my, f2_mul(dx, mx)));
+  const float2 t = f2_mul(dm, alpha);
+  s1[0] = f2_fma(dx, t, s1[0]);
+  s1[1] = f2_fma(dy, t, s1[1]);
+  s1[2] = f2_fma(dz, t, s1[2]);
+  s2[0] = f2_fma(mx, beta, s2[0]);
+  s2[1] = f2_fma(my, beta, s2[1]);
+  s2[2] = f2_fma(mz, beta, s2[2]);
+}
+
+// f += T(d, s) m / K with the far (P, Q) = (r^-5, -5 r^-7) of the clamped distance.
+__device__ __forceinline__ void force_pair2(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
+                                            float2 sx, float2 sy, float2 sz, float2 smx, float2 smy, float2 smz,
+                                            float near2, float2* f) {
+  const float2 dx = f2_sub(tx, sx), dy = f2_sub(ty, sy), dz = f2_sub(tz, sz);
+  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+  const float2 ri = clamp_rsqrt2(r2, near2);
+  const float2 ri2 = f2_mul(ri, ri);
+  const float2 ri5 = f2_mul(f2_mul(ri2, ri2), ri);
+  const float2 ds = f2_fma(dz, smz, f2_fma(dy, smy, f2_mul(dx, smx)));
+  const float2 dm = f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx)));
+  const float2 sm = f2_fma(smz, tmz, f2_fma(smy, tmy, f2_mul(smx, tmx)));
+  const float2 u = f2_mul(ds, ri5);
+  const float2 v = f2_mul(dm, ri5);
+  const float2 e = f2_mul(f2_mul(ri2, ds), f2_dup(-5.f));
+  const float2 w = f2_fma(e, v, f2_mul(sm, ri5));
+  f[0] = f2_fma(dx, w, f2_fma(tmx, u, f2_fma(smx, v, f[0])));
+  f[1] = f2_fma(dy, w, f2_fma(tmy, u, f2_fma(smy, v, f[1])));
+  f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_fma(smz, v, f[2])));
+}
+
+// The clamped far coefficients every near pair received in the packed loop
+// (the same rsqrt and products; equal to within rounding).
+__device__ __forceinline__ void clamped_field_coeffs(float near2, float& alpha, float& beta) {
+  const float ri = rsqrt_approx(near2);
+  const float ri2 = ri * ri;
+  beta = ri2 * ri;
+  alpha = beta * ri2;
+}
+__device__ __forceinline__ void clamped_force_coeffs(float near2, float& P, float& Q) {
+  const float ri = rsqrt_approx(near2);
+  const float ri2 = ri * ri;
+  P = (ri2 * ri2) * ri;
+  Q = ri2 * -5.f * P;
+}
+
+// Branch-free FP32 forms of the near-field coefficients for the correction
+// pass, where lanes of a warp sit on different branches: both SPH pieces are
+// evaluated and selected; the fitted-curve piece is looked up in a 4 x 10
+// coefficient table (c1 then c2 of each piece, highest power first).
+// Same mathematics as field_near_coeffs / force_near_coeffs.
+__device__ __forceinline__ void field_near_coeffs_fast(float r2, float inv_h, float ih3, float& alpha, float& beta) {
+  const float ri = rsqrt_approx(r2);
+  const bool pos = r2 > 0.f;
+  const float r = pos ? r2 * ri : 0.f;
+  const float q = r * inv_h, q2 = q * q, q3 = q2 * q;
+  const float tmq = 2.f - q, tmq3 = tmq * tmq * tmq;
+  const float omq = 1.f - q;
+  const float Pq = q3 * (q3 * (1.f / 6.f) - q2 * (6.f / 5.f) + 3.f * q - 8.f / 3.f) + 1.f / 15.f;
+  float rq3;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rq3) : "f"(fmaxf(q3, 1.f)));
+  const bool hi = q >= 1.f;
+  const float wa = hi ? -3.f * Pq * rq3 : (15.f * q3 - 36.f * q2 + 40.f) * 0.1f;
+  const float wd = hi ? tmq3 : tmq3 - 4.f * omq * omq * omq;
+  beta = (wa * (1.f / 3.f) - wd) * ih3;
+  alpha = pos ? (wa - wd) * ih3 * (1.f / 3.f) * (ri * ri) : 0.f;
+}
+
+__device__ __forceinline__ void force_near_coeffs_fast(float r2, const float* __restrict__ tbl, float inv_h,
+                                                       float ih4_over_k, float& P, float& Q) {
+  const float ri = rsqrt_approx(r2);
+  const bool pos = r2 > 0.f;
+  const float r = pos ? r2 * ri : 0.f;
+  const float q = fminf(r * inv_h, 4.f);
+  const int piece = min(max(int(ceilf(q)) - 1, 0), 3);
+  const float* c = tbl + piece * 10;
+  const float c1 = q * (q * (q * (q * c[0] + c[1]) + c[2]) + c[3]) + c[4];
+  const float c2 = q * (q * (q * (q * c[5] + c[6]) + c[7]) + c[8]) + c[9];
+  const float s = ih4_over_k * ri;
+  P = pos ? c1 * s : 0.f;
+  Q = pos ? (c2 - 3.f * c1) * s * (ri * ri) : 0.f;
+}
+
+// The fitted-curve table in the layout force_near_coeffs_fast reads
+// (Dipole_hessian.kern:53-61): per piece, C1 then C2, highest power first.
+#define MF_FITTED_CURVE_TABLE                                                                      \
+  {9.97813616438174e-09f,  -2.97897856524718e-08f, 2.38918644566813e-09f,  4.53199938857366e-08f,  \
+   2.44617454752747e-11f,  6.69550479838731e-08f,  -1.61753307173877e-07f, 1.68213714992711e-08f,  \
+   1.34558143036838e-07f,  1.10976027980100e-10f,  -2.76473728643294e-09f, 2.86975546540539e-08f,  \
+   -9.94582836806651e-08f, 1.25129924573675e-07f,  -2.37010166723652e-08f, -3.08460139955194e-08f, \
+   2.29192245602275e-07f,  -5.88399621128587e-07f, 5.61170054591844e-07f,  -1.14421132829680e-07f, \
+   -1.09679990621465e-09f, 9.77055663264614e-09f,  -2.54781238661150e-08f, 2.65020634884934e-09f,  \
+   5.00787562417835e-08f,  3.50477408060213e-09f,  -5.25956271895141e-08f, 2.78876509535747e-07f,  \
+   -6.24199554212217e-07f, 4.91807818904985e-07f,  3.79927162333632e-10f,  -6.26368404962679e-09f, \
+   3.94760528277489e-08f,  -1.13580541622200e-07f, 1.27491333574323e-07f,  7.33485346367840e-10f,  \
+   -9.58855788627803e-09f, 4.37085309763591e-08f,  -7.48004594092261e-08f, 2.34161209605651e-08f}
+
+// Correction of one near field pair (r^2 < near2): exact minus clamped,
+// accumulated as s1 (d (d.m) dalpha) and s2 (m dbeta) like the packed loop.
+__device__ __forceinline__ void field_near_correction(float dx, float dy, float dz, float mx, float my, float mz,
+                                                      const PairConsts<float>& pc, float alpha_c, float beta_c,
+                                                      float* s1, float* s2) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  float alpha, beta;
+  field_near_coeffs<float>(r2, pc, alpha, beta);
+  const float da = alpha - alpha_c, db = beta - beta_c;
+  const float t = (dx * mx + dy * my + dz * mz) * da;
+  s1[0] += dx * t;
+  s1[1] += dy * t;
+  s1[2] += dz * t;
+  s2[0] += mx * db;
+  s2[1] += my * db;
+  s2[2] += mz * db;
+}
+
+// Correction of one near force pair (r^2 <= near2), contracted with m.
+__device__ __forceinline__ void force_near_correction(float dx, float dy, float dz, float sx, float sy, float sz,
+                                                      float mx, float my, float mz, const PairConsts<float>& pc,
+                                                      float P_c, float Q_c, float* f) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  float P, Q;
+  force_near_coeffs<float>(r2, pc, P, Q);
+  const float dP = P - P_c, dQ = Q - Q_c;
+  const float ds = dx * sx + dy * sy + dz * sz;
+  const float dm = dx * mx + dy * my + dz * mz;
+  const float sm = sx * mx + sy * my + sz * mz;
+  const float u = dP * ds, v = dP * dm, w = dP * sm + dQ * ds * dm;
+  f[0] += dx * w + mx * u + sx * v;
+  f[1] += dy * w + my * u + sy * v;
+  f[2] += dz * w + mz * u + sz * v;
+}
+
 // One tensor pair (6 unique entries xx, yy, zz, xy, xz, yz): t += T(d, s) / K.
 template <class Real>
 __device__ __forceinline__ void tensor_pair(Real dx, Real dy, Real dz, Real sx, Real sy, Real sz,
