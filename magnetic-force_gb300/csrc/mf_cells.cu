@@ -167,27 +167,25 @@ __global__ void k_sort_cells(const int32_t* __restrict__ start, int64_t n_cells,
 
 __constant__ float c_fit_tbl[40] = MF_FITTED_CURVE_TABLE;
 
-// Near-field correction, one CTA per cell: the cell's particles are the
-// targets (one per thread); the particles of each neighbouring row of cells
-// are staged in shared memory chunk by chunk.  Each thread first marks which
-// of the next 32 staged sources are near it (a 32-bit mask, cheap distance
-// tests with every lane busy), then evaluates only those, lanes stepping
-// through their own masks together, so the expensive near evaluations keep
-// the warp mostly full.  Sources are visited in increasing staged order, so
-// the sums are deterministic.
+// Near-field correction, one warp per cell: the cell's particles are the
+// targets, handled kT at a time, held by every lane; the lanes split the
+// candidate sources of the neighbourhood (rows of cells trimmed to the
+// cell-level distance bound of the near radius), each lane sweeping its
+// sources in increasing order, and every target's sum is finished by a fixed
+// shuffle tree, so results are deterministic.
 template <bool kForce>
-__global__ void __launch_bounds__(64) k_correction_cells(const CellGrid* __restrict__ grids, int n_scenes,
-                                                         int64_t n_cells, const int32_t* __restrict__ perm,
-                                                         const int32_t* __restrict__ start,
-                                                         const float4* __restrict__ pos,
-                                                         const float4* __restrict__ mom, float4* __restrict__ corr) {
-  constexpr int kChunk = 256;
-  __shared__ float4 s_pos[kChunk];
-  __shared__ float4 s_mom[kChunk];
+__global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __restrict__ grids, int n_scenes,
+                                                          int64_t n_cells, const int32_t* __restrict__ perm,
+                                                          const int32_t* __restrict__ start,
+                                                          const float4* __restrict__ pos,
+                                                          const float4* __restrict__ mom, float4* __restrict__ corr) {
+  constexpr int kT = 8;
   __shared__ float s_tbl[40];
   if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];
   __syncthreads();
-  for (int64_t c = blockIdx.x; c < n_cells; c += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n_warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += n_warps) {
     const int32_t cb = start[c], ce = start[c + 1];
     if (cb == ce) continue;
     int lo = 0, hi = n_scenes - 1;
@@ -201,91 +199,82 @@ __global__ void __launch_bounds__(64) k_correction_cells(const CellGrid* __restr
     const int ix = int(lc % g.nx), iy = int((lc / g.nx) % g.ny), iz = int(lc / (int64_t(g.nx) * g.ny));
     const int R = kForce ? g.reach_force : g.reach_field;
     const float near2 = kForce ? g.pc.near2_force : g.pc.near2_field;
+    const float cs = 1.f / g.inv_cs;
     const float inv_h = g.pc.inv_h, ih3 = g.pc.ih3, ih4k = g.pc.ih4_over_k;
     float cA, cB;
     if (kForce) clamped_force_coeffs(near2, cA, cB);
     else clamped_field_coeffs(near2, cA, cB);
-    const int cx0 = max(ix - R, 0), cx1 = min(ix + R, g.nx - 1);
-    for (int32_t tb = cb; tb < ce; tb += blockDim.x) {
-      const int32_t q = tb + int32_t(threadIdx.x);
-      const bool active = q < ce;
-      const int32_t i = active ? perm[q] : 0;
-      const float4 pi = pos[i];
-      const float4 mi = mom[i];
-      float s1[3] = {0.f, 0.f, 0.f}, s2[3] = {0.f, 0.f, 0.f};
+    for (int32_t t0 = cb; t0 < ce; t0 += kT) {
+      const int nt = min(kT, ce - t0);
+      int32_t ti[kT];
+      float4 tp[kT], tm[kT];
+      float acc[kT][3];
+#pragma unroll
+      for (int t = 0; t < kT; ++t) {
+        ti[t] = perm[t0 + (t < nt ? t : 0)];
+        tp[t] = pos[ti[t]];
+        tm[t] = kForce ? mom[ti[t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        acc[t][0] = acc[t][1] = acc[t][2] = 0.f;
+      }
       for (int dz = -R; dz <= R; ++dz) {
         const int cz = iz + dz;
         if (cz < 0 || cz >= g.nz) continue;
+        const float gz = float(max(abs(dz) - 1, 0)) * cs;
         for (int dy = -R; dy <= R; ++dy) {
           const int cy = iy + dy;
           if (cy < 0 || cy >= g.ny) continue;
+          const float gy = float(max(abs(dy) - 1, 0)) * cs;
+          const float rem = near2 - gz * gz - gy * gy;
+          if (rem < 0.f) continue;  // the whole row lies beyond the near radius
+          const int dxm = min(R, int(sqrtf(rem) * g.inv_cs) + 1);
+          const int cx0 = max(ix - dxm, 0), cx1 = min(ix + dxm, g.nx - 1);
           const int64_t row = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx;
           const int32_t sb = start[row + cx0], se = start[row + cx1 + 1];
-          for (int32_t ch = sb; ch < se; ch += kChunk) {
-            const int cnt = min(kChunk, se - ch);
-            __syncthreads();
-            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-              const int32_t j = perm[ch + k];
-              s_pos[k] = pos[j];
-              s_mom[k] = mom[j];
-            }
-            __syncthreads();
-            if (!active) continue;
-            for (int w = 0; w < cnt; w += 32) {
-              const int lim = min(32, cnt - w);
-              uint32_t mask = 0;
-              for (int b = 0; b < lim; ++b) {
-                const float4 pj = s_pos[w + b];
-                const float dx = pi.x - pj.x, dy2 = pi.y - pj.y, dz2 = pi.z - pj.z;
-                const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-                const bool near = kForce ? (r2 <= near2) : (r2 < near2);
-                mask |= uint32_t(near) << b;
-              }
-              while (mask) {
-                const int b = __ffs(mask) - 1;
-                mask &= mask - 1;
-                const float4 pj = s_pos[w + b];
-                const float4 mj = s_mom[w + b];
-                const float dx = pi.x - pj.x, dy2 = pi.y - pj.y, dz2 = pi.z - pj.z;
-                const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+          for (int32_t q = sb + lane; q < se; q += 32) {
+            const int32_t j = perm[q];
+            const float4 pj = pos[j];
+            const float4 mj = mom[j];
+#pragma unroll
+            for (int t = 0; t < kT; ++t) {
+              const float dx = tp[t].x - pj.x, dy2 = tp[t].y - pj.y, dz2 = tp[t].z - pj.z;
+              const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+              if (t < nt && (kForce ? (r2 <= near2) : (r2 < near2))) {
                 if (kForce) {
                   float P, Q;
                   force_near_coeffs_fast(r2, s_tbl, inv_h, ih4k, P, Q);
                   const float dP = P - cA, dQ = Q - cB;
                   const float ds = dx * mj.x + dy2 * mj.y + dz2 * mj.z;
-                  const float dm = dx * mi.x + dy2 * mi.y + dz2 * mi.z;
-                  const float sm = mj.x * mi.x + mj.y * mi.y + mj.z * mi.z;
+                  const float dm = dx * tm[t].x + dy2 * tm[t].y + dz2 * tm[t].z;
+                  const float sm = mj.x * tm[t].x + mj.y * tm[t].y + mj.z * tm[t].z;
                   const float u = dP * ds, v = dP * dm, wv = dP * sm + dQ * ds * dm;
-                  s1[0] += dx * wv + mi.x * u + mj.x * v;
-                  s1[1] += dy2 * wv + mi.y * u + mj.y * v;
-                  s1[2] += dz2 * wv + mi.z * u + mj.z * v;
+                  acc[t][0] += dx * wv + tm[t].x * u + mj.x * v;
+                  acc[t][1] += dy2 * wv + tm[t].y * u + mj.y * v;
+                  acc[t][2] += dz2 * wv + tm[t].z * u + mj.z * v;
                 } else {
                   float al, be;
                   field_near_coeffs_fast(r2, inv_h, ih3, al, be);
-                  const float da = al - cA, db = be - cB;
-                  const float t = (dx * mj.x + dy2 * mj.y + dz2 * mj.z) * da;
-                  s1[0] += dx * t;
-                  s1[1] += dy2 * t;
-                  s1[2] += dz2 * t;
-                  s2[0] += mj.x * db;
-                  s2[1] += mj.y * db;
-                  s2[2] += mj.z * db;
+                  const float t3 = 3.f * (dx * mj.x + dy2 * mj.y + dz2 * mj.z) * (al - cA);
+                  const float db = be - cB;
+                  acc[t][0] += dx * t3 - mj.x * db;
+                  acc[t][1] += dy2 * t3 - mj.y * db;
+                  acc[t][2] += dz2 * t3 - mj.z * db;
                 }
               }
             }
           }
         }
       }
-      if (active) {
-        float4 o;
-        if (kForce) {
-          const float k = float(kForceK);
-          o = make_float4(s1[0] * k, s1[1] * k, s1[2] * k, 0.f);
-        } else {
-          const float k = float(kInv4Pi);
-          o = make_float4((3.f * s1[0] - s2[0]) * k, (3.f * s1[1] - s2[1]) * k, (3.f * s1[2] - s2[2]) * k, 0.f);
+      const float scale = kForce ? float(kForceK) : float(kInv4Pi);
+#pragma unroll
+      for (int t = 0; t < kT; ++t) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          float v = acc[t][k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          acc[t][k] = v;
         }
-        corr[i] = o;
+        if (lane == 0 && t < nt) corr[ti[t]] = make_float4(acc[t][0] * scale, acc[t][1] * scale, acc[t][2] * scale, 0.f);
       }
     }
   }
@@ -411,9 +400,10 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
       ext[c] = std::max(0.0, double(ord2f(hb[6 * s + 3 + c])) - lo[c]);
       if (!std::isfinite(lo[c]) || !std::isfinite(ext[c])) return fail(MF_ERR_INVALID_ARG, "non-finite positions");
     }
-    // Cells a hair wider than 2h: two points closer than 2h then always land
-    // in the same or adjacent cells, whatever the rounding of the cell map.
-    double cs = 2.0 * h * (1.0 + 1e-4);
+    // Cells a hair wider than h (about 8 particles at h = 2 spacings): a point
+    // closer than 2h (4h) to a target then always lies within 2 (4) cells of
+    // it, whatever the rounding of the cell map.
+    double cs = h * (1.0 + 1e-4);
     // Keep the grid at most ~8 cells per particle: widen cells for sparse scenes.
     const double cap = std::max(64.0, 8.0 * double(scenes[s].n));
     for (int it = 0; it < 64; ++it) {
@@ -469,7 +459,7 @@ static unsigned cell_grid(int64_t cells) {
 }
 
 mf_status CellList::field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
-  k_correction_cells<false><<<cell_grid(n_cells_), 64, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
+  k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
                                                                    perm_.as<int32_t>(), cell_start_.as<int32_t>(),
                                                                    pos4, mom4, corr);
   MF_CUDA_TRY(cudaGetLastError());
@@ -487,7 +477,7 @@ mf_status CellList::field_correction_at(const float4* tpos4, int64_t nt, const f
 }
 
 mf_status CellList::force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
-  k_correction_cells<true><<<cell_grid(n_cells_), 64, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
+  k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
                                                                   perm_.as<int32_t>(), cell_start_.as<int32_t>(),
                                                                   pos4, mom4, corr);
   MF_CUDA_TRY(cudaGetLastError());
