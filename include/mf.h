@@ -233,6 +233,55 @@ mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h
 /* Frees the scratch the mf_direct_* calls keep per device. */
 mf_status mf_release_scratch(void);
 
+/* ---------------------------------------------------------------------- */
+/* Batched scenes.  Not in the reference, which solves one object per       */
+/* cuda_magnet_cgOptimizer instance: here many independent objects (each   */
+/* the reference's problem with its own particles, h, V, chi and uniform    */
+/* external field) advance together, every stage one launch for all of     */
+/* them, FP32 pair arithmetic and FP64 solver sums.                         */
+/* ---------------------------------------------------------------------- */
+typedef struct mf_scene_desc {
+  int64_t n;          /* particles */
+  const float* pos;   /* host AoS [n][3] */
+  float h;            /* smoothing length */
+  float volume;       /* particle volume V */
+  float chi;          /* susceptibility */
+  float H0[3];        /* uniform external field */
+} mf_scene_desc;
+
+typedef struct mf_batch mf_batch;
+
+mf_status mf_batch_create(const mf_scene_desc* scenes, int32_t n_scenes, int32_t device, mf_batch** out);
+mf_status mf_batch_destroy(mf_batch* b);
+mf_status mf_batch_set_stream(mf_batch* b, void* stream);
+mf_status mf_batch_num_scenes(mf_batch* b, int32_t* n);
+
+/* CG solve of every scene's magnetization (warm start), each scene stopping
+ * at relative residual rel_tol or after max_iter iterations.  *max_iters
+ * (may be NULL) gets the most iterations any scene ran, *worst_res the
+ * largest final relative residual. */
+mf_status mf_batch_solve(mf_batch* b, int64_t max_iter, double rel_tol, int64_t* max_iters, double* worst_res);
+
+/* Kelvin force of every scene (after a solve). */
+mf_status mf_batch_eval_force(mf_batch* b);
+
+/* `steps` timesteps: solve (at most iters_per_step CG iterations, rel_tol),
+ * force, symplectic Euler with unit density.  With use_graph != 0 one
+ * timestep is captured in a CUDA graph on first use (for these dt,
+ * iters_per_step, rel_tol) and replayed. */
+mf_status mf_batch_advance(mf_batch* b, double dt, int32_t steps, int32_t iters_per_step, double rel_tol,
+                           int32_t use_graph);
+
+/* A scene's quantity (MF_Q_POSITIONS, MF_Q_M, MF_Q_B_OVER_MU0, MF_Q_HEXT,
+ * MF_Q_FORCE, MF_Q_VELOCITY) into host AoS dst [n][3]. */
+mf_status mf_batch_get(mf_batch* b, int32_t scene, int32_t quantity, float* dst);
+
+/* Per-scene relative residuals and iterations of the last solve. */
+mf_status mf_batch_solver_state(mf_batch* b, double* rel_res, double* iters);
+
+mf_status mf_batch_get_counters(mf_batch* b, mf_counters* c);
+mf_status mf_batch_reset_counters(mf_batch* b);
+
 /* mf_direct_field without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- hosts that
  * have handed the device's whole memory budget to their own pool allocator,

@@ -191,6 +191,8 @@ struct Launcher {
     a.done_flags = io.done_flags;
     a.done_stride = io.done_stride;
     a.corr4 = io.corr4;
+    a.done_count = io.done_count;
+    a.done_total = io.done_total;
     a.partials = partials;
     a.counters = counters;
     a.err = err;

@@ -69,6 +69,10 @@ struct AllPairsArgs {
   int32_t done_stride;
   // Optional near-field correction per target (added before the epilogue's scale).
   const R4* corr4;
+  // Optional: the launch does nothing once *done_count reaches done_total
+  // (every scene's solve has stopped).
+  const int32_t* done_count;
+  int32_t done_total;
   double* partials;    // [grid][2][TPB*TPT][kOut]
   int32_t* counters;   // [total target blocks], zero between launches
   int32_t* err;        // device error word
@@ -417,8 +421,9 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
   const int64_t k_begin = step_start(T, G, b);
   const int64_t k_end = step_start(T, G, b + 1);
   if (k_begin >= k_end) return;
-  // A single-scene launch whose solve has already stopped does nothing.
+  // A launch whose solves have all stopped does nothing.
   if (a.done_flags && a.n_scenes == 1 && a.done_flags[0] != 0.0) return;
+  if (a.done_count && *a.done_count >= a.done_total) return;
 
   // Stage s: TILE source positions, then TILE source dipoles (computed, not
   // tabulated, so a runtime stage index does not put the table in local memory).

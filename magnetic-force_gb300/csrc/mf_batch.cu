@@ -1,0 +1,564 @@
+// mf_batch.cu -- many independent scenes advanced together (mf_batch_* in mf.h).
+//
+// Every scene is the reference's problem (its own particles, h, V, chi and
+// uniform external field).  Scenes are laid out back to back (each starting
+// at an even index, so the pair-layout source tiles never straddle two
+// scenes) and every stage of the step is one launch for all of them:
+//   * the all-pairs field / force kernels take all scenes in one flat step
+//     space (mf_allpairs.cuh), so small and large scenes share the SMs evenly;
+//   * the near-field correction runs over one cell list holding every scene;
+//   * the CG vector updates and FP64 inner products reduce per scene
+//     (blockIdx.y = scene) with the scalar steps applied on the device;
+//   * a scene whose solve has stopped is skipped by every later launch, and
+//     a launch does nothing once all scenes have stopped, so a fixed number of
+//     iterations can be captured in a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include "mf_internal.h"
+#include "mf_vec.cuh"
+
+namespace mfgb {
+namespace {
+
+__global__ void k_batch_init_rows(double* scal, int n, double tol, double maxit, int32_t* done_count) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    double* row = scal + int64_t(s) * kScal;
+    for (int k = 0; k < S_CONST_C; ++k) row[k] = 0.0;
+    row[S_TOL] = tol;
+    row[S_MAXIT] = maxit;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *done_count = 0;
+}
+
+// M = c b per scene (the dipoles of the force pass).
+struct BPublish {
+  static constexpr int kN = 0;
+  const float4* b;
+  float4* mom;
+  __device__ bool skip(const double*) const { return false; }
+  __device__ void elem(int64_t i, double*, const double* row) const {
+    const float c = float(row[S_CONST_C]);
+    const float4 v = b[i];
+    mom[i] = make_float4(c * v.x, c * v.y, c * v.z, 0.f);
+  }
+  __device__ void finish(const double*, double*) const {}
+};
+
+// Symplectic Euler with the scene's 1 / mass.
+struct BIntegrate {
+  static constexpr int kN = 0;
+  const float* fx;
+  const float* fy;
+  const float* fz;
+  float4* vel;
+  float4* pos;
+  float dt;
+  __device__ bool skip(const double*) const { return false; }
+  __device__ void elem(int64_t i, double*, const double* row) const {
+    const float im = float(row[S_CONST_INVM]);
+    float4 v = vel[i], p = pos[i];
+    v.x += dt * fx[i] * im;
+    v.y += dt * fy[i] * im;
+    v.z += dt * fz[i] * im;
+    p.x += dt * v.x;
+    p.y += dt * v.y;
+    p.z += dt * v.z;
+    vel[i] = v;
+    pos[i] = p;
+  }
+  __device__ void finish(const double*, double*) const {}
+};
+
+}  // namespace
+
+class Batch {
+ public:
+  ~Batch() {
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    if (own_stream_) cudaStreamDestroy(own_stream_);
+    if (pinned_) cudaFreeHost(pinned_);
+  }
+
+  mf_status init(const mf_scene_desc* d, int n, int device) {
+    if (n <= 0 || !d) return fail(MF_ERR_INVALID_ARG, "no scenes");
+    device_ = device;
+    sms_ = device_sms(device);
+    int64_t off = 0, max_n = 0;
+    for (int s = 0; s < n; ++s) {
+      const mf_scene_desc& x = d[s];
+      if (x.n <= 0 || !x.pos) return fail(MF_ERR_INVALID_ARG, "scene without particles");
+      if (!(x.h > 0.f) || !(x.volume > 0.f) || !std::isfinite(x.h) || !std::isfinite(x.volume))
+        return fail(MF_ERR_INVALID_ARG, "scene h and volume must be finite and > 0");
+      if (!std::isfinite(x.chi) || x.chi <= -1.f) return fail(MF_ERR_INVALID_ARG, "scene chi must be > -1");
+      for (int64_t i = 0; i < 3 * x.n; ++i)
+        if (!std::isfinite(x.pos[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
+      SI si;
+      si.off = off;
+      si.n = x.n;
+      si.h = x.h;
+      si.V = x.volume;
+      si.chi = x.chi;
+      for (int k = 0; k < 3; ++k) si.H0[k] = x.H0[k];
+      sc_.push_back(si);
+      off += x.n + (x.n & 1);  // next scene starts at an even index
+      max_n = std::max(max_n, x.n);
+    }
+    n_alloc_ = off;
+    MF_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+    st_ = own_stream_;
+    MF_CUDA_TRY(cudaMallocHost(&pinned_, 64));
+
+    const size_t v4 = size_t(n_alloc_ + 2) * sizeof(float4);
+    for (DevBuf* b : {&pos4_, &pos2_, &vel4_, &b4_, &r4_, &p4_, &q4_, &hext4_, &mom4_, &mom2_, &corr_})
+      MF_TRY(b->reserve(v4, false, true));
+    MF_TRY(fs_.reserve(size_t(3 * n_alloc_) * sizeof(float), false, true));
+
+    // Positions, external field, solver constants.
+    std::vector<float4> hp(size_t(n_alloc_ + 2), make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float4> hh(size_t(n_alloc_ + 2), make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<double> rows(size_t(n) * kScal, 0.0);
+    std::vector<VecRange> rg(static_cast<size_t>(n));
+    for (int s = 0; s < n; ++s) {
+      const SI& si = sc_[size_t(s)];
+      for (int64_t i = 0; i < si.n; ++i) {
+        hp[size_t(si.off + i)] = make_float4(d[s].pos[3 * i], d[s].pos[3 * i + 1], d[s].pos[3 * i + 2], 0.f);
+        hh[size_t(si.off + i)] = make_float4(si.H0[0], si.H0[1], si.H0[2], 0.f);
+      }
+      // A scene with an odd count borrows its dummy partner's slot at its end:
+      // park it on the scene's first particle (zero dipole, contributes nothing).
+      if (si.n & 1) hp[size_t(si.off + si.n)] = hp[size_t(si.off)];
+      double* row = &rows[size_t(s) * kScal];
+      row[S_CONST_C] = si.V * si.chi / (1.0 + si.chi);
+      row[S_CONST_INVM] = 1.0 / si.V;
+      for (int k = 0; k < 3; ++k) row[S_CONST_H0 + k] = si.H0[k];
+      rg[size_t(s)] = VecRange{si.off, si.n};
+    }
+    MF_CUDA_TRY(cudaMemcpy(pos4_.ptr, hp.data(), v4, cudaMemcpyHostToDevice));
+    MF_CUDA_TRY(cudaMemcpy(hext4_.ptr, hh.data(), v4, cudaMemcpyHostToDevice));
+    MF_TRY(scal_.reserve(rows.size() * sizeof(double)));
+    MF_CUDA_TRY(cudaMemcpy(scal_.ptr, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
+    MF_TRY(ranges_.reserve(rg.size() * sizeof(VecRange)));
+    MF_CUDA_TRY(cudaMemcpy(ranges_.ptr, rg.data(), rg.size() * sizeof(VecRange), cudaMemcpyHostToDevice));
+    red_gx_ = int(std::min<int64_t>((max_n + 255) / 256, 16));
+    MF_TRY(red_part_.reserve(size_t(n) * red_gx_ * 2 * sizeof(double)));
+    MF_TRY(red_tickets_.reserve(size_t(n) * sizeof(int32_t), false, true));
+    MF_TRY(done_count_.reserve(16, false, true));
+
+    // Launch plans (one scene table per kind of product).
+    std::vector<SceneSpec> resid, cgq, force;
+    for (const SI& si : sc_) {
+      SceneSpec b;
+      b.t_off = si.off;
+      b.nt = si.n;
+      b.s_off = si.off;
+      b.ns = si.n;
+      b.h = si.h;
+      const double c = si.V * si.chi / (1.0 + si.chi);
+      SceneSpec r = b;  // r = c G b + Hext - b
+      r.scale = c;
+      r.coef_add = 1.0;
+      r.coef_add2 = -1.0;
+      resid.push_back(r);
+      SceneSpec q = b;  // q = p - c G p
+      q.scale = -c;
+      q.coef_add = 1.0;
+      cgq.push_back(q);
+      force.push_back(b);
+      pairs_ += double(si.n) * double(si.n);
+    }
+    MF_TRY(build_plan<float>(Body::FieldF2, resid, plan_resid_));
+    MF_TRY(build_plan<float>(Body::FieldF2, cgq, plan_cgq_));
+    MF_TRY(build_plan<float>(Body::ForceF2, force, plan_force_));
+    for (const Plan<float>* p : {&plan_resid_, &plan_cgq_, &plan_force_}) {
+      size_t pd = 0, nc = 0;
+      plan_scratch_needs(*p, &pd, &nc);
+      MF_TRY(scr_.ensure(pd, nc));
+    }
+
+    std::vector<CellSceneSpec> cs;
+    for (const SI& si : sc_) cs.push_back(CellSceneSpec{si.off, si.n, si.h});
+    MF_TRY(cells_.build(pos4_.as<float4>(), cs, st_, /*margin_h=*/2.0));
+    to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
+    MF_CUDA_TRY(cudaGetLastError());
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    iters_base_.assign(size_t(n), 0.0);
+    return MF_OK;
+  }
+
+  void set_stream(cudaStream_t s) {
+    st_ = s ? s : own_stream_;
+    drop_graph();
+  }
+  int scenes() const { return int(sc_.size()); }
+
+  // ---- solve -----------------------------------------------------------------
+  mf_status solve(int64_t max_iter, double tol, bool host_checks) {
+    const int n = scenes();
+    k_batch_init_rows<<<(n + 127) / 128, 128, 0, st_>>>(scal_.as<double>(), n, tol, double(max_iter),
+                                                        done_count_.as<int32_t>());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    // r = c G b + Hext - b
+    MF_TRY(field(plan_resid_, b4_.as<float4>(), r4_.as<float4>(), hext4_.as<float4>(), b4_.as<float4>(), false));
+    MF_TRY(reduce(CgStart<float4>{r4_.as<float4>(), p4_.as<float4>(), hext4_.as<float4>(), done_count_.as<int32_t>()}));
+    ++solves_;
+    for (int64_t it = 0; it < max_iter; ++it) {
+      MF_TRY(field(plan_cgq_, p4_.as<float4>(), q4_.as<float4>(), p4_.as<float4>(), nullptr, true));
+      MF_TRY(reduce(CgPq<float4>{p4_.as<float4>(), q4_.as<float4>(), done_count_.as<int32_t>()}));
+      MF_TRY(reduce(CgUpdate<float, float4>{b4_.as<float4>(), r4_.as<float4>(), p4_.as<float4>(), q4_.as<float4>(),
+                                            done_count_.as<int32_t>()}));
+      MF_TRY(reduce(CgDirection<float, float4>{r4_.as<float4>(), p4_.as<float4>()}));
+      if (host_checks && (it % 4 == 3 || it + 1 == max_iter)) {
+        MF_CUDA_TRY(cudaMemcpyAsync(pinned_, done_count_.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+        MF_CUDA_TRY(cudaStreamSynchronize(st_));
+        if (*static_cast<int32_t*>(pinned_) >= n) break;
+      }
+    }
+    MF_TRY(reduce(BPublish{b4_.as<float4>(), mom4_.as<float4>()}));
+    return MF_OK;
+  }
+
+  mf_status eval_force() {
+    to_pairs(mom4_.as<float4>(), mom2_.as<float4>(), n_alloc_, st_);
+    MF_TRY(cells_.force_correction(pos4_.as<float4>(), mom4_.as<float4>(), corr_.as<float4>(), st_));
+    LaunchIO<float> io;
+    io.tpos = pos4_.as<float4>();
+    io.tmom = mom4_.as<float4>();
+    io.spos = pos2_.as<float4>();
+    io.smom = mom2_.as<float4>();
+    io.corr4 = corr_.as<float4>();
+    float* F = fs_.as<float>();
+    for (int k = 0; k < 3; ++k) io.out[k] = F + int64_t(k) * n_alloc_;
+    MF_TRY(run_plan<float>(plan_force_, io, scr_, st_));
+    ctr_.kernel_launches += 3;
+    ctr_.force_passes += 1;
+    ctr_.force_pairs += pairs_;
+    return MF_OK;
+  }
+
+  mf_status step(double dt, int iters, double tol) {
+    MF_TRY(solve(iters, tol, false));
+    MF_TRY(eval_force());
+    const float* F = fs_.as<float>();
+    MF_TRY(reduce(BIntegrate{F, F + n_alloc_, F + 2 * n_alloc_, vel4_.as<float4>(), pos4_.as<float4>(), float(dt)}));
+    MF_TRY(cells_.rebin(pos4_.as<float4>(), st_));
+    to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
+    MF_CUDA_TRY(cudaGetLastError());
+    ctr_.kernel_launches += 6;
+    return MF_OK;
+  }
+
+  mf_status advance(double dt, int steps, int iters, double tol, bool graph) {
+    if (steps < 0 || iters < 0) return fail(MF_ERR_INVALID_ARG, "negative steps or iterations");
+    if (!graph) {
+      for (int k = 0; k < steps; ++k) MF_TRY(step(dt, iters, tol));
+      MF_CUDA_TRY(cudaStreamSynchronize(st_));
+      MF_TRY(scr_.check(st_));
+      return MF_OK;
+    }
+    if (!gexec_ || g_dt_ != dt || g_iters_ != iters || g_tol_ != tol) {
+      drop_graph();
+      cudaGraph_t gr = nullptr;
+      MF_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+      const mf_counters saved = ctr_;
+      mf_status s = step(dt, iters, tol);
+      cudaError_t e = cudaStreamEndCapture(st_, &gr);
+      launches_per_step_ = ctr_.kernel_launches - saved.kernel_launches;
+      force_per_step_ = ctr_.force_passes - saved.force_passes;
+      ctr_ = saved;  // capture records the launches; the replays count them
+      if (s != MF_OK) {
+        if (gr) cudaGraphDestroy(gr);
+        return s;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&gexec_, gr, 0);
+      cudaGraphDestroy(gr);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      g_dt_ = dt;
+      g_iters_ = iters;
+      g_tol_ = tol;
+    }
+    for (int k = 0; k < steps; ++k) {
+      MF_CUDA_TRY(cudaGraphLaunch(gexec_, st_));
+      ++solves_;
+      ctr_.kernel_launches += launches_per_step_;
+      ctr_.force_passes += force_per_step_;
+      ctr_.force_pairs += double(force_per_step_) * pairs_;
+    }
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    MF_TRY(scr_.check(st_));
+    return MF_OK;
+  }
+
+  // ---- results ---------------------------------------------------------------
+  mf_status get(int scene, int q, float* dst) {
+    if (scene < 0 || scene >= scenes()) return fail(MF_ERR_INVALID_ARG, "scene index out of range");
+    if (!dst) return fail(MF_ERR_INVALID_ARG, "dst is NULL");
+    const SI& si = sc_[size_t(scene)];
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    if (q == MF_Q_FORCE) {
+      std::vector<float> t(size_t(si.n));
+      for (int k = 0; k < 3; ++k) {
+        MF_CUDA_TRY(cudaMemcpy(t.data(), fs_.as<float>() + int64_t(k) * n_alloc_ + si.off,
+                               size_t(si.n) * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < si.n; ++i) dst[3 * i + k] = t[size_t(i)];
+      }
+      return MF_OK;
+    }
+    const DevBuf* src = nullptr;
+    switch (q) {
+      case MF_Q_POSITIONS: src = &pos4_; break;
+      case MF_Q_M: src = &mom4_; break;
+      case MF_Q_B_OVER_MU0: src = &b4_; break;
+      case MF_Q_HEXT: src = &hext4_; break;
+      case MF_Q_VELOCITY: src = &vel4_; break;
+      default: return fail(MF_ERR_INVALID_ARG, "quantity not kept for batched scenes");
+    }
+    std::vector<float4> t(size_t(si.n));
+    MF_CUDA_TRY(cudaMemcpy(t.data(), src->as<float4>() + si.off, size_t(si.n) * sizeof(float4),
+                           cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < si.n; ++i) {
+      dst[3 * i] = t[size_t(i)].x;
+      dst[3 * i + 1] = t[size_t(i)].y;
+      dst[3 * i + 2] = t[size_t(i)].z;
+    }
+    return MF_OK;
+  }
+
+  mf_status solver_state(double* relres, double* iters) {
+    const int n = scenes();
+    std::vector<double> rows(size_t(n) * kScal);
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    MF_CUDA_TRY(cudaMemcpy(rows.data(), scal_.ptr, rows.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < n; ++s) {
+      if (relres) relres[s] = rows[size_t(s) * kScal + S_RELRES];
+      if (iters) iters[s] = rows[size_t(s) * kScal + S_ITERS];
+    }
+    return MF_OK;
+  }
+
+  // Field pairs actually evaluated: every solve runs one residual product for
+  // every scene, and each CG iteration a product for the scenes still going.
+  mf_status counters(mf_counters* c) {
+    const int n = scenes();
+    std::vector<double> rows(size_t(n) * kScal);
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    MF_CUDA_TRY(cudaMemcpy(rows.data(), scal_.ptr, rows.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double fp = 0;
+    int64_t products = 0;
+    for (int s = 0; s < n; ++s) {
+      const double nn = double(sc_[size_t(s)].n) * double(sc_[size_t(s)].n);
+      const double it = rows[size_t(s) * kScal + S_ITERS_TOTAL] - iters_base_[s];
+      fp += nn * (double(solves_ - solves_base_) + it);
+      products = std::max<int64_t>(products, int64_t(it));
+    }
+    *c = ctr_;
+    c->field_pairs = fp;
+    c->field_products = products + (solves_ - solves_base_);
+    return MF_OK;
+  }
+
+  mf_status reset_counters() {
+    const int n = scenes();
+    std::vector<double> rows(size_t(n) * kScal);
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    MF_CUDA_TRY(cudaMemcpy(rows.data(), scal_.ptr, rows.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    iters_base_.assign(size_t(n), 0.0);
+    for (int s = 0; s < n; ++s) iters_base_[size_t(s)] = rows[size_t(s) * kScal + S_ITERS_TOTAL];
+    solves_base_ = solves_;
+    ctr_ = mf_counters{};
+    return MF_OK;
+  }
+
+  cudaStream_t stream() const { return st_; }
+  int device_ = 0;
+
+ private:
+  struct SI {
+    int64_t off, n;
+    double h, V, chi;
+    float H0[3];
+  };
+
+  mf_status field(const Plan<float>& plan, const float4* src_mom, float4* out4, const float4* add4,
+                  const float4* add4b, bool skip_done) {
+    const int n = scenes();
+    const int32_t* dc = skip_done ? done_count_.as<int32_t>() : nullptr;
+    to_pairs(src_mom, mom2_.as<float4>(), n_alloc_, st_, dc, n);
+    MF_TRY(cells_.field_correction(pos4_.as<float4>(), src_mom, corr_.as<float4>(), st_,
+                                   skip_done ? scal_.as<double>() : nullptr, kScal, dc, n));
+    LaunchIO<float> io;
+    io.tpos = pos4_.as<float4>();
+    io.spos = pos2_.as<float4>();
+    io.smom = mom2_.as<float4>();
+    io.corr4 = corr_.as<float4>();
+    io.out4 = out4;
+    io.add4 = add4;
+    io.add4b = add4b;
+    if (skip_done) {
+      io.done_flags = scal_.as<double>();
+      io.done_stride = kScal;
+      io.done_count = dc;
+      io.done_total = n;
+    }
+    MF_TRY(run_plan<float>(plan, io, scr_, st_));
+    ctr_.kernel_launches += 3;
+    return MF_OK;
+  }
+
+  template <class Op>
+  mf_status reduce(const Op& op) {
+    const dim3 grid{static_cast<unsigned>(red_gx_), static_cast<unsigned>(scenes())};
+    reduce_kernel<Op><<<grid, 256, 0, st_>>>(op, ranges_.as<VecRange>(), scal_.as<double>(),
+                                             red_part_.as<double>(), red_tickets_.as<int32_t>());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    return MF_OK;
+  }
+
+  void drop_graph() {
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    gexec_ = nullptr;
+  }
+
+  std::vector<SI> sc_;
+  int64_t n_alloc_ = 0;
+  double pairs_ = 0;
+  int sms_ = 1;
+  int red_gx_ = 1;
+  cudaStream_t st_ = nullptr, own_stream_ = nullptr;
+  void* pinned_ = nullptr;
+  DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
+  DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
+  Plan<float> plan_resid_, plan_cgq_, plan_force_;
+  Scratch scr_;
+  CellList cells_;
+  mf_counters ctr_ = {};
+  int64_t solves_ = 0, solves_base_ = 0;
+  std::vector<double> iters_base_;
+  cudaGraphExec_t gexec_ = nullptr;
+  double g_dt_ = 0, g_tol_ = 0;
+  int g_iters_ = -1;
+  int64_t launches_per_step_ = 0, force_per_step_ = 0;
+};
+
+}  // namespace mfgb
+
+using namespace mfgb;
+
+struct mf_batch {
+  std::unique_ptr<Batch> b;
+  int device = 0;
+};
+
+namespace {
+template <class F>
+mf_status bguard(mf_batch* b, F&& fn) {
+  if (!b || !b->b) return fail(MF_ERR_INVALID_ARG, "NULL batch handle");
+  try {
+    cudaError_t e = cudaSetDevice(b->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return fn(*b->b);
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  } catch (...) {
+    return fail(MF_ERR_CUDA, "unexpected exception");
+  }
+}
+}  // namespace
+
+extern "C" {
+
+mf_status mf_batch_create(const mf_scene_desc* scenes, int32_t n_scenes, int32_t device, mf_batch** out) {
+  if (!out) return fail(MF_ERR_INVALID_ARG, "NULL out");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MF_ERR_UNSUPPORTED, "no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(MF_ERR_INVALID_ARG, "bad device ordinal");
+  try {
+    MF_CUDA_TRY(cudaSetDevice(device));
+    std::unique_ptr<mf_batch> h(new mf_batch);
+    h->device = device;
+    h->b.reset(new Batch());
+    h->b->device_ = device;
+    MF_TRY(h->b->init(scenes, n_scenes, device));
+    *out = h.release();
+    return MF_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  }
+}
+
+mf_status mf_batch_destroy(mf_batch* b) {
+  if (!b) return MF_OK;
+  cudaSetDevice(b->device);
+  if (b->b) cudaStreamSynchronize(b->b->stream());
+  delete b;
+  return MF_OK;
+}
+
+mf_status mf_batch_set_stream(mf_batch* b, void* stream) {
+  return bguard(b, [&](Batch& x) {
+    x.set_stream(static_cast<cudaStream_t>(stream));
+    return MF_OK;
+  });
+}
+
+mf_status mf_batch_num_scenes(mf_batch* b, int32_t* n) {
+  return bguard(b, [&](Batch& x) {
+    if (!n) return fail(MF_ERR_INVALID_ARG, "NULL");
+    *n = x.scenes();
+    return MF_OK;
+  });
+}
+
+mf_status mf_batch_solve(mf_batch* b, int64_t max_iter, double rel_tol, int64_t* max_iters, double* worst_res) {
+  return bguard(b, [&](Batch& x) {
+    if (max_iter < 0 || !(rel_tol > 0)) return fail(MF_ERR_INVALID_ARG, "bad iteration cap or tolerance");
+    MF_TRY(x.solve(max_iter, rel_tol, true));
+    std::vector<double> rr(size_t(x.scenes())), it(size_t(x.scenes()));
+    MF_TRY(x.solver_state(rr.data(), it.data()));
+    if (max_iters) *max_iters = int64_t(*std::max_element(it.begin(), it.end()));
+    const double worst = *std::max_element(rr.begin(), rr.end());
+    if (worst_res) *worst_res = worst;
+    return worst < rel_tol ? MF_OK : fail(MF_ERR_NOT_CONVERGED, "some scenes stopped above tolerance");
+  });
+}
+
+mf_status mf_batch_eval_force(mf_batch* b) {
+  return bguard(b, [&](Batch& x) { return x.eval_force(); });
+}
+
+mf_status mf_batch_advance(mf_batch* b, double dt, int32_t steps, int32_t iters_per_step, double rel_tol,
+                           int32_t use_graph) {
+  return bguard(b, [&](Batch& x) {
+    if (!std::isfinite(dt) || !(rel_tol > 0)) return fail(MF_ERR_INVALID_ARG, "bad dt or tolerance");
+    return x.advance(dt, steps, iters_per_step, rel_tol, use_graph != 0);
+  });
+}
+
+mf_status mf_batch_get(mf_batch* b, int32_t scene, int32_t quantity, float* dst) {
+  return bguard(b, [&](Batch& x) { return x.get(scene, quantity, dst); });
+}
+
+mf_status mf_batch_solver_state(mf_batch* b, double* rel_res, double* iters) {
+  return bguard(b, [&](Batch& x) { return x.solver_state(rel_res, iters); });
+}
+
+mf_status mf_batch_get_counters(mf_batch* b, mf_counters* c) {
+  return bguard(b, [&](Batch& x) {
+    if (!c) return fail(MF_ERR_INVALID_ARG, "NULL");
+    return x.counters(c);
+  });
+}
+
+mf_status mf_batch_reset_counters(mf_batch* b) {
+  return bguard(b, [&](Batch& x) { return x.reset_counters(); });
+}
+
+}  // extern "C"

@@ -178,8 +178,11 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
                                                           int64_t n_cells, const int32_t* __restrict__ perm,
                                                           const int32_t* __restrict__ start,
                                                           const float4* __restrict__ pos,
-                                                          const float4* __restrict__ mom, float4* __restrict__ corr) {
+                                                          const float4* __restrict__ mom, float4* __restrict__ corr,
+                                                          const double* __restrict__ done_flags, int done_stride,
+                                                          const int32_t* __restrict__ done_count, int done_total) {
   constexpr int kT = 8;
+  if (done_count && *done_count >= done_total) return;
   __shared__ float s_tbl[40];
   if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];
   __syncthreads();
@@ -194,6 +197,7 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
       if (grids[mid].cell_off <= c) lo = mid;
       else hi = mid - 1;
     }
+    if (done_flags && done_flags[int64_t(lo) * done_stride] != 0.0) continue;  // scene's solve stopped
     const CellGrid& g = grids[lo];
     const int64_t lc = c - g.cell_off;
     const int ix = int(lc % g.nx), iy = int((lc / g.nx) % g.ny), iz = int(lc / (int64_t(g.nx) * g.ny));
@@ -341,7 +345,9 @@ __global__ void __launch_bounds__(128) k_correction(const CellGrid* __restrict__
   }
 }
 
-__global__ void k_to_pairs(const float4* __restrict__ src, float4* __restrict__ dst, int64_t n) {
+__global__ void k_to_pairs(const float4* __restrict__ src, float4* __restrict__ dst, int64_t n,
+                           const int32_t* __restrict__ done_count, int done_total) {
+  if (done_count && *done_count >= done_total) return;
   const int64_t np = (n + 1) / 2;
   for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < np; p += int64_t(gridDim.x) * blockDim.x) {
     const float4 a = src[2 * p];
@@ -359,11 +365,13 @@ unsigned grid_for(int64_t n, int per_block = 256) {
 
 }  // namespace
 
-void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st) {
-  k_to_pairs<<<grid_for((n + 1) / 2), 256, 0, st>>>(src, dst, n);
+void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st, const int32_t* done_count,
+              int done_total) {
+  k_to_pairs<<<grid_for((n + 1) / 2), 256, 0, st>>>(src, dst, n, done_count, done_total);
 }
 
-mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st) {
+mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st,
+                          double margin_h) {
   const int ns = int(scenes.size());
   if (ns == 0) return fail(MF_ERR_INVALID_ARG, "cell list: no scenes");
   n_scenes_ = ns;
@@ -396,8 +404,8 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
     const double h = scenes[s].h;
     double lo[3], ext[3];
     for (int c = 0; c < 3; ++c) {
-      lo[c] = ord2f(hb[6 * s + c]);
-      ext[c] = std::max(0.0, double(ord2f(hb[6 * s + 3 + c])) - lo[c]);
+      lo[c] = ord2f(hb[6 * s + c]) - margin_h * h;
+      ext[c] = std::max(0.0, double(ord2f(hb[6 * s + 3 + c])) + margin_h * h - lo[c]);
       if (!std::isfinite(lo[c]) || !std::isfinite(ext[c])) return fail(MF_ERR_INVALID_ARG, "non-finite positions");
     }
     // Cells a hair wider than h (about 8 particles at h = 2 spacings): a point
@@ -437,6 +445,12 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
   MF_TRY(perm_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(perm_tmp_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(cell_of_.reserve(sizeof(int32_t) * size_t(n_total_)));
+  return rebin(pos4, st);
+}
+
+mf_status CellList::rebin(const float4* pos4, cudaStream_t st) {
+  const int64_t cells = n_cells_;
+  const int ns = n_scenes_;
   int32_t* counts = cursor_.as<int32_t>();
   MF_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * size_t(cells + 1), st));
   const CellGrid* dg = grids_.as<CellGrid>();
@@ -458,10 +472,12 @@ static unsigned cell_grid(int64_t cells) {
   return unsigned(g < 1 ? 1 : g);
 }
 
-mf_status CellList::field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
-  k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
-                                                                   perm_.as<int32_t>(), cell_start_.as<int32_t>(),
-                                                                   pos4, mom4, corr);
+mf_status CellList::field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st,
+                                     const double* done_flags, int done_stride, const int32_t* done_count,
+                                     int done_total) const {
+  k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
+      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
+      done_flags, done_stride, done_count, done_total);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }
@@ -477,9 +493,9 @@ mf_status CellList::field_correction_at(const float4* tpos4, int64_t nt, const f
 }
 
 mf_status CellList::force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
-  k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, n_cells_,
-                                                                  perm_.as<int32_t>(), cell_start_.as<int32_t>(),
-                                                                  pos4, mom4, corr);
+  k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
+      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
+      nullptr, 0, nullptr, 0);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

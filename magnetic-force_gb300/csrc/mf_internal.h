@@ -170,6 +170,8 @@ struct LaunchIO {
   const double* done_flags = nullptr;
   int done_stride = 0;
   const R4* corr4 = nullptr;
+  const int32_t* done_count = nullptr;
+  int32_t done_total = 0;
 };
 
 // Scratch sizes a plan needs.
@@ -214,11 +216,21 @@ class CellList {
   // Bins the particles of every scene into cells of edge >= 2h; particles of
   // a cell are listed in increasing index order (deterministic sums).
   // Synchronises `st` once (the bounding boxes are read on the host).
-  mf_status build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st);
+  mf_status build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st,
+                  double margin_h = 0.0);
+  // Re-bins moved particles on the grids of the last build (no host
+  // synchronisation, so it can be captured in a CUDA graph).  Particles that
+  // left a grid are binned into its border cells, which keeps every
+  // neighbour within reach; build() with a margin (in units of h) leaves room.
+  mf_status rebin(const float4* pos4, cudaStream_t st);
   // corr_i = sum over j within 2h (resp. 4h) of [exact pair term - the
   // clamped far term the packed all-pairs loop gave that pair], in the
   // all-pairs kernels' output units.  Targets = sources = the binned set.
-  mf_status field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const;
+  // done_flags (per-scene solver rows) skip stopped scenes; done_count /
+  // done_total make the launch a no-op once every scene has stopped.
+  mf_status field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st,
+                             const double* done_flags = nullptr, int done_stride = 0,
+                             const int32_t* done_count = nullptr, int done_total = 0) const;
   mf_status force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const;
   // Field correction at separate targets tpos4[0..nt) (single-scene lists).
   mf_status field_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
@@ -236,6 +248,7 @@ class CellList {
 
 // Packed records -> pair layout (sources 2p, 2p+1 as (x_a, x_b, y_a, y_b),
 // (z_a, z_b, 0, 0)); a missing partner (odd n) is written as zeros.
-void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st);
+void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st, const int32_t* done_count = nullptr,
+              int done_total = 0);
 
 }  // namespace mfgb

@@ -35,6 +35,12 @@ enum Scal : int {
   S_DG = 14,     // d_old . (g_old - g)
   S_C = 15,      // c = V chi / (1 + chi)
   S_RESET = 16,  // NLCG: beta restart this iteration
+  // Slots 20.. are kept across solves (batched scenes): per-scene constants
+  // and the running total of CG iterations.
+  S_CONST_C = 20,      // c = V chi / (1 + chi)
+  S_CONST_INVM = 21,   // 1 / particle mass (unit density: 1 / V)
+  S_CONST_H0 = 22,     // uniform external field, 3 slots
+  S_ITERS_TOTAL = 25,  // CG iterations over all solves
   kScal = 32
 };
 
@@ -122,12 +128,21 @@ __global__ void __launch_bounds__(256) reduce_kernel(Op op, const VecRange* rang
 // Conjugate gradients on (I - c G) b = Hext.  The field launch before CgStart
 // leaves r = c G b + Hext - b; before CgPq it leaves q = p - c G p.
 // ---------------------------------------------------------------------------
+// Marks a scene's solve as stopped, counting it once in *done_count (if given).
+__device__ __forceinline__ void mark_done(double* row, int32_t* done_count) {
+  if (row[S_DONE] == 0.0) {
+    row[S_DONE] = 1.0;
+    if (done_count) atomicAdd(done_count, 1);
+  }
+}
+
 template <class R4>
 struct CgStart {
   static constexpr int kN = 2;
   const R4* r;
   R4* p;
   const R4* hext;
+  int32_t* done_count = nullptr;
   __device__ bool skip(const double*) const { return false; }
   __device__ void elem(int64_t i, double* acc, const double*) const {
     const R4 ri = r[i];
@@ -141,7 +156,7 @@ struct CgStart {
     row[S_BNORM] = s[1] > 0.0 ? sqrt(s[1]) : 1.0;
     row[S_RELRES] = sqrt(s[0]) / row[S_BNORM];
     row[S_ITERS] = 0.0;
-    row[S_DONE] = (row[S_RELRES] < row[S_TOL] || row[S_MAXIT] <= 0.0) ? 1.0 : 0.0;
+    if (row[S_RELRES] < row[S_TOL] || row[S_MAXIT] <= 0.0) mark_done(row, done_count);
   }
 };
 
@@ -150,6 +165,7 @@ struct CgPq {
   static constexpr int kN = 1;
   const R4* p;
   const R4* q;
+  int32_t* done_count = nullptr;
   __device__ bool skip(const double* row) const { return row[S_DONE] != 0.0; }
   __device__ void elem(int64_t i, double* acc, const double*) const { acc[0] += dot4(p[i], q[i]); }
   __device__ void finish(const double* s, double* row) const {
@@ -158,7 +174,7 @@ struct CgPq {
       row[S_ALPHA] = row[S_RR] / s[0];
     } else {  // breakdown: the operator lost positive definiteness or r == 0
       row[S_ALPHA] = 0.0;
-      row[S_DONE] = 1.0;
+      mark_done(row, done_count);
     }
   }
 };
@@ -170,6 +186,7 @@ struct CgUpdate {
   R4* r;
   const R4* p;
   const R4* q;
+  int32_t* done_count = nullptr;
   __device__ bool skip(const double* row) const { return row[S_DONE] != 0.0; }
   __device__ void elem(int64_t i, double* acc, const double* row) const {
     const Real a = Real(row[S_ALPHA]);
@@ -191,7 +208,8 @@ struct CgUpdate {
     row[S_RR] = s[0];
     row[S_RELRES] = sqrt(s[0]) / row[S_BNORM];
     row[S_ITERS] += 1.0;
-    if (row[S_RELRES] < row[S_TOL] || row[S_ITERS] >= row[S_MAXIT]) row[S_DONE] = 1.0;
+    row[S_ITERS_TOTAL] += 1.0;
+    if (row[S_RELRES] < row[S_TOL] || row[S_ITERS] >= row[S_MAXIT]) mark_done(row, done_count);
   }
 };
 

@@ -299,6 +299,101 @@ class Solver:
     naive = property(lambda self: bool(self.get_option("naive")), lambda self, v: self.set_option("naive", 1 if v else 0))
 
 
+class mf_scene_desc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("pos", ctypes.c_void_p), ("h", ctypes.c_float), ("volume", ctypes.c_float),
+                ("chi", ctypes.c_float), ("H0", ctypes.c_float * 3)]
+
+
+def _batch_sigs(lib):
+    i32, i64, vp, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_double
+    sig = {
+        "mf_batch_create": (i32, [ctypes.POINTER(mf_scene_desc), i32, i32, ctypes.POINTER(vp)]),
+        "mf_batch_destroy": (i32, [vp]),
+        "mf_batch_set_stream": (i32, [vp, vp]),
+        "mf_batch_num_scenes": (i32, [vp, ctypes.POINTER(i32)]),
+        "mf_batch_solve": (i32, [vp, i64, f64, ctypes.POINTER(i64), ctypes.POINTER(f64)]),
+        "mf_batch_eval_force": (i32, [vp]),
+        "mf_batch_advance": (i32, [vp, f64, i32, i32, f64, i32]),
+        "mf_batch_get": (i32, [vp, i32, i32, vp]),
+        "mf_batch_solver_state": (i32, [vp, vp, vp]),
+        "mf_batch_get_counters": (i32, [vp, ctypes.POINTER(mf_counters)]),
+        "mf_batch_reset_counters": (i32, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+
+
+class Batch:
+    """Many independent scenes advanced together (mf_batch_* in mf.h)."""
+
+    def __init__(self, scenes, device: int = 0):
+        lib = load()
+        _batch_sigs(lib)
+        arr = (mf_scene_desc * len(scenes))()
+        self._keep = []
+        self.sizes = []
+        for k, sc in enumerate(scenes):
+            p = _f32(sc.pos)
+            self._keep.append(p)
+            self.sizes.append(len(p))
+            arr[k].n = len(p)
+            arr[k].pos = p.ctypes.data
+            arr[k].h, arr[k].volume, arr[k].chi = float(sc.h), float(sc.volume), float(sc.chi)
+            for j in range(3):
+                arr[k].H0[j] = float(sc.H0[j])
+        h = ctypes.c_void_p()
+        check(lib.mf_batch_create(arr, len(scenes), int(device), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().mf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, max_iter: int = 200, rel_tol: float = 1e-6):
+        it = ctypes.c_int64(0)
+        worst = ctypes.c_double(0)
+        st = load().mf_batch_solve(self._h, int(max_iter), float(rel_tol), ctypes.byref(it), ctypes.byref(worst))
+        if st not in (MF_OK, 3):
+            check(st)
+        return it.value, worst.value
+
+    def eval_force(self):
+        check(load().mf_batch_eval_force(self._h))
+
+    def advance(self, dt: float, steps: int, iters_per_step: int = 4, rel_tol: float = 1e-6, graph: bool = True):
+        check(load().mf_batch_advance(self._h, float(dt), int(steps), int(iters_per_step), float(rel_tol),
+                                      1 if graph else 0))
+
+    def get(self, scene: int, quantity: str) -> np.ndarray:
+        out = np.empty((self.sizes[scene], 3), dtype=np.float32)
+        check(load().mf_batch_get(self._h, int(scene), Q[quantity], out.ctypes.data))
+        return out
+
+    def solver_state(self):
+        n = len(self.sizes)
+        rr = np.zeros(n)
+        it = np.zeros(n)
+        check(load().mf_batch_solver_state(self._h, rr.ctypes.data, it.ctypes.data))
+        return rr, it
+
+    def counters(self) -> dict:
+        c = mf_counters()
+        check(load().mf_batch_get_counters(self._h, ctypes.byref(c)))
+        return {f: getattr(c, f) for f, _ in mf_counters._fields_}
+
+    def reset_counters(self):
+        check(load().mf_batch_reset_counters(self._h))
+
+
 def probe_fp32_peak() -> float:
     """Measured dense FP32 FMA throughput of the current device, TFLOP/s."""
     v = ctypes.c_double(0)
