@@ -60,7 +60,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--workload", default="allpairs65k", choices=["allpairs65k", "batch256", "plain4096"],
+    ap.add_argument("--requests", type=int, default=24)
+    ap.add_argument("--rate", type=float, default=2.0, help="served: mean Poisson arrival rate, requests/s")
+    ap.add_argument("--workload", default="allpairs65k", choices=["allpairs65k", "batch256", "plain4096", "served"],
                     help="allpairs65k: the headline config (default); batch256: 256 scenes log-uniform "
                          "in [512, 32768] in one launch per stage vs the same scenes one at a time; "
                          "plain4096: N=4096 uniform cube solved in FP64 to 1e-8")
@@ -538,11 +540,78 @@ def run_plain_fp64(args, rank, world, local):
     s.close()
 
 
+def run_served(args, rank, world, local):
+    """Served stream: Poisson arrivals (seeded, mean rate --rate) of scenes with
+    N log-uniform in [1024, 262144] and the batched config's per-scene
+    distributions, 20 timesteps each, continuous batching under a 120 GB
+    budget.  All scenes use the all-pairs path (the FMM path for N > 65,536 is
+    not built).  Reports p50/p99 per tick and per request and aggregate pairs/s."""
+    import math
+    import torch
+    import mfgb
+    import scenes
+
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(99 + rank)
+    reqs = []
+    for k in range(args.requests):
+        n = int(round(math.exp(rng.uniform(math.log(1024), math.log(262144)))))
+        r2 = np.random.default_rng(5000 + k)
+        H = r2.normal(size=3)
+        H /= np.linalg.norm(H)
+        reqs.append(scenes.jittered_lattice(n, "sphere", radius=float(r2.uniform(0.2, 0.5)),
+                                            chi=float(r2.uniform(0.5, 3.0)), seed=5000 + k, H0=tuple(H)))
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=len(reqs)))
+    srv = mfgb.Server(hbm_budget_bytes=120e9, max_active=64, steps_per_request=20, iters_per_step=4,
+                      rel_tol=1e-6, dt=args.dt, device=local)
+    # warm-up request (kernel load, first allocations), not measured
+    wid = srv.submit(scenes.jittered_lattice(2048, "sphere", 0.3, chi=1.0, seed=1))
+    while srv.poll(wid)[0] != 2:
+        srv.step()
+    s0 = srv.stats()
+    ids = []
+    tick_ms = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    while len(ids) < len(reqs) or any(srv.poll(i)[0] != 2 for i in ids):
+        now = time.perf_counter() - t0
+        while len(ids) < len(reqs) and arrivals[len(ids)] <= now:
+            ids.append(srv.submit(reqs[len(ids)]))
+        st = srv.stats()
+        if st["running"] + st["queued"] > 0:
+            a, c, ms = srv.step()
+            if a:
+                tick_ms.append(ms)
+        else:
+            time.sleep(max(0.0, min(0.05, arrivals[len(ids)] - now)))
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    s1 = srv.stats()
+    pairs = (s1["field_pairs"] + s1["force_pairs"]) - (s0["field_pairs"] + s0["force_pairs"])
+    lat = [srv.poll(i)[2] for i in ids]
+    if rank == 0:
+        ns = [r.n for r in reqs]
+        print(json.dumps({
+            "metric": METRIC, "workload": "served", "value": pairs / wall, "unit": UNIT,
+            "requests": len(reqs), "rate_per_s": args.rate, "n_range": [min(ns), max(ns)], "n_mean": float(np.mean(ns)),
+            "wall_s": wall, "busy_s": (s1["busy_ms"] - s0["busy_ms"]) / 1e3,
+            "p50_tick_ms": float(np.percentile(tick_ms, 50)), "p99_tick_ms": float(np.percentile(tick_ms, 99)),
+            "p50_request_ms": float(np.percentile(lat, 50)), "p99_request_ms": float(np.percentile(lat, 99)),
+            "ticks": s1["ticks"] - s0["ticks"], "rebatches": s1["rebatches"] - s0["rebatches"],
+            "pairs": pairs, "budget_bytes": 120e9, "clocks": clk,
+            "note": "all scenes on the all-pairs path; timesteps of 20 per request, <= 4 CG iterations per step"}),
+            flush=True)
+    srv.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "served":
+        run_served(args, rank, world, local)
     elif args.workload == "batch256":
         run_batch(args, rank, world, local)
     elif args.workload == "plain4096":

@@ -282,6 +282,50 @@ mf_status mf_batch_solver_state(mf_batch* b, double* rel_res, double* iters);
 mf_status mf_batch_get_counters(mf_batch* b, mf_counters* c);
 mf_status mf_batch_reset_counters(mf_batch* b);
 
+/* ---------------------------------------------------------------------- */
+/* Serving: a request queue with continuous batching (not in the reference).*/
+/* A request is a scene to advance by steps_per_request timesteps.  Each    */
+/* mf_server_step admits queued requests while the HBM budget and the slot  */
+/* limit allow, advances every running request by one timestep in shared   */
+/* batched launches, and retires finished requests (their final state is   */
+/* kept for mf_server_result).  Particle state stays on the device while a  */
+/* request runs.  A server is used by one host thread at a time.            */
+/* ---------------------------------------------------------------------- */
+typedef struct mf_server_config {
+  double hbm_budget_bytes;   /* admission budget for request state (e.g. 120e9) */
+  int32_t max_active;        /* running requests at most */
+  int32_t steps_per_request; /* timesteps each request runs */
+  int32_t iters_per_step;    /* CG iterations per timestep at most (warm start) */
+  int32_t device;
+  double rel_tol;            /* CG relative tolerance */
+  double dt;                 /* timestep */
+} mf_server_config;
+
+typedef struct mf_server_stats {
+  int64_t submitted, running, queued, completed;
+  int64_t ticks, rebatches;
+  double bytes_in_use;
+  double field_pairs, force_pairs;
+  double busy_ms;            /* wall time spent in mf_server_step */
+} mf_server_stats;
+
+typedef struct mf_server mf_server;
+
+mf_status mf_server_create(const mf_server_config* cfg, mf_server** out);
+mf_status mf_server_destroy(mf_server* s);
+/* Queues a copy of the scene.  MF_ERR_BUDGET if it alone exceeds the budget. */
+mf_status mf_server_submit(mf_server* s, const mf_scene_desc* scene, int64_t* request_id);
+/* One tick; *active gets the requests that ran, *completed those retired.
+ * *tick_ms (may be NULL) gets the tick's wall time. */
+mf_status mf_server_step(mf_server* s, int32_t* active, int32_t* completed, double* tick_ms);
+/* state: 0 queued, 1 running, 2 done.  *latency_ms: submit to done (done only). */
+mf_status mf_server_poll(mf_server* s, int64_t request_id, int32_t* state, int32_t* steps_done,
+                         double* latency_ms);
+/* Final MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0 or MF_Q_FORCE of a
+ * done request, host AoS [n][3]. */
+mf_status mf_server_result(mf_server* s, int64_t request_id, int32_t quantity, float* dst);
+mf_status mf_server_get_stats(mf_server* s, mf_server_stats* out);
+
 /* mf_direct_field without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- hosts that
  * have handed the device's whole memory budget to their own pool allocator,

@@ -13,10 +13,14 @@
 //     a launch does nothing once all scenes have stopped, so a fixed number of
 //     iterations can be captured in a CUDA graph.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
 #include <new>
+#include <stdexcept>
 #include <vector>
 
 #include "mf_internal.h"
@@ -84,19 +88,30 @@ class Batch {
     if (pinned_) cudaFreeHost(pinned_);
   }
 
-  mf_status init(const mf_scene_desc* d, int n, int device) {
+  // Device-resident state of one scene: n positions, velocities and warm
+  // starts (packed float4 records).
+  struct SceneState {
+    float4* pos;
+    float4* vel;
+    float4* b;
+  };
+
+  // Scenes from host positions (dev == nullptr), or from device-resident
+  // state (dev[s] for scene s; the descriptors' pos pointers are unused).
+  mf_status init(const mf_scene_desc* d, int n, int device, const SceneState* dev = nullptr) {
     if (n <= 0 || !d) return fail(MF_ERR_INVALID_ARG, "no scenes");
     device_ = device;
     sms_ = device_sms(device);
     int64_t off = 0, max_n = 0;
     for (int s = 0; s < n; ++s) {
       const mf_scene_desc& x = d[s];
-      if (x.n <= 0 || !x.pos) return fail(MF_ERR_INVALID_ARG, "scene without particles");
+      if (x.n <= 0 || (!dev && !x.pos)) return fail(MF_ERR_INVALID_ARG, "scene without particles");
       if (!(x.h > 0.f) || !(x.volume > 0.f) || !std::isfinite(x.h) || !std::isfinite(x.volume))
         return fail(MF_ERR_INVALID_ARG, "scene h and volume must be finite and > 0");
       if (!std::isfinite(x.chi) || x.chi <= -1.f) return fail(MF_ERR_INVALID_ARG, "scene chi must be > -1");
-      for (int64_t i = 0; i < 3 * x.n; ++i)
-        if (!std::isfinite(x.pos[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
+      if (!dev)
+        for (int64_t i = 0; i < 3 * x.n; ++i)
+          if (!std::isfinite(x.pos[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
       SI si;
       si.off = off;
       si.n = x.n;
@@ -126,12 +141,12 @@ class Batch {
     for (int s = 0; s < n; ++s) {
       const SI& si = sc_[size_t(s)];
       for (int64_t i = 0; i < si.n; ++i) {
-        hp[size_t(si.off + i)] = make_float4(d[s].pos[3 * i], d[s].pos[3 * i + 1], d[s].pos[3 * i + 2], 0.f);
+        if (!dev) hp[size_t(si.off + i)] = make_float4(d[s].pos[3 * i], d[s].pos[3 * i + 1], d[s].pos[3 * i + 2], 0.f);
         hh[size_t(si.off + i)] = make_float4(si.H0[0], si.H0[1], si.H0[2], 0.f);
       }
       // A scene with an odd count borrows its dummy partner's slot at its end:
       // park it on the scene's first particle (zero dipole, contributes nothing).
-      if (si.n & 1) hp[size_t(si.off + si.n)] = hp[size_t(si.off)];
+      if ((si.n & 1) && !dev) hp[size_t(si.off + si.n)] = hp[size_t(si.off)];
       double* row = &rows[size_t(s) * kScal];
       row[S_CONST_C] = si.V * si.chi / (1.0 + si.chi);
       row[S_CONST_INVM] = 1.0 / si.V;
@@ -139,6 +154,19 @@ class Batch {
       rg[size_t(s)] = VecRange{si.off, si.n};
     }
     MF_CUDA_TRY(cudaMemcpy(pos4_.ptr, hp.data(), v4, cudaMemcpyHostToDevice));
+    if (dev) {
+      for (int s = 0; s < n; ++s) {
+        const SI& si = sc_[size_t(s)];
+        const size_t bytes = size_t(si.n) * sizeof(float4);
+        MF_CUDA_TRY(cudaMemcpyAsync(pos4_.as<float4>() + si.off, dev[s].pos, bytes, cudaMemcpyDeviceToDevice, st_));
+        MF_CUDA_TRY(cudaMemcpyAsync(vel4_.as<float4>() + si.off, dev[s].vel, bytes, cudaMemcpyDeviceToDevice, st_));
+        MF_CUDA_TRY(cudaMemcpyAsync(b4_.as<float4>() + si.off, dev[s].b, bytes, cudaMemcpyDeviceToDevice, st_));
+        if (si.n & 1)
+          MF_CUDA_TRY(cudaMemcpyAsync(pos4_.as<float4>() + si.off + si.n, dev[s].pos, sizeof(float4),
+                                      cudaMemcpyDeviceToDevice, st_));
+      }
+      MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    }
     MF_CUDA_TRY(cudaMemcpy(hext4_.ptr, hh.data(), v4, cudaMemcpyHostToDevice));
     MF_TRY(scal_.reserve(rows.size() * sizeof(double)));
     MF_CUDA_TRY(cudaMemcpy(scal_.ptr, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -375,6 +403,16 @@ class Batch {
     return MF_OK;
   }
 
+  // Copies scene s's positions, velocities and warm start out (device to device).
+  mf_status export_state(int s, const SceneState& dst) {
+    const SI& si = sc_[size_t(s)];
+    const size_t bytes = size_t(si.n) * sizeof(float4);
+    MF_CUDA_TRY(cudaMemcpyAsync(dst.pos, pos4_.as<float4>() + si.off, bytes, cudaMemcpyDeviceToDevice, st_));
+    MF_CUDA_TRY(cudaMemcpyAsync(dst.vel, vel4_.as<float4>() + si.off, bytes, cudaMemcpyDeviceToDevice, st_));
+    MF_CUDA_TRY(cudaMemcpyAsync(dst.b, b4_.as<float4>() + si.off, bytes, cudaMemcpyDeviceToDevice, st_));
+    return MF_OK;
+  }
+
   cudaStream_t stream() const { return st_; }
   int device_ = 0;
 
@@ -447,9 +485,291 @@ class Batch {
   int64_t launches_per_step_ = 0, force_per_step_ = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Serving with continuous batching.
+// ---------------------------------------------------------------------------
+class Server {
+  using Clock = std::chrono::steady_clock;
+
+ public:
+  ~Server() { batch_.reset(); }
+
+  mf_status init(const mf_server_config& c) {
+    if (!(c.hbm_budget_bytes > 0) || c.max_active <= 0 || c.steps_per_request <= 0 || c.iters_per_step < 0 ||
+        !(c.rel_tol > 0) || !std::isfinite(c.dt))
+      return fail(MF_ERR_INVALID_ARG, "bad server configuration");
+    cfg_ = c;
+    return MF_OK;
+  }
+
+  // Device bytes a running request holds: its own state (3 records per
+  // particle) plus its share of the batch buffers, cell list and scratch.
+  static double need_bytes(int64_t n) { return double(n) * 320.0 + 4.0 * 1024 * 1024; }
+
+  mf_status submit(const mf_scene_desc& d, int64_t* id) {
+    if (d.n <= 0 || !d.pos) return fail(MF_ERR_INVALID_ARG, "scene without particles");
+    if (need_bytes(d.n) > cfg_.hbm_budget_bytes) return fail(MF_ERR_BUDGET, "scene exceeds the HBM budget");
+    for (int64_t i = 0; i < 3 * d.n; ++i)
+      if (!std::isfinite(d.pos[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");
+    Req r;
+    r.id = next_id_++;
+    r.d = d;
+    r.pos.assign(d.pos, d.pos + 3 * d.n);
+    r.d.pos = nullptr;
+    r.t_submit = Clock::now();
+    queue_.push_back(r.id);
+    reqs_.emplace(r.id, std::move(r));
+    ++stats_.submitted;
+    if (id) *id = reqs_.rbegin()->first;
+    return MF_OK;
+  }
+
+  mf_status step(int32_t* n_active, int32_t* n_completed, double* tick_ms) {
+    const auto t0 = Clock::now();
+    int completed = 0;
+    // Admit in arrival order while the budget and the slots allow.
+    while (!queue_.empty() && int(active_.size()) < cfg_.max_active) {
+      Req& r = reqs_.at(queue_.front());
+      const double need = need_bytes(r.d.n);
+      if (used_ + need > cfg_.hbm_budget_bytes) break;
+      const size_t bytes = size_t(r.d.n) * sizeof(float4);
+      MF_TRY(r.state.reserve(3 * bytes, false, true));
+      std::vector<float4> p(size_t(r.d.n));
+      for (int64_t i = 0; i < r.d.n; ++i) p[size_t(i)] = make_float4(r.pos[3 * i], r.pos[3 * i + 1], r.pos[3 * i + 2], 0.f);
+      MF_CUDA_TRY(cudaMemcpy(r.state.ptr, p.data(), bytes, cudaMemcpyHostToDevice));
+      used_ += need;
+      r.phase = 1;
+      active_.push_back(r.id);
+      queue_.pop_front();
+      dirty_ = true;
+    }
+    if (!active_.empty()) {
+      if (dirty_) MF_TRY(rebatch());
+      MF_TRY(batch_->step(cfg_.dt, cfg_.iters_per_step, cfg_.rel_tol));
+      MF_CUDA_TRY(cudaStreamSynchronize(batch_->stream()));
+      ++stats_.ticks;
+      for (int64_t id : active_) ++reqs_.at(id).steps;
+      // Retire finished requests: keep their final state on the host.
+      std::vector<int64_t> keep;
+      for (size_t k = 0; k < members_.size(); ++k) {
+        Req& r = reqs_.at(members_[k]);
+        if (r.steps >= cfg_.steps_per_request) {
+          const int s = int(k);
+          r.out.resize(5);
+          const int qs[5] = {MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0, MF_Q_FORCE};
+          for (int j = 0; j < 5; ++j) {
+            r.out[size_t(j)].resize(size_t(3 * r.d.n));
+            MF_TRY(batch_->get(s, qs[j], r.out[size_t(j)].data()));
+          }
+          r.state.release();
+          used_ -= need_bytes(r.d.n);
+          r.phase = 2;
+          r.t_done = Clock::now();
+          ++completed;
+          ++stats_.completed;
+          dirty_ = true;
+        } else {
+          keep.push_back(r.id);
+        }
+      }
+      active_ = keep;
+    }
+    const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+    stats_.busy_ms += ms;
+    if (n_active) *n_active = int32_t(active_.size() + size_t(completed));
+    if (n_completed) *n_completed = completed;
+    if (tick_ms) *tick_ms = ms;
+    return MF_OK;
+  }
+
+  mf_status poll(int64_t id, int32_t* phase, int32_t* steps, double* latency_ms) {
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) return fail(MF_ERR_INVALID_ARG, "unknown request");
+    const Req& r = it->second;
+    if (phase) *phase = r.phase;
+    if (steps) *steps = r.steps;
+    if (latency_ms)
+      *latency_ms = r.phase == 2 ? std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count() : -1.0;
+    return MF_OK;
+  }
+
+  mf_status result(int64_t id, int q, float* dst) {
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) return fail(MF_ERR_INVALID_ARG, "unknown request");
+    const Req& r = it->second;
+    if (r.phase != 2) return fail(MF_ERR_INVALID_ARG, "request not done");
+    if (!dst) return fail(MF_ERR_INVALID_ARG, "dst is NULL");
+    int j = -1;
+    switch (q) {
+      case MF_Q_POSITIONS: j = 0; break;
+      case MF_Q_VELOCITY: j = 1; break;
+      case MF_Q_M: j = 2; break;
+      case MF_Q_B_OVER_MU0: j = 3; break;
+      case MF_Q_FORCE: j = 4; break;
+      default: return fail(MF_ERR_INVALID_ARG, "quantity not kept for served requests");
+    }
+    std::copy(r.out[size_t(j)].begin(), r.out[size_t(j)].end(), dst);
+    return MF_OK;
+  }
+
+  mf_status get_stats(mf_server_stats* out) {
+    mf_server_stats s = stats_;
+    s.running = int64_t(active_.size());
+    s.queued = int64_t(queue_.size());
+    s.bytes_in_use = used_;
+    if (batch_) {
+      mf_counters c{};
+      MF_TRY(batch_->counters(&c));
+      s.field_pairs += c.field_pairs;
+      s.force_pairs += c.force_pairs;
+    }
+    *out = s;
+    return MF_OK;
+  }
+
+ private:
+  struct Req {
+    int64_t id = 0;
+    mf_scene_desc d{};
+    std::vector<float> pos;
+    DevBuf state;  // [3][n] float4: positions, velocities, warm start
+    int32_t phase = 0;
+    int32_t steps = 0;
+    Clock::time_point t_submit, t_done;
+    std::vector<std::vector<float>> out;
+  };
+
+  Batch::SceneState state_of(Req& r) {
+    float4* base = r.state.as<float4>();
+    return Batch::SceneState{base, base + r.d.n, base + 2 * r.d.n};
+  }
+
+  // Membership changed: save the continuing requests' state out of the old
+  // batch, lay out a new one over all running requests, bring new ones to a
+  // converged magnetization.
+  mf_status rebatch() {
+    if (batch_) {
+      for (size_t k = 0; k < members_.size(); ++k) {
+        Req& r = reqs_.at(members_[k]);
+        if (r.phase == 1) MF_TRY(batch_->export_state(int(k), state_of(r)));
+      }
+      MF_CUDA_TRY(cudaStreamSynchronize(batch_->stream()));
+      mf_counters c{};
+      MF_TRY(batch_->counters(&c));
+      stats_.field_pairs += c.field_pairs;
+      stats_.force_pairs += c.force_pairs;
+      batch_.reset();
+    }
+    members_ = active_;
+    std::vector<mf_scene_desc> descs;
+    std::vector<Batch::SceneState> st;
+    for (int64_t id : members_) {
+      Req& r = reqs_.at(id);
+      descs.push_back(r.d);
+      st.push_back(state_of(r));
+    }
+    batch_.reset(new Batch());
+    batch_->device_ = cfg_.device;
+    MF_TRY(batch_->init(descs.data(), int(descs.size()), cfg_.device, st.data()));
+    MF_TRY(batch_->solve(500, cfg_.rel_tol, true));
+    ++stats_.rebatches;
+    dirty_ = false;
+    return MF_OK;
+  }
+
+  mf_server_config cfg_{};
+  std::map<int64_t, Req> reqs_;
+  std::deque<int64_t> queue_;
+  std::vector<int64_t> active_, members_;
+  std::unique_ptr<Batch> batch_;
+  bool dirty_ = false;
+  double used_ = 0;
+  int64_t next_id_ = 1;
+  mf_server_stats stats_{};
+};
+
 }  // namespace mfgb
 
 using namespace mfgb;
+
+struct mf_server {
+  std::unique_ptr<Server> s;
+  int device = 0;
+};
+
+namespace {
+template <class F>
+mf_status sguard(mf_server* s, F&& fn) {
+  if (!s || !s->s) return fail(MF_ERR_INVALID_ARG, "NULL server handle");
+  try {
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return fn(*s->s);
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  } catch (const std::out_of_range&) {
+    return fail(MF_ERR_INVALID_ARG, "unknown request");
+  } catch (...) {
+    return fail(MF_ERR_CUDA, "unexpected exception");
+  }
+}
+}  // namespace
+
+extern "C" {
+
+mf_status mf_server_create(const mf_server_config* cfg, mf_server** out) {
+  if (!cfg || !out) return fail(MF_ERR_INVALID_ARG, "NULL argument");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MF_ERR_UNSUPPORTED, "no CUDA device available");
+  if (cfg->device < 0 || cfg->device >= ndev) return fail(MF_ERR_INVALID_ARG, "bad device ordinal");
+  try {
+    MF_CUDA_TRY(cudaSetDevice(cfg->device));
+    std::unique_ptr<mf_server> h(new mf_server);
+    h->device = cfg->device;
+    h->s.reset(new Server());
+    MF_TRY(h->s->init(*cfg));
+    *out = h.release();
+    return MF_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  }
+}
+
+mf_status mf_server_destroy(mf_server* s) {
+  if (!s) return MF_OK;
+  cudaSetDevice(s->device);
+  delete s;
+  return MF_OK;
+}
+
+mf_status mf_server_submit(mf_server* s, const mf_scene_desc* scene, int64_t* request_id) {
+  return sguard(s, [&](Server& x) {
+    if (!scene) return fail(MF_ERR_INVALID_ARG, "NULL scene");
+    return x.submit(*scene, request_id);
+  });
+}
+
+mf_status mf_server_step(mf_server* s, int32_t* active, int32_t* completed, double* tick_ms) {
+  return sguard(s, [&](Server& x) { return x.step(active, completed, tick_ms); });
+}
+
+mf_status mf_server_poll(mf_server* s, int64_t request_id, int32_t* state, int32_t* steps_done, double* latency_ms) {
+  return sguard(s, [&](Server& x) { return x.poll(request_id, state, steps_done, latency_ms); });
+}
+
+mf_status mf_server_result(mf_server* s, int64_t request_id, int32_t quantity, float* dst) {
+  return sguard(s, [&](Server& x) { return x.result(request_id, quantity, dst); });
+}
+
+mf_status mf_server_get_stats(mf_server* s, mf_server_stats* out) {
+  return sguard(s, [&](Server& x) {
+    if (!out) return fail(MF_ERR_INVALID_ARG, "NULL");
+    return x.get_stats(out);
+  });
+}
+
+}  // extern "C"
 
 struct mf_batch {
   std::unique_ptr<Batch> b;

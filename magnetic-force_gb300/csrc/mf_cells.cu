@@ -181,7 +181,9 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
                                                           const float4* __restrict__ mom, float4* __restrict__ corr,
                                                           const double* __restrict__ done_flags, int done_stride,
                                                           const int32_t* __restrict__ done_count, int done_total) {
-  constexpr int kT = 8;
+  // Targets held per pass: the force keeps each target's dipole too, so it
+  // holds fewer to stay clear of spills and keep more warps resident.
+  constexpr int kT = kForce ? 4 : 8;
   if (done_count && *done_count >= done_total) return;
   __shared__ float s_tbl[40];
   if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];

@@ -394,6 +394,88 @@ class Batch:
         check(load().mf_batch_reset_counters(self._h))
 
 
+class mf_server_config(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_double), ("max_active", ctypes.c_int32),
+                ("steps_per_request", ctypes.c_int32), ("iters_per_step", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("rel_tol", ctypes.c_double), ("dt", ctypes.c_double)]
+
+
+class mf_server_stats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("running", ctypes.c_int64), ("queued", ctypes.c_int64),
+                ("completed", ctypes.c_int64), ("ticks", ctypes.c_int64), ("rebatches", ctypes.c_int64),
+                ("bytes_in_use", ctypes.c_double), ("field_pairs", ctypes.c_double), ("force_pairs", ctypes.c_double),
+                ("busy_ms", ctypes.c_double)]
+
+
+class Server:
+    """Request queue with continuous batching (mf_server_* in mf.h)."""
+
+    def __init__(self, hbm_budget_bytes=120e9, max_active=64, steps_per_request=20, iters_per_step=4,
+                 rel_tol=1e-6, dt=1e-4, device=0):
+        lib = load()
+        i32, i64, vp, f64 = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_double
+        for name, res, args in (
+                ("mf_server_create", i32, [ctypes.POINTER(mf_server_config), ctypes.POINTER(vp)]),
+                ("mf_server_destroy", i32, [vp]),
+                ("mf_server_submit", i32, [vp, ctypes.POINTER(mf_scene_desc), ctypes.POINTER(i64)]),
+                ("mf_server_step", i32, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(f64)]),
+                ("mf_server_poll", i32, [vp, i64, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(f64)]),
+                ("mf_server_result", i32, [vp, i64, i32, vp]),
+                ("mf_server_get_stats", i32, [vp, ctypes.POINTER(mf_server_stats)])):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        cfg = mf_server_config(float(hbm_budget_bytes), int(max_active), int(steps_per_request), int(iters_per_step),
+                               int(device), float(rel_tol), float(dt))
+        h = ctypes.c_void_p()
+        check(lib.mf_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.sizes = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().mf_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, sc) -> int:
+        p = _f32(sc.pos)
+        d = mf_scene_desc()
+        d.n, d.pos = len(p), p.ctypes.data
+        d.h, d.volume, d.chi = float(sc.h), float(sc.volume), float(sc.chi)
+        for j in range(3):
+            d.H0[j] = float(sc.H0[j])
+        rid = ctypes.c_int64(0)
+        check(load().mf_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)))
+        self.sizes[rid.value] = len(p)
+        return rid.value
+
+    def step(self):
+        a, c, ms = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
+        check(load().mf_server_step(self._h, ctypes.byref(a), ctypes.byref(c), ctypes.byref(ms)))
+        return a.value, c.value, ms.value
+
+    def poll(self, rid):
+        st, steps, lat = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
+        check(load().mf_server_poll(self._h, int(rid), ctypes.byref(st), ctypes.byref(steps), ctypes.byref(lat)))
+        return st.value, steps.value, lat.value
+
+    def result(self, rid, quantity: str) -> np.ndarray:
+        out = np.empty((self.sizes[rid], 3), dtype=np.float32)
+        check(load().mf_server_result(self._h, int(rid), Q[quantity], out.ctypes.data))
+        return out
+
+    def stats(self) -> dict:
+        s = mf_server_stats()
+        check(load().mf_server_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in mf_server_stats._fields_}
+
+
 def probe_fp32_peak() -> float:
     """Measured dense FP32 FMA throughput of the current device, TFLOP/s."""
     v = ctypes.c_double(0)
