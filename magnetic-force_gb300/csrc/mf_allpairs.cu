@@ -266,6 +266,7 @@ mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>&
     d.n_tb = int32_t((s.nt + tbt - 1) / tbt);
     d.step_off = step;
     d.tb_off = tbo;
+    d.flag_index = s.flag_index >= 0 ? s.flag_index : int32_t(plan.host.size());
     fill_coefs(s, d);
     step += int64_t(d.n_tiles) * d.n_tb;
     tbo += d.n_tb;

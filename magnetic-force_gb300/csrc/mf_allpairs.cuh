@@ -38,6 +38,8 @@ struct SceneDesc {
   int64_t tb_off;        // first global target-block index of this scene
   int32_t n_tiles;       // ceil(ns / TILE)
   int32_t n_tb;          // ceil(nt / (TPB*TPT))
+  int32_t flag_index;    // this scene's row in the launch's done_flags
+  int32_t pad_;
   PairConsts<Real> pc;
   // Field epilogue: out = scale * value + coef_add * add4 + coef_add2 * add4b + cvec.
   // Force / tensor epilogues use scale only.
@@ -422,7 +424,8 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
   const int64_t k_end = step_start(T, G, b + 1);
   if (k_begin >= k_end) return;
   // A launch whose solves have all stopped does nothing.
-  if (a.done_flags && a.n_scenes == 1 && a.done_flags[0] != 0.0) return;
+  if (a.done_flags && a.n_scenes == 1 && a.done_flags[int64_t(a.scenes[0].flag_index) * a.done_stride] != 0.0)
+    return;
   if (a.done_count && *a.done_count >= a.done_total) return;
 
   // Stage s: TILE source positions, then TILE source dipoles (computed, not
@@ -495,7 +498,7 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
       k_fail = k;
       break;
     }
-    const bool skip_scene = a.done_flags && a.done_flags[int64_t(si) * a.done_stride] != 0.0;
+    const bool skip_scene = a.done_flags && a.done_flags[int64_t(sc.flag_index) * a.done_stride] != 0.0;
 
     // Sweep the tile.
     if (!skip_scene) {

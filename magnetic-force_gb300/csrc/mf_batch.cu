@@ -177,40 +177,55 @@ class Batch {
     MF_TRY(red_tickets_.reserve(size_t(n) * sizeof(int32_t), false, true));
     MF_TRY(done_count_.reserve(16, false, true));
 
-    // Launch plans (one scene table per kind of product).
-    std::vector<SceneSpec> resid, cgq, force;
-    for (const SI& si : sc_) {
+    // Launch plans, one scene table per kind of product and path: [0] the
+    // exact-branch kernels for scenes below kPacked*Min, [1] the packed
+    // kernels plus near-field correction for the larger ones.
+    std::vector<SceneSpec> resid[2], cgq[2], force[2];
+    std::vector<int32_t> skip_field, skip_force;
+    for (size_t k = 0; k < sc_.size(); ++k) {
+      const SI& si = sc_[k];
       SceneSpec b;
       b.t_off = si.off;
       b.nt = si.n;
       b.s_off = si.off;
       b.ns = si.n;
       b.h = si.h;
+      b.flag_index = int32_t(k);
+      const int pf = si.n >= kPackedFieldMin ? 1 : 0;
+      const int pg = si.n >= kPackedForceMin ? 1 : 0;
       const double c = si.V * si.chi / (1.0 + si.chi);
       SceneSpec r = b;  // r = c G b + Hext - b
       r.scale = c;
       r.coef_add = 1.0;
       r.coef_add2 = -1.0;
-      resid.push_back(r);
+      resid[pf].push_back(r);
       SceneSpec q = b;  // q = p - c G p
       q.scale = -c;
       q.coef_add = 1.0;
-      cgq.push_back(q);
-      force.push_back(b);
+      cgq[pf].push_back(q);
+      force[pg].push_back(b);
+      skip_field.push_back(pf ? 0 : 1);
+      skip_force.push_back(pg ? 0 : 1);
       pairs_ += double(si.n) * double(si.n);
     }
-    MF_TRY(build_plan<float>(Body::FieldF2, resid, plan_resid_));
-    MF_TRY(build_plan<float>(Body::FieldF2, cgq, plan_cgq_));
-    MF_TRY(build_plan<float>(Body::ForceF2, force, plan_force_));
-    for (const Plan<float>* p : {&plan_resid_, &plan_cgq_, &plan_force_}) {
-      size_t pd = 0, nc = 0;
-      plan_scratch_needs(*p, &pd, &nc);
-      MF_TRY(scr_.ensure(pd, nc));
+    for (int p = 0; p < 2; ++p) {
+      const Body fb = p ? Body::FieldF2 : Body::Field;
+      const Body gb = p ? Body::ForceF2 : Body::Force;
+      if (!resid[p].empty()) MF_TRY(build_plan<float>(fb, resid[p], plan_resid_[p]));
+      if (!cgq[p].empty()) MF_TRY(build_plan<float>(fb, cgq[p], plan_cgq_[p]));
+      if (!force[p].empty()) MF_TRY(build_plan<float>(gb, force[p], plan_force_[p]));
+      for (const Plan<float>* pl : {&plan_resid_[p], &plan_cgq_[p], &plan_force_[p]}) {
+        if (pl->n_scenes == 0) continue;
+        size_t pd = 0, nc = 0;
+        plan_scratch_needs(*pl, &pd, &nc);
+        MF_TRY(scr_.ensure(pd, nc));
+      }
     }
 
     std::vector<CellSceneSpec> cs;
     for (const SI& si : sc_) cs.push_back(CellSceneSpec{si.off, si.n, si.h});
     MF_TRY(cells_.build(pos4_.as<float4>(), cs, st_, /*margin_h=*/2.0));
+    MF_TRY(cells_.set_skips(skip_field, skip_force));
     to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
     MF_CUDA_TRY(cudaGetLastError());
     MF_CUDA_TRY(cudaStreamSynchronize(st_));
@@ -252,18 +267,27 @@ class Batch {
   }
 
   mf_status eval_force() {
-    to_pairs(mom4_.as<float4>(), mom2_.as<float4>(), n_alloc_, st_);
-    MF_TRY(cells_.force_correction(pos4_.as<float4>(), mom4_.as<float4>(), corr_.as<float4>(), st_));
     LaunchIO<float> io;
     io.tpos = pos4_.as<float4>();
     io.tmom = mom4_.as<float4>();
-    io.spos = pos2_.as<float4>();
-    io.smom = mom2_.as<float4>();
-    io.corr4 = corr_.as<float4>();
     float* F = fs_.as<float>();
     for (int k = 0; k < 3; ++k) io.out[k] = F + int64_t(k) * n_alloc_;
-    MF_TRY(run_plan<float>(plan_force_, io, scr_, st_));
-    ctr_.kernel_launches += 3;
+    if (plan_force_[0].n_scenes) {  // small scenes: exact branches, records as sources
+      LaunchIO<float> s = io;
+      s.spos = pos4_.as<float4>();
+      s.smom = mom4_.as<float4>();
+      MF_TRY(run_plan<float>(plan_force_[0], s, scr_, st_));
+      ctr_.kernel_launches += 1;
+    }
+    if (plan_force_[1].n_scenes) {  // large scenes: packed pairs + correction
+      to_pairs(mom4_.as<float4>(), mom2_.as<float4>(), n_alloc_, st_);
+      MF_TRY(cells_.force_correction(pos4_.as<float4>(), mom4_.as<float4>(), corr_.as<float4>(), st_));
+      io.spos = pos2_.as<float4>();
+      io.smom = mom2_.as<float4>();
+      io.corr4 = corr_.as<float4>();
+      MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
+      ctr_.kernel_launches += 3;
+    }
     ctr_.force_passes += 1;
     ctr_.force_pairs += pairs_;
     return MF_OK;
@@ -423,18 +447,12 @@ class Batch {
     float H0[3];
   };
 
-  mf_status field(const Plan<float>& plan, const float4* src_mom, float4* out4, const float4* add4,
+  mf_status field(const Plan<float>* plans, const float4* src_mom, float4* out4, const float4* add4,
                   const float4* add4b, bool skip_done) {
     const int n = scenes();
     const int32_t* dc = skip_done ? done_count_.as<int32_t>() : nullptr;
-    to_pairs(src_mom, mom2_.as<float4>(), n_alloc_, st_, dc, n);
-    MF_TRY(cells_.field_correction(pos4_.as<float4>(), src_mom, corr_.as<float4>(), st_,
-                                   skip_done ? scal_.as<double>() : nullptr, kScal, dc, n));
     LaunchIO<float> io;
     io.tpos = pos4_.as<float4>();
-    io.spos = pos2_.as<float4>();
-    io.smom = mom2_.as<float4>();
-    io.corr4 = corr_.as<float4>();
     io.out4 = out4;
     io.add4 = add4;
     io.add4b = add4b;
@@ -444,8 +462,23 @@ class Batch {
       io.done_count = dc;
       io.done_total = n;
     }
-    MF_TRY(run_plan<float>(plan, io, scr_, st_));
-    ctr_.kernel_launches += 3;
+    if (plans[0].n_scenes) {  // small scenes: exact branches, records as sources
+      LaunchIO<float> s = io;
+      s.spos = pos4_.as<float4>();
+      s.smom = src_mom;
+      MF_TRY(run_plan<float>(plans[0], s, scr_, st_));
+      ctr_.kernel_launches += 1;
+    }
+    if (plans[1].n_scenes) {  // large scenes: packed pairs + correction
+      to_pairs(src_mom, mom2_.as<float4>(), n_alloc_, st_, dc, n);
+      MF_TRY(cells_.field_correction(pos4_.as<float4>(), src_mom, corr_.as<float4>(), st_,
+                                     skip_done ? scal_.as<double>() : nullptr, kScal, dc, n));
+      io.spos = pos2_.as<float4>();
+      io.smom = mom2_.as<float4>();
+      io.corr4 = corr_.as<float4>();
+      MF_TRY(run_plan<float>(plans[1], io, scr_, st_));
+      ctr_.kernel_launches += 3;
+    }
     return MF_OK;
   }
 
@@ -473,7 +506,7 @@ class Batch {
   void* pinned_ = nullptr;
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
-  Plan<float> plan_resid_, plan_cgq_, plan_force_;
+  Plan<float> plan_resid_[2], plan_cgq_[2], plan_force_[2];  // [0] exact branches, [1] packed
   Scratch scr_;
   CellList cells_;
   mf_counters ctr_ = {};

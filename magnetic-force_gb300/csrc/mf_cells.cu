@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
                                                           const int32_t* __restrict__ start,
                                                           const float4* __restrict__ pos,
                                                           const float4* __restrict__ mom, float4* __restrict__ corr,
+                                                          const int32_t* __restrict__ skip_scene,
                                                           const double* __restrict__ done_flags, int done_stride,
                                                           const int32_t* __restrict__ done_count, int done_total) {
   // Targets held per pass: the force keeps each target's dipole too, so it
@@ -200,6 +201,7 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
       else hi = mid - 1;
     }
     if (done_flags && done_flags[int64_t(lo) * done_stride] != 0.0) continue;  // scene's solve stopped
+    if (skip_scene && skip_scene[lo]) continue;  // scene evaluated by the exact-branch kernels
     const CellGrid& g = grids[lo];
     const int64_t lc = c - g.cell_off;
     const int ix = int(lc % g.nx), iy = int((lc / g.nx) % g.ny), iz = int(lc / (int64_t(g.nx) * g.ny));
@@ -479,7 +481,7 @@ mf_status CellList::field_correction(const float4* pos4, const float4* mom4, flo
                                      int done_total) const {
   k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
-      done_flags, done_stride, done_count, done_total);
+      skip_field_.as<int32_t>(), done_flags, done_stride, done_count, done_total);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }
@@ -494,10 +496,28 @@ mf_status CellList::field_correction_at(const float4* tpos4, int64_t nt, const f
   return MF_OK;
 }
 
+mf_status CellList::set_skips(const std::vector<int32_t>& field, const std::vector<int32_t>& force) {
+  auto put = [&](const std::vector<int32_t>& v, DevBuf& b) -> mf_status {
+    bool any = false;
+    for (int32_t x : v) any = any || x != 0;
+    if (!any) {
+      b.release();
+      return MF_OK;
+    }
+    if (int(v.size()) != n_scenes_) return fail(MF_ERR_INVALID_ARG, "skip list size");
+    MF_TRY(b.reserve(v.size() * sizeof(int32_t)));
+    MF_CUDA_TRY(cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    return MF_OK;
+  };
+  MF_TRY(put(field, skip_field_));
+  MF_TRY(put(force, skip_force_));
+  return MF_OK;
+}
+
 mf_status CellList::force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
   k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
-      nullptr, 0, nullptr, 0);
+      skip_force_.as<int32_t>(), nullptr, 0, nullptr, 0);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

@@ -352,7 +352,7 @@ class Engine final : public EngineBase {
     if (!rext_zero_)
       for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
     io.naive_quirks = naive_ ? 1 : 0;
-    MF_TRY(prepare_packed(mom4(), true, io));
+    if (plan_force_.body == Body::ForceF2) MF_TRY(prepare_packed(mom4(), true, io));
     MF_TRY(run(plan_force_, io));
     ctr_.force_passes += 1;
     ctr_.force_pairs += plan_force_.pairs;
@@ -563,8 +563,8 @@ class Engine final : public EngineBase {
     s.coef_add = 1.0;
     s.coef_add2 = -1.0;
     // FP32 uses the packed two-source kernels; FP64 the exact-branch kernels.
-    const Body fb = kF32 ? Body::FieldF2 : Body::Field;
-    const Body gb = kF32 ? Body::ForceF2 : Body::Force;
+    const Body fb = (kF32 && np_ >= kPackedFieldMin) ? Body::FieldF2 : Body::Field;
+    const Body gb = (kF32 && np_ >= kPackedForceMin) ? Body::ForceF2 : Body::Force;
     MF_TRY(build_plan<Real>(fb, {s}, plan_resid_));
     // gradient g = c G(r) - r            (D_transpose, :1281-1284)
     // D(d) = c G(d) - d                  (D, :1275-1278)
@@ -709,7 +709,7 @@ class Engine final : public EngineBase {
     io.tpos = pos4();
     io.spos = pos4();
     io.smom = src_mom;
-    MF_TRY(prepare_packed(src_mom, false, io));
+    if (plan.body == Body::FieldF2) MF_TRY(prepare_packed(src_mom, false, io));
     io.out4 = out4;
     io.add4 = add4;
     io.add4b = add4b;

@@ -77,6 +77,14 @@ struct DevBuf {
 // array (mf_cells.cu) added in the epilogue.
 enum class Body { Field = 0, Force = 1, Tensor = 2, FieldF2 = 3, ForceF2 = 4 };
 
+// Scene sizes from which the packed path (clamped far form + near-field
+// correction) beats the exact-branch kernels.  Near pairs per particle are
+// fixed by the density (~270 inside 2h, ~2100 inside 4h at h = 2 spacings)
+// while far pairs grow with N, and a corrected near pair costs several far
+// pairs, so small scenes stay on the exact-branch kernels.
+constexpr int64_t kPackedFieldMin = 2048;
+constexpr int64_t kPackedForceMin = 12288;
+
 template <class Real, Body B>
 struct KCfg;
 // FP32: 256 threads x 2 targets, 256-source tiles, 3 stages (24 KB of smem).
@@ -122,6 +130,7 @@ struct SceneSpec {
   double coef_add = 0.0;   // field: coefficient of add4
   double coef_add2 = 0.0;  // field: coefficient of add4b
   double cvec[3] = {0.0, 0.0, 0.0};
+  int32_t flag_index = -1; // row in done_flags (default: the scene's position in the plan)
 };
 
 // A laid-out launch: device scene table plus its step-space totals.
@@ -232,6 +241,9 @@ class CellList {
                              const double* done_flags = nullptr, int done_stride = 0,
                              const int32_t* done_count = nullptr, int done_total = 0) const;
   mf_status force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const;
+  // Scenes (by build order) whose field / force use the exact-branch kernels
+  // and so need no correction.
+  mf_status set_skips(const std::vector<int32_t>& field, const std::vector<int32_t>& force);
   // Field correction at separate targets tpos4[0..nt) (single-scene lists).
   mf_status field_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
                                 float4* corr, cudaStream_t st) const;
@@ -241,6 +253,7 @@ class CellList {
 
  private:
   DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
+  DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
   std::vector<CellGrid> host_grids_;
   int64_t n_total_ = 0, n_cells_ = 0;
   int32_t n_scenes_ = 0;
