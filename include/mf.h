@@ -86,10 +86,20 @@ typedef enum mf_option {
   MF_OPT_SOLVER = 3,        /* mf_solver_kind */
   MF_OPT_REL_TOL = 4,       /* CG relative residual tolerance (default 1e-6 FP32, 1e-8 FP64) */
   MF_OPT_CG_MAX_ITER = 5,   /* CG iteration cap (default 500) */
-  MF_OPT_CRIT_SIZE = 6,     /* accepted for compatibility (crit_size, :647); unused */
+  MF_OPT_CRIT_SIZE = 6,     /* accepted for compatibility (crit_size, :647); the FMM's leaf
+                               size is MF_OPT_FMM_LEAF */
   MF_OPT_CHECK_INTERVAL = 7,/* CG: iterations launched between host convergence checks
                                (default 1 for N >= 16384, else 4) */
-  MF_OPT_KERNEL_TIMING = 8  /* 1: time every all-pairs launch with CUDA events (mf_get_kernel_stats) */
+  MF_OPT_KERNEL_TIMING = 8, /* 1: time every all-pairs launch (and every FMM product as a
+                               whole) with CUDA events (mf_get_kernel_stats) */
+  MF_OPT_FMM = 9,           /* field and force products of FP32 handles: 0 auto (the FMM
+                               above 65,536 particles, all-pairs below), 1 always the FMM,
+                               2 always all-pairs.  FP64 handles are all-pairs. */
+  MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
+                               (terms of degree n < P): 4..8, default 6 (magnetic_force.cu:661) */
+  MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture, default 0.5 (FMMOptions.hpp:118) */
+  MF_OPT_FMM_LEAF = 12      /* FMM leaf level: the deepest whose boxes hold at least this many
+                               particles on average (default 64) */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -198,6 +208,34 @@ typedef struct mf_kernel_stats {
   double pairs;
 } mf_kernel_stats;
 mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out);
+
+/* Shape and work of the handle's FMM (uniform octree over the current
+ * positions; built on the first product after the positions change).
+ * Replaces the tree and interaction-list state of the reference's
+ * fmmtl::kernel_matrix plans (KernelMatrixPlan.hpp:75-113). */
+typedef struct mf_fmm_stats {
+  int32_t active;            /* 1 if the handle's products use the FMM */
+  int32_t levels;            /* box grid levels, root included */
+  int32_t leaf_level;
+  int32_t degree;            /* expansion degree (order - 1) */
+  int64_t leaf_boxes;        /* boxes of the leaf grid */
+  int64_t occupied_leaves;
+  int32_t max_leaf;          /* particles in the fullest leaf box */
+  int32_t near_rows;         /* rows of near leaf boxes per target box */
+  double p2p_pairs;          /* near-field pairs executed per product */
+  double m2l_per_product;    /* multipole-to-local translations per product */
+  int32_t launches_per_product;
+  int32_t pad;
+  int64_t field_products;    /* FMM products since the last mf_reset_counters */
+  int64_t force_products;
+} mf_fmm_stats;
+mf_status mf_get_fmm_stats(mf_solver* s, mf_fmm_stats* out);
+
+/* out = G(moments): B/mu0_i = sum_j K_B(x_i - x_j; h) m_j over the handle's
+ * particles, through the path its products take (FMM or all-pairs).  moments
+ * and out are float [n][3] (AOS) or [3][n] (SOA) in host or device memory.
+ * Replaces cuda_magnet_cgOptimizer::G (magnetic_force.cu:1196-1271). */
+mf_status mf_apply_field(mf_solver* s, const float* moments, int32_t layout, int32_t where, float* out);
 
 /* Measured dense FP32 FMA throughput of the current device in TFLOP/s
  * (independent FFMA chains on every SM, timed with CUDA events): the

@@ -402,6 +402,8 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
   MF_CUDA_TRY(cudaStreamSynchronize(st));
 
   host_grids_.assign(size_t(ns), CellGrid{});
+  host_bbox_.assign(6 * size_t(ns), 0.0);
+  for (size_t k = 0; k < hb.size(); ++k) host_bbox_[k] = double(ord2f(hb[k]));
   int64_t cells = 0, prefix = 0;
   for (int s = 0; s < ns; ++s) {
     CellGrid& g = host_grids_[size_t(s)];

@@ -172,8 +172,13 @@ struct EngineBase {
   virtual cudaStream_t stream() const = 0;
   virtual mf_status kernel_stats(int kind, mf_kernel_stats* out) = 0;
   virtual void reset_stats() = 0;
+  virtual mf_status fmm_stats(mf_fmm_stats* out) = 0;
+  virtual mf_status apply_field(const float* m, int layout, int where, float* out) = 0;
   int device = 0;
 };
+
+// Particle count above which FP32 handles take the FMM by default.
+constexpr int64_t kFmmAutoMin = 65536;
 
 template <class Real>
 class Engine final : public EngineBase {
@@ -343,6 +348,13 @@ class Engine final : public EngineBase {
   // ---- evaluate_fitted_near_foece ----------------------------------------------
   mf_status eval_force() override {
     MF_TRY(publish_b());  // M = c b (magnetic_force.cu:899, :915)
+    if (use_fmm()) {
+      MF_TRY(fmm_product(true, plan_force_, mom4(), nullptr, nullptr, nullptr, nullptr));
+      ctr_.force_passes += 1;
+      ctr_.force_pairs += plan_force_.pairs;
+      MF_TRY(scr_.check(st_));
+      return MF_OK;
+    }
     LaunchIO<Real> io;
     io.tpos = pos4();
     io.tmom = mom4();
@@ -448,6 +460,25 @@ class Engine final : public EngineBase {
         check_interval_set_ = true;
         return MF_OK;
       case MF_OPT_KERNEL_TIMING: timing_ = v != 0.0; return MF_OK;
+      case MF_OPT_FMM:
+        if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "fmm mode must be 0, 1 or 2");
+        fmm_mode_ = int(v);
+        return MF_OK;
+      case MF_OPT_FMM_ORDER:
+        if (v < 4 || v > 8 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..8");
+        fmm_cfg_.order = int(v);
+        fmm_dirty_ = true;
+        return MF_OK;
+      case MF_OPT_FMM_THETA:
+        if (!(v > 0.0 && v <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm theta must be in (0, 1]");
+        fmm_cfg_.theta = v;
+        fmm_dirty_ = true;
+        return MF_OK;
+      case MF_OPT_FMM_LEAF:
+        if (v < 1 || v > 4096) return fail(MF_ERR_INVALID_ARG, "fmm leaf size must be 1..4096");
+        fmm_cfg_.leaf_min = int(v);
+        fmm_dirty_ = true;
+        return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -464,6 +495,10 @@ class Engine final : public EngineBase {
       case MF_OPT_CRIT_SIZE: *v = crit_size_; return MF_OK;
       case MF_OPT_CHECK_INTERVAL: *v = interval(); return MF_OK;
       case MF_OPT_KERNEL_TIMING: *v = timing_ ? 1.0 : 0.0; return MF_OK;
+      case MF_OPT_FMM: *v = fmm_mode_; return MF_OK;
+      case MF_OPT_FMM_ORDER: *v = fmm_cfg_.order; return MF_OK;
+      case MF_OPT_FMM_THETA: *v = fmm_cfg_.theta; return MF_OK;
+      case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -486,7 +521,13 @@ class Engine final : public EngineBase {
   DevBuf pos2_, mom2_, corr_;
   CellList cells_;
   bool cells_dirty_ = true;
-  Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_;
+  Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_, plan_apply_;
+  // FMM state (FP32 handles): the octree of the current positions.
+  Fmm fmm_;
+  FmmConfig fmm_cfg_;
+  bool fmm_dirty_ = true;
+  int fmm_mode_ = 0;
+  int64_t fmm_field_products_ = 0, fmm_force_products_ = 0;
   bool plans_ready_ = false;
   bool rext_zero_ = true;
 
@@ -580,6 +621,7 @@ class Engine final : public EngineBase {
     MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_));
     s = base;
     MF_TRY(build_plan<Real>(gb, {s}, plan_force_));
+    MF_TRY(build_plan<Real>(fb, {base}, plan_apply_));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
     return MF_OK;
@@ -655,6 +697,64 @@ class Engine final : public EngineBase {
     }
     timed_.clear();
     for (auto& a : agg_) a = mf_kernel_stats{};
+    fmm_field_products_ = fmm_force_products_ = 0;
+  }
+
+  mf_status fmm_stats(mf_fmm_stats* out) override {
+    if (!out) return fail(MF_ERR_INVALID_ARG, "NULL");
+    *out = mf_fmm_stats{};
+    out->active = use_fmm() ? 1 : 0;
+    if (use_fmm()) MF_TRY(ensure_fmm());
+    const FmmStats& f = fmm_.stats();
+    out->levels = f.levels;
+    out->leaf_level = f.leaf_level;
+    out->degree = f.degree;
+    out->leaf_boxes = f.leaf_boxes;
+    out->occupied_leaves = f.occupied_leaves;
+    out->max_leaf = f.max_leaf;
+    out->near_rows = f.near_rows;
+    out->p2p_pairs = f.p2p_pairs;
+    out->m2l_per_product = f.m2l_per_product;
+    out->launches_per_product = fmm_.launches_per_product();
+    out->field_products = fmm_field_products_;
+    out->force_products = fmm_force_products_;
+    return MF_OK;
+  }
+
+  // G(m) at the handle's particles (plan_apply_: scale 1, no addends).
+  mf_status apply_field(const float* m, int layout, int where, float* out) override {
+    if (!m || !out) return fail(MF_ERR_INVALID_ARG, "NULL argument");
+    if (layout != MF_LAYOUT_AOS && layout != MF_LAYOUT_SOA) return fail(MF_ERR_INVALID_ARG, "bad layout");
+    if (where != MF_HOST && where != MF_DEVICE) return fail(MF_ERR_INVALID_ARG, "bad memory kind");
+    const int64_t n = np_;
+    const float* src = m;
+    MF_TRY(staging_.reserve(size_t(3 * n) * sizeof(double)));
+    MF_TRY(staging2_.reserve(size_t(3 * n) * sizeof(double)));
+    if (where == MF_HOST) {
+      MF_CUDA_TRY(cudaMemcpyAsync(staging_.ptr, m, size_t(3 * n) * sizeof(float), cudaMemcpyHostToDevice, st_));
+      src = staging_.template as<float>();
+    }
+    MF_CUDA_TRY(cudaMemsetAsync(bad_.ptr, 0, sizeof(int32_t), st_));
+    k_pack_positions<Real, R4><<<grid_1d(n, sms_), 256, 0, st_>>>(src, layout, n, v4(V_GOLD), nullptr, nullptr,
+                                                                    nullptr, bad_.template as<int32_t>());
+    MF_CUDA_TRY(cudaGetLastError());
+    ++ctr_.kernel_launches;
+    MF_TRY(field(plan_apply_, v4(V_GOLD), v4(V_DD), nullptr, nullptr));
+    float* soa = staging2_.template as<float>();
+    for (int k = 0; k < 3; ++k) MF_TRY(gather_r4f(v4(V_DD), k, soa + size_t(k) * size_t(n), n));
+    const float* res = soa;
+    if (layout == MF_LAYOUT_AOS) {
+      MF_TRY(soa_to_aos<float>(soa, staging_.template as<float>(), n));
+      res = staging_.template as<float>();
+    }
+    MF_CUDA_TRY(cudaMemcpyAsync(out, res, size_t(3 * n) * sizeof(float),
+                                where == MF_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st_));
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
+    int32_t bad = 0;
+    MF_CUDA_TRY(cudaMemcpy(&bad, bad_.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (bad) return fail(MF_ERR_INVALID_ARG, "non-finite moment");
+    MF_TRY(scr_.check(st_));
+    return MF_OK;
   }
 
  private:
@@ -700,11 +800,78 @@ class Engine final : public EngineBase {
       to_pairs(pos4(), pos2_.template as<float4>(), np_, st_);
       ++ctr_.kernel_launches;
       cells_dirty_ = true;
+      fmm_dirty_ = true;
     }
+  }
+
+  bool use_fmm() const {
+    if constexpr (!kF32) return false;
+    return fmm_mode_ == 1 || (fmm_mode_ == 0 && np_ > kFmmAutoMin);
+  }
+  mf_status ensure_fmm() {
+    if constexpr (kF32) {
+      MF_TRY(ensure_cells());
+      if (fmm_dirty_) {
+        MF_TRY(fmm_.build(pos4(), np_, h_, cells_.bbox(0), fmm_cfg_, st_));
+        ctr_.kernel_launches += 8;
+        fmm_dirty_ = false;
+      }
+      MF_TRY(scr_.ensure(0, 0));
+    }
+    return MF_OK;
+  }
+  // One FMM product with the epilogue of `plan` (field: out4 / add4 / add4b;
+  // force: the published force arrays), timed as a whole when timing is on.
+  mf_status fmm_product(bool force, const Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4,
+                        const R4* add4b, const double* done) {
+    if constexpr (kF32) {
+      MF_TRY(ensure_fmm());
+      float4* corr = corr_.template as<float4>();
+      if (force) MF_TRY(cells_.force_correction(pos4(), src_mom, corr, st_));
+      else MF_TRY(cells_.field_correction(pos4(), src_mom, corr, st_, done, 0));
+      AllPairsArgs<float> a{};
+      a.tpos = pos4();
+      a.corr4 = corr;
+      a.err = scr_.err.template as<int32_t>();
+      if (force) {
+        a.tmom = src_mom;
+        for (int k = 0; k < 3; ++k) a.out[k] = pubr(MF_Q_FORCE, k);
+        if (!rext_zero_)
+          for (int k = 0; k < 9; ++k) a.rext[k] = rext(k);
+        a.naive_quirks = naive_ ? 1 : 0;
+      } else {
+        a.out4 = out4;
+        a.add4 = add4;
+        a.add4b = add4b;
+      }
+      TimedLaunch t;
+      if (timing_) {
+        t.body = force ? 1 : 0;
+        t.pairs = plan.pairs;
+        MF_CUDA_TRY(cudaEventCreate(&t.start));
+        MF_CUDA_TRY(cudaEventCreate(&t.stop));
+        MF_CUDA_TRY(cudaEventRecord(t.start, st_));
+      }
+      MF_TRY(fmm_.product(force, pos4(), src_mom, a, plan.host[0], st_, done));
+      if (timing_) {
+        MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
+        timed_.push_back(t);
+      }
+      ctr_.kernel_launches += fmm_.launches_per_product() + 1;
+      if (force) ++fmm_force_products_;
+      else ++fmm_field_products_;
+    }
+    return MF_OK;
   }
 
   mf_status field(Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4, const R4* add4b,
                   const double* done = nullptr) {
+    if (use_fmm()) {
+      MF_TRY(fmm_product(false, plan, src_mom, out4, add4, add4b, done));
+      ctr_.field_products += 1;
+      ctr_.field_pairs += plan.pairs;  // effective pairs (N^2), the FMM convention
+      return MF_OK;
+    }
     LaunchIO<Real> io;
     io.tpos = pos4();
     io.spos = pos4();
@@ -1204,6 +1371,14 @@ mf_status mf_reset_counters(mf_solver* s) {
 
 mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out) {
   return guarded(s, [&](EngineBase& e) { return e.kernel_stats(kind, out); });
+}
+
+mf_status mf_get_fmm_stats(mf_solver* s, mf_fmm_stats* out) {
+  return guarded(s, [&](EngineBase& e) { return e.fmm_stats(out); });
+}
+
+mf_status mf_apply_field(mf_solver* s, const float* moments, int32_t layout, int32_t where, float* out) {
+  return guarded(s, [&](EngineBase& e) { return e.apply_field(moments, layout, where, out); });
 }
 
 mf_status mf_probe_fp32_peak(double* tflops) {

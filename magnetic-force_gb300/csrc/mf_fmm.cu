@@ -1,0 +1,1120 @@
+// mf_fmm.cu -- uniform-octree fast multipole method for the field and force
+// products of large scenes.
+//
+// The reference evaluates large products with FMMTL (KernelMatrix.hpp:26-164,
+// DualTraversal.hpp:80-125, BatchNear.hpp:57-75): an adaptive octree,
+// spherical expansions in FP64 on the host CPU and a GPU near field.  Here the
+// whole product stays on the device:
+//   * one uniform box grid per level (level 0 is one box around the scene);
+//     the leaf level is the deepest with >= leaf_min particles per box on
+//     average, so a leaf box fills a 128-thread block of the near-field kernel;
+//   * particles binned into leaf boxes in row-major order (x fastest), each
+//     box's list in increasing particle index and padded to an even length,
+//     so every run of x-adjacent boxes is one contiguous, pair-aligned range of
+//     sources for the packed two-source pair body;
+//   * Cartesian Taylor expansions of the dipole potential
+//       phi(x) = 1/(4 pi) sum_j m_j . (x - y_j) / |x - y_j|^3
+//     (multipoles and locals of degree 1..Q, Q = P - 1, M2L truncated at
+//     |alpha| + |beta| <= Q + 1), each level's coefficients scaled by its box
+//     edge so M2M, M2L and L2L do not depend on the level;
+//   * box pairs accepted by the criterion of FMMOptions.hpp:56-78 (theta on
+//     the box radii, with the separation test that the reference enables) are
+//     far only if their gap also exceeds the kernel's near radius 4h, so every
+//     far pair is in the pure-dipole regime of Dipole_B.kern:46-104 /
+//     Dipole_hessian.kern:155-207 and the truncation is the only approximation;
+//   * near leaf boxes (not accepted at the leaf level) are summed with the
+//     packed clamped pair body of the all-pairs kernel, and the cell-list
+//     correction (mf_cells.cu) turns the clamped pairs inside the near radius
+//     into the reference's SPH / fitted-curve kernel.
+// Every launch reads a solver stop flag and does nothing once it is set.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "mf_internal.h"
+
+namespace mfgb {
+namespace {
+
+constexpr int kMaxDegree = 7;  // P = 8
+constexpr int kMaxLevel = 10;
+
+// Multi-indices in graded order: degree n, then s = y + z, then z.
+__host__ __device__ constexpr int ncoef(int q) { return q < 0 ? 0 : (q + 1) * (q + 2) * (q + 3) / 6; }
+__host__ __device__ constexpr int gidx(int x, int y, int z) {
+  return ncoef(x + y + z - 1) + (y + z) * (y + z + 1) / 2 + z;
+}
+
+// Multi-index table up to degree kMaxDegree + 1.
+__constant__ char4 c_mi[ncoef(kMaxDegree + 1)];
+// 1-D translation factors: c_shift[c][j] = ((c - 1/2) / 2)^j / j!, the child
+// centre offset in parent box units raised to j over j!.
+__constant__ float c_shift[2][kMaxDegree + 2];
+
+// ---------------------------------------------------------------------------
+// Binning
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t leaf_of(const FmmLevel& lv, float4 p) {
+  const float inv = 1.f / lv.side;
+  const int ix = min(max(int(floorf((p.x - lv.ox) * inv)), 0), lv.nx - 1);
+  const int iy = min(max(int(floorf((p.y - lv.oy) * inv)), 0), lv.ny - 1);
+  const int iz = min(max(int(floorf((p.z - lv.oz) * inv)), 0), lv.nz - 1);
+  return (int64_t(iz) * lv.ny + iy) * lv.nx + ix;
+}
+
+__global__ void k_fmm_count(const float4* __restrict__ pos, int64_t n, FmmLevel lv, int32_t* __restrict__ cell_of,
+                            int32_t* __restrict__ cnt) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = leaf_of(lv, pos[i]);
+    cell_of[i] = int32_t(c);
+    atomicAdd(&cnt[c], 1);
+  }
+}
+
+// Exclusive scan of the even-padded counts into start[0..n], one CTA.
+__global__ void __launch_bounds__(1024) k_fmm_scan(const int32_t* __restrict__ cnt, int64_t n,
+                                                   int32_t* __restrict__ start) {
+  __shared__ int32_t sh[1024];
+  const int t = threadIdx.x;
+  const int64_t chunk = (n + 1023) / 1024;
+  const int64_t b = t * chunk, e = min(n, b + chunk);
+  int32_t s = 0;
+  for (int64_t i = b; i < e; ++i) s += cnt[i] + (cnt[i] & 1);
+  sh[t] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int32_t v = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += v;
+    __syncthreads();
+  }
+  int32_t run = sh[t] - s;
+  for (int64_t i = b; i < e; ++i) {
+    start[i] = run;
+    run += cnt[i] + (cnt[i] & 1);
+  }
+  if (t == 1023) start[n] = sh[1023];
+}
+
+__global__ void k_fmm_scatter(const int32_t* __restrict__ cell_of, int64_t n, int32_t* __restrict__ cursor,
+                              int32_t* __restrict__ tmp) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    tmp[atomicAdd(&cursor[cell_of[i]], 1)] = int32_t(i);
+}
+
+// Each box's list in increasing particle index (one warp per box ranks its
+// entries), then -1 in the padding slot of an odd box.
+__global__ void k_fmm_sort(const int32_t* __restrict__ start, const int32_t* __restrict__ cnt, int64_t ncell,
+                           const int32_t* __restrict__ tmp, int32_t* __restrict__ perm) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); c < ncell; c += warps) {
+    const int32_t b = start[c], m = cnt[c];
+    for (int32_t k = lane; k < m; k += 32) {
+      const int32_t v = tmp[b + k];
+      int32_t rank = 0;
+      for (int32_t l = 0; l < m; ++l) rank += tmp[b + l] < v;
+      perm[b + rank] = v;
+    }
+    if (lane == 0 && (m & 1)) perm[b + m] = -1;
+  }
+}
+
+// Occupancy of a level from its children's.
+__global__ void k_fmm_occ_up(FmmLevel lc, FmmLevel lp, int32_t* __restrict__ occ) {
+  for (int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; b < lp.nbox; b += int64_t(gridDim.x) * blockDim.x) {
+    const int px = int(b % lp.nx), py = int((b / lp.nx) % lp.ny), pz = int(b / (int64_t(lp.nx) * lp.ny));
+    int32_t s = 0;
+    for (int ch = 0; ch < 8; ++ch) {
+      const int x = 2 * px + (ch & 1), y = 2 * py + ((ch >> 1) & 1), z = 2 * pz + (ch >> 2);
+      if (x < lc.nx && y < lc.ny && z < lc.nz) s += occ[lc.box_off + (int64_t(z) * lc.ny + y) * lc.nx + x];
+    }
+    occ[lp.box_off + b] = s;
+  }
+}
+
+// Sorted records in pair layout: slots 2p, 2p+1 as (x_a, x_b, y_a, y_b),
+// (z_a, z_b, 0, 0).  A padding slot (always the odd one) repeats its
+// partner's position (pos) or holds a zero dipole (moments).
+__global__ void k_fmm_gather_pairs(const int32_t* __restrict__ perm, const float4* __restrict__ src, int64_t n_pairs,
+                                   float4* __restrict__ dst, int is_pos, const double* __restrict__ done) {
+  if (done && *done != 0.0) return;
+  for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n_pairs;
+       p += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t ia = perm[2 * p], ib = perm[2 * p + 1];
+    const float4 A = src[ia];
+    const float4 B = ib >= 0 ? src[ib] : (is_pos ? A : make_float4(0.f, 0.f, 0.f, 0.f));
+    dst[2 * p] = make_float4(A.x, B.x, A.y, B.y);
+    dst[2 * p + 1] = make_float4(A.z, B.z, 0.f, 0.f);
+  }
+}
+
+// Executed near-field pairs (real targets x real sources) and the largest leaf.
+__global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, const int4* __restrict__ rows,
+                                int n_rows, unsigned long long* __restrict__ out) {
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < lv.nbox; c += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t n = cnt[c];
+    if (n == 0) continue;
+    const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
+    unsigned long long s = 0;
+    for (int r = 0; r < n_rows; ++r) {
+      const int4 rw = rows[r];
+      const int cy = iy + rw.y, cz = iz + rw.z;
+      if (cy < 0 || cy >= lv.ny || cz < 0 || cz >= lv.nz) continue;
+      const int cx0 = max(ix - rw.x, 0), cx1 = min(ix + rw.x, lv.nx - 1);
+      const int64_t rb = (int64_t(cz) * lv.ny + cy) * lv.nx;
+      for (int x = cx0; x <= cx1; ++x) s += unsigned(cnt[rb + x]);
+    }
+    atomicAdd(&out[0], s * unsigned(n));
+    atomicMax(&out[1], (unsigned long long)n);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Upward pass
+// ---------------------------------------------------------------------------
+// Leaf multipoles, one CTA per box, one thread per coefficient alpha:
+//   M_alpha = (-1)^|alpha| sum_j sum_k m_jk u_j^(alpha - e_k) / (alpha - e_k)!,
+// u_j = (y_j - centre) / edge.
+template <int Q>
+__global__ void __launch_bounds__(128) k_fmm_p2m(FmmLevel lv, const int32_t* __restrict__ start,
+                                                 const int32_t* __restrict__ cnt, const int32_t* __restrict__ perm,
+                                                 const float4* __restrict__ pos4, const float4* __restrict__ mom4,
+                                                 float* __restrict__ M, const double* __restrict__ done) {
+  constexpr int NC = ncoef(Q) - 1;
+  constexpr int W = 3 * Q + 3;  // powers u^i/i! (i < Q) per axis, then the dipole
+  if (done && *done != 0.0) return;
+  __shared__ float s_p[128][W + 1];
+  const int tid = threadIdx.x;
+  const bool act = tid < NC;
+  int ax = 0, ay = 0, az = 0;
+  if (act) {
+    const char4 e = c_mi[tid + 1];
+    ax = e.x;
+    ay = e.y;
+    az = e.z;
+  }
+  const float sign = ((ax + ay + az) & 1) ? -1.f : 1.f;
+  const float inv_s = 1.f / lv.side;
+  for (int64_t c = blockIdx.x; c < lv.nbox; c += gridDim.x) {
+    const int32_t n = cnt[c];
+    float acc = 0.f;
+    if (n > 0) {
+      const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
+      const float cx = lv.ox + (float(ix) + 0.5f) * lv.side;
+      const float cy = lv.oy + (float(iy) + 0.5f) * lv.side;
+      const float cz = lv.oz + (float(iz) + 0.5f) * lv.side;
+      const int32_t b = start[c];
+      for (int j0 = 0; j0 < n; j0 += 128) {
+        const int nj = min(128, n - j0);
+        __syncthreads();
+        if (tid < nj) {
+          const int32_t i = perm[b + j0 + tid];
+          const float4 p = pos4[i], m = mom4[i];
+          const float u[3] = {(p.x - cx) * inv_s, (p.y - cy) * inv_s, (p.z - cz) * inv_s};
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            float v = 1.f;
+            s_p[tid][a * Q] = 1.f;
+#pragma unroll
+            for (int k = 1; k < Q; ++k) {
+              v = v * u[a] * (1.f / float(k));
+              s_p[tid][a * Q + k] = v;
+            }
+          }
+          s_p[tid][3 * Q] = m.x;
+          s_p[tid][3 * Q + 1] = m.y;
+          s_p[tid][3 * Q + 2] = m.z;
+        }
+        __syncthreads();
+        if (act) {
+          for (int j = 0; j < nj; ++j) {
+            const float* q = s_p[j];
+            float t = 0.f;
+            if (ax > 0) t += q[3 * Q] * q[ax - 1] * q[Q + ay] * q[2 * Q + az];
+            if (ay > 0) t += q[3 * Q + 1] * q[ax] * q[Q + ay - 1] * q[2 * Q + az];
+            if (az > 0) t += q[3 * Q + 2] * q[ax] * q[Q + ay] * q[2 * Q + az - 1];
+            acc += t;
+          }
+        }
+      }
+    }
+    if (act) M[int64_t(tid) * lv.nbox + c] = sign * acc;
+  }
+}
+
+// Children -> parent:  M^p_alpha = sum_c sum_{gamma <= alpha}
+//   2^(1-|gamma|) M^c_gamma (-1)^|delta| v_c^delta / delta!,  delta = alpha - gamma,
+// v_c the child centre offset in parent box units.  One thread per (alpha, box).
+template <int Q>
+__global__ void k_fmm_m2m(FmmLevel lc, FmmLevel lp, const int32_t* __restrict__ occ, float* __restrict__ M,
+                          const double* __restrict__ done) {
+  constexpr int NC = ncoef(Q) - 1;
+  if (done && *done != 0.0) return;
+  const float* Mc = M + lc.box_off * NC;
+  float* Mp = M + lp.box_off * NC;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < int64_t(NC) * lp.nbox;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t / lp.nbox);
+    const int64_t b = t % lp.nbox;
+    float acc = 0.f;
+    if (occ[lp.box_off + b] > 0) {
+      const char4 e = c_mi[k + 1];
+      const int px = int(b % lp.nx), py = int((b / lp.nx) % lp.ny), pz = int(b / (int64_t(lp.nx) * lp.ny));
+      for (int ch = 0; ch < 8; ++ch) {
+        const int cx = ch & 1, cy = (ch >> 1) & 1, cz = ch >> 2;
+        const int x = 2 * px + cx, y = 2 * py + cy, z = 2 * pz + cz;
+        if (x >= lc.nx || y >= lc.ny || z >= lc.nz) continue;
+        const int64_t cb = (int64_t(z) * lc.ny + y) * lc.nx + x;
+        if (occ[lc.box_off + cb] == 0) continue;
+        for (int gx = 0; gx <= e.x; ++gx)
+          for (int gy = 0; gy <= e.y; ++gy)
+            for (int gz = 0; gz <= e.z; ++gz) {
+              const int g = gx + gy + gz;
+              if (g == 0) continue;
+              const int dx = e.x - gx, dy = e.y - gy, dz = e.z - gz;
+              // (-1)^|delta| v^delta / delta! = prod over axes of ((1/2 - c) / 2)^d / d!
+              const float w = c_shift[1 - cx][dx] * c_shift[1 - cy][dy] * c_shift[1 - cz][dz];
+              acc += Mc[int64_t(gidx(gx, gy, gz) - 1) * lc.nbox + cb] * w * ldexpf(1.f, 1 - g);
+            }
+      }
+    }
+    Mp[int64_t(k) * lp.nbox + b] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// M2L:  L_beta += sum_alpha M_alpha D_(alpha + beta)(d),  |alpha| + |beta| <= Q + 1,
+// D_gamma(d) = d^gamma (1/|d|) at the box-centre offset d in box units.  The
+// sum is an unrolled program over compile-time (gamma, alpha, beta) triples,
+// gamma-major so each D value is loaded once; beta degrees BLO..BHI per
+// variant (two variants split the largest degrees so the multipole and the
+// accumulators both stay in registers).
+// ---------------------------------------------------------------------------
+template <int Q, int BLO, int BHI>
+struct M2LPlan {
+  static constexpr int AMAX = (Q < Q + 1 - BLO) ? Q : Q + 1 - BLO;
+  static constexpr int NA = ncoef(AMAX) - 1;
+  static constexpr int BOFF = ncoef(BLO - 1);
+  static constexpr int NB = ncoef(BHI) - ncoef(BLO - 1);
+  struct Ent {
+    int16_t g, a, b, first;
+  };
+  static constexpr int count() {
+    int k = 0;
+    for (int g = BLO + 1; g <= Q + 1; ++g)
+      for (int s = 0; s <= g; ++s)
+        for (int gz = 0; gz <= s; ++gz) {
+          const int gy = s - gz, gx = g - s;
+          for (int ax = 0; ax <= gx; ++ax)
+            for (int ay = 0; ay <= gy; ++ay)
+              for (int az = 0; az <= gz; ++az) {
+                const int a = ax + ay + az, b = g - a;
+                if (a >= 1 && a <= AMAX && b >= BLO && b <= BHI) ++k;
+              }
+        }
+    return k;
+  }
+  static constexpr int K = count();
+  struct Tab {
+    Ent e[K];
+  };
+  static constexpr Tab make() {
+    Tab t{};
+    int k = 0;
+    for (int g = BLO + 1; g <= Q + 1; ++g)
+      for (int s = 0; s <= g; ++s)
+        for (int gz = 0; gz <= s; ++gz) {
+          const int gy = s - gz, gx = g - s;
+          bool first = true;
+          for (int ax = 0; ax <= gx; ++ax)
+            for (int ay = 0; ay <= gy; ++ay)
+              for (int az = 0; az <= gz; ++az) {
+                const int a = ax + ay + az, b = g - a;
+                if (a >= 1 && a <= AMAX && b >= BLO && b <= BHI) {
+                  t.e[k].g = int16_t(gidx(gx, gy, gz));
+                  t.e[k].a = int16_t(gidx(ax, ay, az) - 1);
+                  t.e[k].b = int16_t(gidx(gx - ax, gy - ay, gz - az) - BOFF);
+                  t.e[k].first = int16_t(first ? 1 : 0);
+                  first = false;
+                  ++k;
+                }
+              }
+        }
+    return t;
+  }
+  static constexpr Tab tab = make();
+  template <int I>
+  struct At {
+    static constexpr int g = tab.e[I].g, a = tab.e[I].a, b = tab.e[I].b, first = tab.e[I].first;
+  };
+};
+
+template <class Pl, int I>
+__device__ __forceinline__ void m2l_step(float* acc, const float* M, const float* __restrict__ dt, float& dg) {
+  using E = typename Pl::template At<I>;
+  if constexpr (E::first != 0) dg = __ldg(dt + E::g);
+  acc[E::b] = fmaf(M[E::a], dg, acc[E::b]);
+}
+
+template <class Pl, int... Is>
+__device__ __forceinline__ void m2l_apply(float* acc, const float* M, const float* __restrict__ dt,
+                                          std::integer_sequence<int, Is...>) {
+  float dg = 0.f;
+  (m2l_step<Pl, Is>(acc, M, dt, dg), ...);
+}
+
+struct M2LArgs {
+  FmmLevel lv;
+  const int32_t* occ;
+  const float* M;     // this level's multipoles (NC rows of nbox)
+  float* Lp;          // [chunks][NC][nbox] partial locals
+  const int4* list;   // (dx, dy, dz, row of dtab)
+  const float* dtab;  // [rows][ncoef(Q + 1)]
+  int64_t list_off[8];
+  int32_t list_cnt[8];
+  int32_t chunks;
+  int32_t hx, hy, hz;  // half-grid extents (boxes per class along each axis)
+  int64_t per_class;   // hx * hy * hz rounded up to a multiple of 32
+  const double* done;
+};
+
+// One thread per (list chunk, target box); the warps of a block share the
+// chunk and the target parity class, so they walk the same offsets.
+template <int Q, int BLO, int BHI>
+__global__ void __launch_bounds__(128) k_fmm_m2l(const M2LArgs p) {
+  using Pl = M2LPlan<Q, BLO, BHI>;
+  constexpr int NC = ncoef(Q) - 1;
+  constexpr int NG = ncoef(Q + 1);
+  if (p.done && *p.done != 0.0) return;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t per = p.per_class;
+  const int ch = int(t / (8 * per));
+  if (ch >= p.chunks) return;
+  const int cls = int((t / per) % 8);
+  const int64_t r = t % per;
+  const int hi = int(r % p.hx), hj = int((r / p.hx) % p.hy);
+  const int64_t hk = r / (int64_t(p.hx) * p.hy);
+  if (hk >= p.hz) return;
+  const FmmLevel& lv = p.lv;
+  const int tx = 2 * hi + (cls & 1), ty = 2 * hj + ((cls >> 1) & 1), tz = 2 * int(hk) + (cls >> 2);
+  if (tx >= lv.nx || ty >= lv.ny || tz >= lv.nz) return;
+  const int64_t tb = (int64_t(tz) * lv.ny + ty) * lv.nx + tx;
+  if (p.occ[lv.box_off + tb] == 0) return;
+  const int64_t n = p.list_cnt[cls];
+  const int64_t e0 = p.list_off[cls] + n * ch / p.chunks;
+  const int64_t e1 = p.list_off[cls] + n * (ch + 1) / p.chunks;
+  float acc[Pl::NB];
+#pragma unroll
+  for (int q = 0; q < Pl::NB; ++q) acc[q] = 0.f;
+  for (int64_t e = e0; e < e1; ++e) {
+    const int4 d = __ldg(p.list + e);
+    const int sx = tx - d.x, sy = ty - d.y, sz = tz - d.z;
+    if (unsigned(sx) >= unsigned(lv.nx) || unsigned(sy) >= unsigned(lv.ny) || unsigned(sz) >= unsigned(lv.nz))
+      continue;
+    const int64_t sb = (int64_t(sz) * lv.ny + sy) * lv.nx + sx;
+    if (__ldg(p.occ + lv.box_off + sb) == 0) continue;
+    float M[Pl::NA];
+#pragma unroll
+    for (int q = 0; q < Pl::NA; ++q) M[q] = __ldg(p.M + int64_t(q) * lv.nbox + sb);
+    m2l_apply<Pl>(acc, M, p.dtab + int64_t(d.w) * NG, std::make_integer_sequence<int, Pl::K>{});
+  }
+  float* out = p.Lp + int64_t(ch) * NC * lv.nbox;
+#pragma unroll
+  for (int q = 0; q < Pl::NB; ++q) out[int64_t(Pl::BOFF - 1 + q) * lv.nbox + tb] = acc[q];
+}
+
+// Locals of a level: the M2L partials plus the parent's locals shifted to the
+// child centre,  L^c_beta += 2^(-2-|beta|) sum_delta L^p_(beta+delta) v_c^delta / delta!.
+template <int Q>
+__global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_t* __restrict__ occ,
+                          const float* __restrict__ Lpart, int chunks, float* __restrict__ L,
+                          const double* __restrict__ done) {
+  constexpr int NC = ncoef(Q) - 1;
+  if (done && *done != 0.0) return;
+  const float* Lpar = L + lp.box_off * NC;
+  float* Lout = L + lv.box_off * NC;
+  for (int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < int64_t(NC) * lv.nbox;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    const int k = int(t / lv.nbox);
+    const int64_t b = t % lv.nbox;
+    float v = 0.f;
+    if (occ[lv.box_off + b] > 0) {
+      for (int ch = 0; ch < chunks; ++ch) v += Lpart[(int64_t(ch) * NC + k) * lv.nbox + b];
+      if (has_parent) {
+        const char4 e = c_mi[k + 1];
+        const int deg = e.x + e.y + e.z;
+        const int x = int(b % lv.nx), y = int((b / lv.nx) % lv.ny), z = int(b / (int64_t(lv.nx) * lv.ny));
+        const int64_t pb = (int64_t(z >> 1) * lp.ny + (y >> 1)) * lp.nx + (x >> 1);
+        const int cx = x & 1, cy = y & 1, cz = z & 1;
+        float s = 0.f;
+        for (int dx = 0; dx <= Q - deg; ++dx)
+          for (int dy = 0; dy <= Q - deg - dx; ++dy)
+            for (int dz = 0; dz <= Q - deg - dx - dy; ++dz)
+              s += Lpar[int64_t(gidx(e.x + dx, e.y + dy, e.z + dz) - 1) * lp.nbox + pb] * c_shift[cx][dx] *
+                   c_shift[cy][dy] * c_shift[cz][dz];
+        v += ldexpf(s, -2 - deg);
+      }
+    }
+    Lout[int64_t(k) * lv.nbox + b] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Near field + L2P + epilogue: one CTA per leaf box, one target per thread.
+// Source runs (rows of x-adjacent near boxes) are cut into tiles staged in
+// shared memory by bulk copies on an mbarrier pipeline, as in the all-pairs
+// kernel, and swept with the packed clamped pair body.
+// ---------------------------------------------------------------------------
+constexpr int kP2PThreads = 128;
+constexpr int kP2PTile = 256;  // sources (slots) per stage
+constexpr int kP2PStages = 3;
+constexpr int kP2PMaxSteps = 1024;
+constexpr int kP2PSmem = kP2PStages * 2 * kP2PTile * int(sizeof(float4));
+
+struct P2PArgs {
+  FmmLevel lv;
+  const int32_t* start;
+  const int32_t* cnt;
+  const int32_t* perm;
+  const float4* pos2s;
+  const float4* mom2s;
+  const float* L;     // leaf locals, NC rows of nbox
+  const int4* rows;   // (half-width w, dy, dz, 0)
+  int32_t n_rows;
+  const double* done;
+};
+
+template <int Q, bool kForce>
+__global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const AllPairsArgs<float> a,
+                                                         const SceneDesc<float> sc) {
+  using Body = std::conditional_t<kForce, ForceF2Body, FieldF2Body>;
+  constexpr int NC = ncoef(Q) - 1;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[kP2PStages];
+  __shared__ int2 s_steps[kP2PMaxSteps];
+  __shared__ int s_nsteps, s_row, s_pos;
+  __shared__ float s_L[NC];
+  if (p.done && *p.done != 0.0) return;
+  const FmmLevel& lv = p.lv;
+  const int64_t c = blockIdx.x;
+  const int32_t n = p.cnt[c];
+  if (n == 0) return;
+  const int tid = threadIdx.x;
+  const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
+  const int32_t st0 = p.start[c];
+  for (int k = tid; k < NC; k += kP2PThreads) s_L[k] = p.L[int64_t(k) * lv.nbox + c];
+  auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + s * 2 * kP2PTile; };
+  auto stage_mom = [&](int s) { return stage_pos(s) + kP2PTile; };
+  if (tid == 0) {
+    for (int s = 0; s < kP2PStages; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto issue = [&](int k, int s) {
+    const int2 stp = s_steps[k];
+    const uint32_t bytes = uint32_t(stp.y) * uint32_t(sizeof(float4));
+    mbar_arrive_expect_tx(&bar[s], 2 * bytes);
+    bulk_g2s(stage_pos(s), p.pos2s + stp.x, bytes, &bar[s]);
+    bulk_g2s(stage_mom(s), p.mom2s + stp.x, bytes, &bar[s]);
+  };
+  // Thread 0: next tiles of the row walk into s_steps.
+  auto fill = [&]() {
+    int k = 0, r = s_row;
+    int32_t pos = s_pos;
+    while (r < p.n_rows && k < kP2PMaxSteps) {
+      const int4 rw = p.rows[r];
+      const int cy = iy + rw.y, cz = iz + rw.z;
+      if (cy < 0 || cy >= lv.ny || cz < 0 || cz >= lv.nz) {
+        ++r;
+        pos = -1;
+        continue;
+      }
+      const int cx0 = max(ix - rw.x, 0), cx1 = min(ix + rw.x, lv.nx - 1);
+      const int64_t rb = (int64_t(cz) * lv.ny + cy) * lv.nx;
+      const int32_t b = p.start[rb + cx0], e = p.start[rb + cx1 + 1];
+      if (pos < 0) pos = b;
+      if (pos >= e) {
+        ++r;
+        pos = -1;
+        continue;
+      }
+      const int32_t m = min(kP2PTile, e - pos);
+      s_steps[k++] = make_int2(pos, m);
+      pos += m;
+    }
+    s_row = r;
+    s_pos = pos;
+    s_nsteps = k;
+  };
+
+  uint32_t u = 0;  // steps consumed so far (stage and parity of the next)
+  bool failed = false;
+  int fail_k = 0, fail_ns = 0;
+  for (int t0 = 0; t0 < n && !failed; t0 += kP2PThreads) {
+    const bool act = t0 + tid < n;
+    const int32_t i = p.perm[st0 + (act ? t0 + tid : 0)];
+    typename Body::TData td;
+    Body::load(a, i, td);
+    float run[3] = {0.f, 0.f, 0.f}, cmp[3] = {0.f, 0.f, 0.f};
+    if (tid == 0) {
+      s_row = 0;
+      s_pos = -1;
+    }
+    for (;;) {
+      __syncthreads();  // the previous segment's steps are consumed
+      if (tid == 0) fill();
+      __syncthreads();
+      const int ns = s_nsteps;
+      if (ns == 0) break;
+      if (tid == 0)
+        for (int k = 0; k < kP2PStages && k < ns; ++k) issue(k, int((u + k) % kP2PStages));
+      for (int k = 0; k < ns; ++k) {
+        const uint32_t uu = u + uint32_t(k);
+        const int s = int(uu % kP2PStages);
+        const bool ok = mbar_wait_bounded(&bar[s], (uu / kP2PStages) & 1u);
+        if (__syncthreads_or(!ok)) {
+          failed = true;
+          fail_k = k;
+          fail_ns = ns;
+          break;
+        }
+        const int n_items = s_steps[k].y >> 1;
+        const float4* __restrict__ sp = stage_pos(s);
+        const float4* __restrict__ sm = stage_mom(s);
+        typename Body::Acc acc;
+        acc.zero();
+#pragma unroll 4
+        for (int j = 0; j < n_items; ++j) Body::pair(td, Body::load_item(sp, sm, j), sc.pc, acc);
+        float o[3];
+        Body::tile_out(acc, o);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) comp_add(run[q], cmp[q], o[q]);
+        __syncthreads();  // stage s is free
+        if (tid == 0 && k + kP2PStages < ns) {
+          fence_proxy_async_smem();
+          issue(k + kP2PStages, s);
+        }
+      }
+      if (failed) break;
+      u += uint32_t(ns);
+    }
+    if (failed) break;
+    __syncthreads();  // stages idle: reuse them for the power tables
+    // Far field from the box's local expansion at w = (x - centre) / edge.
+    float* pw = reinterpret_cast<float*>(smem_raw);  // [3Q][threads]
+    const float4 tp = a.tpos[i];
+    const float inv_s = 1.f / lv.side;
+    const float w[3] = {(tp.x - (lv.ox + (float(ix) + 0.5f) * lv.side)) * inv_s,
+                        (tp.y - (lv.oy + (float(iy) + 0.5f) * lv.side)) * inv_s,
+                        (tp.z - (lv.oz + (float(iz) + 0.5f) * lv.side)) * inv_s};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      float v = 1.f;
+      pw[(ax * Q) * kP2PThreads + tid] = 1.f;
+#pragma unroll
+      for (int k = 1; k < Q; ++k) {
+        v = v * w[ax] * (1.f / float(k));
+        pw[(ax * Q + k) * kP2PThreads + tid] = v;
+      }
+    }
+    double v[3];
+    for (int q = 0; q < 3; ++q) v[q] = double(run[q]) + double(cmp[q]);
+    if constexpr (!kForce) {
+      // H = -grad phi = -1/(4 pi s^3) sum_g L_(g + e_k) w^g / g!
+      float h0 = 0.f, h1 = 0.f, h2 = 0.f;
+      for (int g = 0; g < ncoef(Q - 1); ++g) {
+        const char4 e = c_mi[g];
+        const float mono = pw[e.x * kP2PThreads + tid] * pw[(Q + e.y) * kP2PThreads + tid] *
+                           pw[(2 * Q + e.z) * kP2PThreads + tid];
+        h0 = fmaf(s_L[gidx(e.x + 1, e.y, e.z) - 1], mono, h0);
+        h1 = fmaf(s_L[gidx(e.x, e.y + 1, e.z) - 1], mono, h1);
+        h2 = fmaf(s_L[gidx(e.x, e.y, e.z + 1) - 1], mono, h2);
+      }
+      const double f = -kInv4Pi * double(inv_s) * double(inv_s) * double(inv_s);
+      v[0] += f * double(h0);
+      v[1] += f * double(h1);
+      v[2] += f * double(h2);
+    } else {
+      // Hess phi = 1/(4 pi s^4) sum_g L_(g + e_a + e_b) w^g / g!;  F = -mu0 Hess phi m_t
+      float hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
+      for (int g = 0; g < ncoef(Q - 2); ++g) {
+        const char4 e = c_mi[g];
+        const float mono = pw[e.x * kP2PThreads + tid] * pw[(Q + e.y) * kP2PThreads + tid] *
+                           pw[(2 * Q + e.z) * kP2PThreads + tid];
+        hxx = fmaf(s_L[gidx(e.x + 2, e.y, e.z) - 1], mono, hxx);
+        hyy = fmaf(s_L[gidx(e.x, e.y + 2, e.z) - 1], mono, hyy);
+        hzz = fmaf(s_L[gidx(e.x, e.y, e.z + 2) - 1], mono, hzz);
+        hxy = fmaf(s_L[gidx(e.x + 1, e.y + 1, e.z) - 1], mono, hxy);
+        hxz = fmaf(s_L[gidx(e.x + 1, e.y, e.z + 1) - 1], mono, hxz);
+        hyz = fmaf(s_L[gidx(e.x, e.y + 1, e.z + 1) - 1], mono, hyz);
+      }
+      const double is2 = double(inv_s) * double(inv_s);
+      const double f = -kMu0 * kInv4Pi * is2 * is2;
+      const float4 tm = a.tmom[i];
+      v[0] += f * (double(hxx) * tm.x + double(hxy) * tm.y + double(hxz) * tm.z);
+      v[1] += f * (double(hxy) * tm.x + double(hyy) * tm.y + double(hyz) * tm.z);
+      v[2] += f * (double(hxz) * tm.x + double(hyz) * tm.y + double(hzz) * tm.z);
+    }
+    if (act) Body::epilogue(a, sc, i, td, v);
+  }
+  if (failed && tid == 0) {
+    // Copies in flight: steps fail_k .. min(fail_ns, fail_k + stages) - 1 of
+    // the segment that failed, one per stage; wait for each (bounded).
+    atomicExch(a.err, MF_DEVERR_STAGE_TIMEOUT);
+    bool drained = true;
+    const int k_stop = min(fail_ns, fail_k + kP2PStages);
+    for (int k = fail_k; k < k_stop; ++k) {
+      const uint32_t uu = u + uint32_t(k);
+      if (!mbar_wait_bounded(&bar[uu % kP2PStages], (uu / kP2PStages) & 1u)) drained = false;
+    }
+    if (!drained) atomicExch(a.err, MF_DEVERR_DRAIN_TIMEOUT);
+  }
+}
+
+unsigned blocks_for(int64_t n, int per = 256, int64_t cap = 65535) {
+  int64_t g = (n + per - 1) / per;
+  if (g > cap) g = cap;
+  return unsigned(g < 1 ? 1 : g);
+}
+
+// Taylor coefficients of 1/|R| times gamma!: D_gamma = d^gamma (1/|R|), all
+// gamma of degree <= nmax, in graded order.  Recurrence on the coefficients
+// T_n = d^n(1/|R|)/n!:  |n| R^2 T_n + (2|n|-1) sum_i R_i T_(n-e_i) + (|n|-1) sum_i T_(n-2e_i) = 0.
+void taylor_inv_r(const double R[3], int nmax, std::vector<double>& D) {
+  const int N = ncoef(nmax);
+  std::vector<double> T(size_t(N), 0.0);
+  std::vector<int> mx(static_cast<size_t>(N)), my(static_cast<size_t>(N)), mz(static_cast<size_t>(N));
+  const double r2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+  for (int n = 0; n <= nmax; ++n)
+    for (int s = 0; s <= n; ++s)
+      for (int z = 0; z <= s; ++z) {
+        const int x = n - s, y = s - z;
+        const int k = gidx(x, y, z);
+        mx[size_t(k)] = x;
+        my[size_t(k)] = y;
+        mz[size_t(k)] = z;
+        if (n == 0) {
+          T[size_t(k)] = 1.0 / std::sqrt(r2);
+          continue;
+        }
+        const int a[3] = {x, y, z};
+        double acc = 0.0;
+        for (int i = 0; i < 3; ++i) {
+          int b[3] = {x, y, z};
+          if (a[i] >= 1) {
+            b[i] -= 1;
+            acc += double(2 * n - 1) * R[i] * T[size_t(gidx(b[0], b[1], b[2]))];
+            b[i] += 1;
+          }
+          if (a[i] >= 2) {
+            b[i] -= 2;
+            acc += double(n - 1) * T[size_t(gidx(b[0], b[1], b[2]))];
+          }
+        }
+        T[size_t(k)] = -acc / (double(n) * r2);
+      }
+  D.assign(size_t(N), 0.0);
+  auto fact = [](int v) {
+    double f = 1.0;
+    for (int i = 2; i <= v; ++i) f *= double(i);
+    return f;
+  };
+  for (int k = 0; k < N; ++k) D[size_t(k)] = T[size_t(k)] * fact(mx[size_t(k)]) * fact(my[size_t(k)]) * fact(mz[size_t(k)]);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox, const FmmConfig& cfg,
+                     cudaStream_t st) {
+  if (n <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no particles");
+  if (n >= (int64_t(1) << 30)) return fail(MF_ERR_INVALID_ARG, "fmm: too many particles");
+  if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 8]");
+  if (!(cfg.theta > 0.0 && cfg.theta <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm: theta must be in (0, 1]");
+  if (cfg.leaf_min < 1) return fail(MF_ERR_INVALID_ARG, "fmm: leaf_min must be >= 1");
+  cfg_ = cfg;
+  degree_ = cfg.order - 1;
+  n_ = n;
+  const int Q = degree_;
+  const int NC = ncoef(Q) - 1;
+
+  // Constant tables (cheap; the module's symbols are per device).
+  {
+    std::vector<char4> mi(static_cast<size_t>(ncoef(kMaxDegree + 1)));
+    for (int d = 0; d <= kMaxDegree + 1; ++d)
+      for (int s = 0; s <= d; ++s)
+        for (int z = 0; z <= s; ++z) mi[size_t(gidx(d - s, s - z, z))] = make_char4(char(d - s), char(s - z), char(z), 0);
+    MF_CUDA_TRY(cudaMemcpyToSymbolAsync(c_mi, mi.data(), mi.size() * sizeof(char4), 0, cudaMemcpyHostToDevice, st));
+    float sh[2][kMaxDegree + 2];
+    for (int c = 0; c < 2; ++c) {
+      const double v = (double(c) - 0.5) / 2.0;
+      double f = 1.0;
+      for (int j = 0; j < kMaxDegree + 2; ++j) {
+        sh[c][j] = float(f);
+        f = f * v / double(j + 1);
+      }
+    }
+    MF_CUDA_TRY(cudaMemcpyToSymbolAsync(c_shift, sh, sizeof(sh), 0, cudaMemcpyHostToDevice, st));
+  }
+
+  // Box grids.
+  double lo[3], ext[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = bbox[k];
+    ext[k] = std::max(0.0, bbox[3 + k] - bbox[k]);
+    if (!std::isfinite(lo[k]) || !std::isfinite(ext[k])) return fail(MF_ERR_INVALID_ARG, "fmm: non-finite positions");
+  }
+  const double emax = std::max({ext[0], ext[1], ext[2]});
+  const double S0 = std::max(emax * (1.0 + 1e-5), h * 1e-3);
+  for (int k = 0; k < 3; ++k) lo[k] -= 0.25e-5 * S0;
+  auto dims_at = [&](int l, int d[3]) {
+    const double s = S0 / double(int64_t(1) << l);
+    for (int k = 0; k < 3; ++k) {
+      int64_t m = int64_t(std::ceil((ext[k] + 0.5e-5 * S0) / s));
+      m = std::max<int64_t>(1, std::min<int64_t>(m, int64_t(1) << l));
+      d[k] = int(m);
+    }
+  };
+  int L = 2;
+  for (int l = 3; l <= kMaxLevel; ++l) {
+    int d[3];
+    dims_at(l, d);
+    const double boxes = double(d[0]) * d[1] * d[2];
+    if (double(n) / boxes < double(cfg.leaf_min) || boxes > double(1 << 24)) break;
+    L = l;
+  }
+  lv_.assign(size_t(L + 1), FmmLevel{});
+  {
+    int d[3];
+    dims_at(L, d);
+    for (int l = L; l >= 0; --l) {
+      FmmLevel& v = lv_[size_t(l)];
+      v.nx = d[0];
+      v.ny = d[1];
+      v.nz = d[2];
+      v.nbox = int64_t(d[0]) * d[1] * d[2];
+      v.side = float(S0 / double(int64_t(1) << l));
+      v.ox = float(lo[0]);
+      v.oy = float(lo[1]);
+      v.oz = float(lo[2]);
+      for (int k = 0; k < 3; ++k) d[k] = (d[k] + 1) / 2;
+    }
+    int64_t off = 0;
+    for (int l = 0; l <= L; ++l) {
+      lv_[size_t(l)].box_off = off;
+      off += lv_[size_t(l)].nbox;
+    }
+  }
+  const FmmLevel& leaf = lv_[size_t(L)];
+  const int64_t nbox_total = leaf.box_off + leaf.nbox;
+  const int64_t ncell = leaf.nbox;
+
+  // Bin.
+  MF_TRY(occ_.reserve(size_t(nbox_total) * sizeof(int32_t)));
+  int32_t* occ = occ_.as<int32_t>();
+  int32_t* cnt = occ + leaf.box_off;
+  MF_TRY(cell_of_.reserve(size_t(n) * sizeof(int32_t)));
+  MF_TRY(start_.reserve(size_t(ncell + 1) * sizeof(int32_t)));
+  MF_TRY(cursor_.reserve(size_t(ncell + 1) * sizeof(int32_t)));
+  MF_TRY(perm_tmp_.reserve(size_t(n + ncell + 2) * sizeof(int32_t)));
+  MF_TRY(perm_.reserve(size_t(n + ncell + 2) * sizeof(int32_t)));
+  MF_CUDA_TRY(cudaMemsetAsync(cnt, 0, size_t(ncell) * sizeof(int32_t), st));
+  k_fmm_count<<<blocks_for(n), 256, 0, st>>>(pos4, n, leaf, cell_of_.as<int32_t>(), cnt);
+  k_fmm_scan<<<1, 1024, 0, st>>>(cnt, ncell, start_.as<int32_t>());
+  MF_CUDA_TRY(cudaMemcpyAsync(cursor_.ptr, start_.ptr, size_t(ncell) * sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+  k_fmm_scatter<<<blocks_for(n), 256, 0, st>>>(cell_of_.as<int32_t>(), n, cursor_.as<int32_t>(),
+                                                perm_tmp_.as<int32_t>());
+  k_fmm_sort<<<blocks_for(ncell * 32), 256, 0, st>>>(start_.as<int32_t>(), cnt, ncell, perm_tmp_.as<int32_t>(),
+                                                      perm_.as<int32_t>());
+  for (int l = L - 1; l >= 0; --l)
+    k_fmm_occ_up<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(lv_[size_t(l + 1)], lv_[size_t(l)], occ);
+  MF_CUDA_TRY(cudaGetLastError());
+  int32_t slots = 0;
+  MF_CUDA_TRY(cudaMemcpyAsync(&slots, start_.as<int32_t>() + ncell, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaStreamSynchronize(st));
+  n_slots_ = slots;
+  if (n_slots_ < n || (n_slots_ & 1)) return fail(MF_ERR_CUDA, "fmm: inconsistent binning");
+  MF_TRY(pos2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
+  MF_TRY(mom2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
+  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), pos4, n_slots_ / 2,
+                                                                pos2s_.as<float4>(), 1, nullptr);
+  MF_CUDA_TRY(cudaGetLastError());
+
+  // Acceptance: box pairs of one level at centre offset d (box units) are far
+  // when theta |d| > r1 + r2 (the box radii, FMMOptions.hpp:56-78) and the gap
+  // |d| - (r1 + r2) exceeds the near radius 4h.
+  const double rnear = 4.0 * h * (1.0 + 1e-4);
+  const double r12 = std::sqrt(3.0);
+  auto far = [&](int l, int dx, int dy, int dz) {
+    if (l <= 0) return false;
+    const double s = double(lv_[size_t(l)].side);
+    const double r0 = std::sqrt(double(dx) * dx + double(dy) * dy + double(dz) * dz);
+    return cfg.theta * r0 > r12 && (r0 - r12) * s > rnear;
+  };
+  auto fdiv = [](int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); };
+  std::map<std::tuple<int, int, int>, int> did;
+  std::vector<int4> list;
+  list_off_.assign(size_t(8 * (L + 1)), 0);
+  list_cnt_.assign(size_t(8 * (L + 1)), 0);
+  for (int l = 2; l <= L; ++l) {
+    const FmmLevel& v = lv_[size_t(l)];
+    // Parent offsets that are not accepted are bounded by this radius.
+    const double sp = 2.0 * double(v.side);
+    const int Dm = int(std::ceil(std::max(r12 / cfg.theta, rnear / sp + r12))) + 1;
+    const int R = 2 * Dm + 2;
+    for (int cls = 0; cls < 8; ++cls) {
+      const int c[3] = {cls & 1, (cls >> 1) & 1, cls >> 2};
+      list_off_[size_t(8 * l + cls)] = int64_t(list.size());
+      const int Rx = std::min(R, v.nx - 1), Ry = std::min(R, v.ny - 1), Rz = std::min(R, v.nz - 1);
+      for (int dz = -Rz; dz <= Rz; ++dz)
+        for (int dy = -Ry; dy <= Ry; ++dy)
+          for (int dx = -Rx; dx <= Rx; ++dx) {
+            if (!far(l, dx, dy, dz)) continue;
+            const int d[3] = {dx, dy, dz};
+            int D[3];
+            for (int k = 0; k < 3; ++k) D[k] = -fdiv(c[k] - d[k], 2);
+            if (far(l - 1, D[0], D[1], D[2])) continue;
+            auto key = std::make_tuple(dx, dy, dz);
+            auto it = did.find(key);
+            int id;
+            if (it == did.end()) {
+              id = int(did.size());
+              did.emplace(key, id);
+            } else {
+              id = it->second;
+            }
+            list.push_back(make_int4(dx, dy, dz, id));
+          }
+      list_cnt_[size_t(8 * l + cls)] = int64_t(list.size()) - list_off_[size_t(8 * l + cls)];
+    }
+  }
+  // Near rows of the leaf level: for each (dy, dz), x offsets |dx| <= w.
+  std::vector<int4> rows;
+  {
+    const int R = int(std::ceil(std::max(r12 / cfg.theta, rnear / double(leaf.side) + r12))) + 1;
+    const int Rx = std::min(R, leaf.nx - 1), Ry = std::min(R, leaf.ny - 1), Rz = std::min(R, leaf.nz - 1);
+    for (int dz = -Rz; dz <= Rz; ++dz)
+      for (int dy = -Ry; dy <= Ry; ++dy) {
+        if (far(L, 0, dy, dz)) continue;
+        int w = 0;
+        while (w + 1 <= Rx && !far(L, w + 1, dy, dz)) ++w;
+        rows.push_back(make_int4(w, dy, dz, 0));
+      }
+  }
+  n_rows_ = int(rows.size());
+  const int NG = ncoef(Q + 1);
+  std::vector<float> dt(did.size() * size_t(NG));
+  {
+    std::vector<double> D;
+    for (const auto& kv : did) {
+      const double R[3] = {double(std::get<0>(kv.first)), double(std::get<1>(kv.first)), double(std::get<2>(kv.first))};
+      taylor_inv_r(R, Q + 1, D);
+      for (int g = 0; g < NG; ++g) dt[size_t(kv.second) * NG + g] = float(D[size_t(g)]);
+    }
+  }
+  MF_TRY(lists_.reserve(std::max<size_t>(1, list.size()) * sizeof(int4)));
+  MF_TRY(rows_.reserve(std::max<size_t>(1, rows.size()) * sizeof(int4)));
+  MF_TRY(dtab_.reserve(std::max<size_t>(1, dt.size()) * sizeof(float)));
+  if (!list.empty())
+    MF_CUDA_TRY(cudaMemcpyAsync(lists_.ptr, list.data(), list.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+  if (!rows.empty())
+    MF_CUDA_TRY(cudaMemcpyAsync(rows_.ptr, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+  if (!dt.empty())
+    MF_CUDA_TRY(cudaMemcpyAsync(dtab_.ptr, dt.data(), dt.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+
+  // Coefficients and the M2L split per level.
+  const int sms = device_sms(current_device());
+  chunks_.assign(size_t(L + 1), 1);
+  int64_t lpart = 1;
+  for (int l = 2; l <= L; ++l) {
+    const FmmLevel& v = lv_[size_t(l)];
+    const int64_t per = ((int64_t((v.nx + 1) / 2) * ((v.ny + 1) / 2) * ((v.nz + 1) / 2)) + 31) / 32 * 32;
+    int64_t ch = (int64_t(sms) * 1024 + 8 * per - 1) / (8 * per);
+    int64_t maxcnt = 1;
+    for (int cls = 0; cls < 8; ++cls) maxcnt = std::max(maxcnt, list_cnt_[size_t(8 * l + cls)]);
+    ch = std::max<int64_t>(1, std::min<int64_t>({ch, 16, maxcnt}));
+    chunks_[size_t(l)] = int32_t(ch);
+    lpart = std::max(lpart, ch * NC * v.nbox);
+  }
+  MF_TRY(mcoef_.reserve(size_t(NC) * size_t(nbox_total) * sizeof(float)));
+  MF_TRY(lcoef_.reserve(size_t(NC) * size_t(nbox_total) * sizeof(float)));
+  MF_TRY(lpart_.reserve(size_t(lpart) * sizeof(float)));
+
+  // Statistics (one more read-back).
+  MF_TRY(stat_.reserve(2 * sizeof(unsigned long long)));
+  MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 2 * sizeof(unsigned long long), st));
+  k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, rows_.as<int4>(), n_rows_,
+                                                      stat_.as<unsigned long long>());
+  MF_CUDA_TRY(cudaGetLastError());
+  unsigned long long hs[2] = {0, 0};
+  std::vector<int32_t> hocc(static_cast<size_t>(ncell));
+  MF_CUDA_TRY(cudaMemcpyAsync(hs, stat_.ptr, sizeof(hs), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaMemcpyAsync(hocc.data(), cnt, size_t(ncell) * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaStreamSynchronize(st));
+  stats_ = FmmStats{};
+  stats_.levels = L + 1;
+  stats_.leaf_level = L;
+  stats_.degree = Q;
+  stats_.leaf_boxes = ncell;
+  for (int32_t c : hocc) stats_.occupied_leaves += c > 0 ? 1 : 0;
+  stats_.p2p_pairs = double(hs[0]);
+  stats_.max_leaf = int32_t(hs[1]);
+  stats_.near_rows = n_rows_;
+  // M2L count from the occupancy of every level (host side, per class list).
+  {
+    std::vector<int32_t> ho(static_cast<size_t>(nbox_total));
+    MF_CUDA_TRY(cudaMemcpy(ho.data(), occ, size_t(nbox_total) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    double m2l = 0;
+    for (int l = 2; l <= L; ++l) {
+      const FmmLevel& v = lv_[size_t(l)];
+      for (int z = 0; z < v.nz; ++z)
+        for (int y = 0; y < v.ny; ++y)
+          for (int x = 0; x < v.nx; ++x) {
+            if (ho[size_t(v.box_off + (int64_t(z) * v.ny + y) * v.nx + x)] == 0) continue;
+            const int cls = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+            for (int64_t e = 0; e < list_cnt_[size_t(8 * l + cls)]; ++e) {
+              const int4 d = list[size_t(list_off_[size_t(8 * l + cls)] + e)];
+              const int sx = x - d.x, sy = y - d.y, sz = z - d.z;
+              if (sx < 0 || sy < 0 || sz < 0 || sx >= v.nx || sy >= v.ny || sz >= v.nz) continue;
+              if (ho[size_t(v.box_off + (int64_t(sz) * v.ny + sy) * v.nx + sx)] == 0) continue;
+              m2l += 1;
+            }
+          }
+    }
+    stats_.m2l_per_product = m2l;
+  }
+  return MF_OK;
+}
+
+mf_status Fmm::product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+                       const SceneDesc<float>& sc, cudaStream_t st, const double* done) {
+  switch (degree_) {
+    case 3: return product_q<3>(force, pos4, smom, a, sc, st, done);
+    case 4: return product_q<4>(force, pos4, smom, a, sc, st, done);
+    case 5: return product_q<5>(force, pos4, smom, a, sc, st, done);
+    case 6: return product_q<6>(force, pos4, smom, a, sc, st, done);
+    case 7: return product_q<7>(force, pos4, smom, a, sc, st, done);
+    default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
+  }
+}
+
+namespace {
+template <int Q>
+struct M2LVariants;
+template <>
+struct M2LVariants<3> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
+    k_fmm_m2l<3, 1, 3><<<g, 128, 0, st>>>(p);
+    *n += 1;
+  }
+};
+template <>
+struct M2LVariants<4> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
+    k_fmm_m2l<4, 1, 4><<<g, 128, 0, st>>>(p);
+    *n += 1;
+  }
+};
+template <>
+struct M2LVariants<5> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
+    k_fmm_m2l<5, 1, 5><<<g, 128, 0, st>>>(p);
+    *n += 1;
+  }
+};
+template <>
+struct M2LVariants<6> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
+    k_fmm_m2l<6, 1, 2><<<g, 128, 0, st>>>(p);
+    k_fmm_m2l<6, 3, 6><<<g, 128, 0, st>>>(p);
+    *n += 2;
+  }
+};
+template <>
+struct M2LVariants<7> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
+    k_fmm_m2l<7, 1, 3><<<g, 128, 0, st>>>(p);
+    k_fmm_m2l<7, 4, 7><<<g, 128, 0, st>>>(p);
+    *n += 2;
+  }
+};
+}  // namespace
+
+template <int Q>
+mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+                         const SceneDesc<float>& sc, cudaStream_t st, const double* done) {
+  constexpr int NC = ncoef(Q) - 1;
+  const int L = int(lv_.size()) - 1;
+  const FmmLevel& leaf = lv_[size_t(L)];
+  int32_t* occ = occ_.as<int32_t>();
+  const int32_t* cnt = occ + leaf.box_off;
+  float* M = mcoef_.as<float>();
+  float* Lc = lcoef_.as<float>();
+  int nl = 0;
+  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), smom, n_slots_ / 2,
+                                                                mom2s_.as<float4>(), 0, done);
+  ++nl;
+  const int sms = device_sms(current_device());
+  k_fmm_p2m<Q><<<blocks_for(leaf.nbox, 1, int64_t(sms) * 16), 128, 0, st>>>(
+      leaf, start_.as<int32_t>(), cnt, perm_.as<int32_t>(), pos4, smom, M + leaf.box_off * NC, done);
+  ++nl;
+  for (int l = L - 1; l >= 2; --l) {
+    k_fmm_m2m<Q><<<blocks_for(int64_t(NC) * lv_[size_t(l)].nbox, 256, int64_t(sms) * 32), 256, 0, st>>>(
+        lv_[size_t(l + 1)], lv_[size_t(l)], occ, M, done);
+    ++nl;
+  }
+  for (int l = 2; l <= L; ++l) {
+    const FmmLevel& v = lv_[size_t(l)];
+    M2LArgs p{};
+    p.lv = v;
+    p.occ = occ;
+    p.M = M + v.box_off * NC;
+    p.Lp = lpart_.as<float>();
+    p.list = lists_.as<int4>();
+    p.dtab = dtab_.as<float>();
+    for (int cls = 0; cls < 8; ++cls) {
+      p.list_off[cls] = list_off_[size_t(8 * l + cls)];
+      p.list_cnt[cls] = int32_t(list_cnt_[size_t(8 * l + cls)]);
+    }
+    p.chunks = chunks_[size_t(l)];
+    p.hx = (v.nx + 1) / 2;
+    p.hy = (v.ny + 1) / 2;
+    p.hz = (v.nz + 1) / 2;
+    p.per_class = ((int64_t(p.hx) * p.hy * p.hz) + 31) / 32 * 32;
+    p.done = done;
+    const int64_t threads = int64_t(p.chunks) * 8 * p.per_class;
+    M2LVariants<Q>::launch(p, unsigned((threads + 127) / 128), st, &nl);
+    k_fmm_l2l<Q><<<blocks_for(int64_t(NC) * v.nbox, 256, int64_t(sms) * 32), 256, 0, st>>>(
+        v, lv_[size_t(l - 1)], l > 2 ? 1 : 0, occ, lpart_.as<float>(), p.chunks, Lc, done);
+    ++nl;
+  }
+  P2PArgs pp{};
+  pp.lv = leaf;
+  pp.start = start_.as<int32_t>();
+  pp.cnt = cnt;
+  pp.perm = perm_.as<int32_t>();
+  pp.pos2s = pos2s_.as<float4>();
+  pp.mom2s = mom2s_.as<float4>();
+  pp.L = Lc + leaf.box_off * NC;
+  pp.rows = rows_.as<int4>();
+  pp.n_rows = n_rows_;
+  pp.done = done;
+  if (leaf.nbox > int64_t(0x7fffffff)) return fail(MF_ERR_INVALID_ARG, "fmm: too many leaf boxes");
+  if (force)
+    k_fmm_p2p<Q, true><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+  else
+    k_fmm_p2p<Q, false><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+  ++nl;
+  launches_ = nl;
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+
+}  // namespace mfgb

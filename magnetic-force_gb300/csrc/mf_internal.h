@@ -250,13 +250,76 @@ class CellList {
   int64_t particles() const { return n_total_; }
   int64_t cells() const { return n_cells_; }
   const std::vector<CellGrid>& grids() const { return host_grids_; }
+  // Bounding box of scene s at the last build (lo xyz, hi xyz; no margin).
+  const double* bbox(int s) const { return host_bbox_.data() + 6 * size_t(s); }
 
  private:
   DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
   std::vector<CellGrid> host_grids_;
+  std::vector<double> host_bbox_;
   int64_t n_total_ = 0, n_cells_ = 0;
   int32_t n_scenes_ = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Uniform-octree FMM for one scene (mf_fmm.cu)
+// ---------------------------------------------------------------------------
+struct FmmConfig {
+  int order = 6;         // expansion terms per degree as the reference counts them (n < P); degree P-1
+  double theta = 0.5;    // multipole acceptance aperture (FMMOptions.hpp:56-78)
+  int leaf_min = 64;     // leaf level: the deepest with at least this many particles per box on average
+};
+
+// One level of the uniform box grid (level 0 is one box holding the scene).
+struct FmmLevel {
+  int32_t nx, ny, nz, pad;
+  int64_t nbox;      // nx * ny * nz
+  int64_t box_off;   // first box of this level in the per-box arrays of all levels
+  float side;        // box edge
+  float ox, oy, oz;  // grid origin (shared by all levels)
+};
+
+struct FmmStats {
+  int32_t levels = 0, leaf_level = 0, degree = 0, pad = 0;
+  int64_t leaf_boxes = 0, occupied_leaves = 0;
+  double p2p_pairs = 0;   // executed near-field pairs per product (real sources)
+  double m2l_per_product = 0;
+  int32_t max_leaf = 0, near_rows = 0;
+};
+
+class Fmm {
+ public:
+  // Builds the box grids, bins the particles of pos4[0..n) into leaf boxes
+  // and lays out the interaction lists.  Synchronises `st` (the bounding box
+  // and the leaf occupancy are read on the host).
+  mf_status build(const float4* pos4, int64_t n, double h, const double* bbox, const FmmConfig& cfg,
+                  cudaStream_t st);
+  // out = epilogue(far field + near field + corr4) of the field (kForce false)
+  // or Kelvin force (kForce true) of the dipoles smom at every particle.  `a`
+  // carries the epilogue's pointers (tpos, tmom, out, out4, add4, add4b, rext,
+  // corr4, err) exactly as for an all-pairs launch; `sc` its coefficients.
+  // `done`: a solver stop flag; every launch is a no-op once it is non-zero.
+  mf_status product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+                    const SceneDesc<float>& sc, cudaStream_t st, const double* done);
+  const FmmStats& stats() const { return stats_; }
+  int launches_per_product() const { return launches_; }
+
+ private:
+  template <int Q>
+  mf_status product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+                      const SceneDesc<float>& sc, cudaStream_t st, const double* done);
+  FmmConfig cfg_;
+  FmmStats stats_;
+  int degree_ = 5;
+  int64_t n_ = 0, n_slots_ = 0;
+  std::vector<FmmLevel> lv_;
+  std::vector<int64_t> list_off_, list_cnt_;  // per (level, class)
+  std::vector<int32_t> chunks_;               // M2L splits per level
+  int n_rows_ = 0;
+  int launches_ = 0;
+  DevBuf cell_of_, cnt_, start_, cursor_, perm_tmp_, perm_, pos2s_, mom2s_;
+  DevBuf occ_, mcoef_, lcoef_, lpart_, lists_, rows_, dtab_, stat_;
 };
 
 // Packed records -> pair layout (sources 2p, 2p+1 as (x_a, x_b, y_a, y_b),

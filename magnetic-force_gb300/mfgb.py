@@ -39,7 +39,9 @@ FP32, FP64 = 0, 1
 Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyforce": 4,
      "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
-       "crit_size": 6, "check_interval": 7, "kernel_timing": 8}
+       "crit_size": 6, "check_interval": 7, "kernel_timing": 8, "fmm": 9, "fmm_order": 10, "fmm_theta": 11,
+       "fmm_leaf": 12}
+FMM_AUTO, FMM_ON, FMM_OFF = 0, 1, 2
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
 
@@ -66,6 +68,14 @@ class mf_counters(ctypes.Structure):
 
 class mf_kernel_stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("total_ms", ctypes.c_double), ("pairs", ctypes.c_double)]
+
+
+class mf_fmm_stats(ctypes.Structure):
+    _fields_ = [("active", ctypes.c_int32), ("levels", ctypes.c_int32), ("leaf_level", ctypes.c_int32),
+                ("degree", ctypes.c_int32), ("leaf_boxes", ctypes.c_int64), ("occupied_leaves", ctypes.c_int64),
+                ("max_leaf", ctypes.c_int32), ("near_rows", ctypes.c_int32), ("p2p_pairs", ctypes.c_double),
+                ("m2l_per_product", ctypes.c_double), ("launches_per_product", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("field_products", ctypes.c_int64), ("force_products", ctypes.c_int64)]
 
 
 KERNEL = {"field": 0, "force": 1, "tensor": 2}
@@ -111,6 +121,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_release_scratch": (i32, []),
         "mf_get_kernel_stats": (i32, [vp, i32, ctypes.POINTER(mf_kernel_stats)]),
         "mf_probe_fp32_peak": (i32, [ctypes.POINTER(f64)]),
+        "mf_get_fmm_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
+        "mf_apply_field": (i32, [vp, vp, i32, i32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -275,6 +287,18 @@ class Solver:
         st = mf_kernel_stats()
         check(load().mf_get_kernel_stats(self._h, KERNEL[kind], ctypes.byref(st)))
         return {"launches": st.launches, "total_ms": st.total_ms, "pairs": st.pairs}
+
+    def fmm_stats(self) -> dict:
+        st = mf_fmm_stats()
+        check(load().mf_get_fmm_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_ if f != "pad"}
+
+    def apply_field(self, moments) -> np.ndarray:
+        """G(m) at the particles: the reference's cuda_magnet_cgOptimizer::G."""
+        m = _f32(moments)
+        out = np.empty_like(m)
+        check(load().mf_apply_field(self._h, m.ctypes.data, LAYOUT_AOS, HOST, out.ctypes.data))
+        return out
 
     def set_option(self, key: str, value: float):
         check(load().mf_set_option(self._h, OPT[key], float(value)))

@@ -1,0 +1,147 @@
+"""GPU tests of the FMM path (uniform octree, Cartesian expansions) against
+the FP64 direct oracle and against the handle's own all-pairs path.
+
+The FMM's only approximation is the expansion truncation: every far box pair
+is beyond the kernel's near radius, so the reference's SPH / fitted-curve
+near field is evaluated exactly.  Tolerances (relative L2 over all sampled
+particles and components), set from measured errors with margin:
+  field operator G(m), P = 8 (degree 7)      1e-5   (measured 2e-6 .. 4e-6)
+  field operator G(m), P = 6 (degree 5)      1e-4   (measured 3e-5 .. 4e-5)
+  solved B/mu0, P = 8, vs all-pairs solve     1e-5   (measured 1e-6)
+  Kelvin force, P = 8, vs all-pairs           3e-4   (measured 3e-5 .. 1.6e-4: the force takes
+                                                     the Hessian of the local expansion)
+  theta -> 0 (every box near): FMM = all-pairs up to summation order, 2e-6
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def solver(mf, sc, **opts):
+    s = mf.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, precision="fp32")
+    for k, v in opts.items():
+        s.set_option(k, v)
+    return s
+
+
+def moments(sc, seed=1):
+    rng = np.random.default_rng(seed)
+    return (np.array([0.2, -0.1, 1.0]) + 0.3 * rng.standard_normal((sc.n, 3))) * sc.volume
+
+
+@pytest.fixture(scope="module")
+def sphere40k():
+    import scenes
+    return scenes.jittered_lattice(40000, "sphere", radius=0.5, chi=1.5, seed=3)
+
+
+@pytest.fixture(scope="module")
+def cylinder100k():
+    import scenes
+    return scenes.jittered_lattice(100000, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=3)
+
+
+@pytest.mark.parametrize("order,leaf,tol", [(8, 8, 1e-5), (6, 8, 1e-4), (8, 64, 1e-5), (5, 16, 3e-4)])
+def test_field_operator_vs_oracle(mf, oracle, sphere40k, order, leaf, tol):
+    sc = sphere40k
+    m = moments(sc)
+    rng = np.random.default_rng(2)
+    idx = rng.choice(sc.n, 1500, replace=False)
+    want = oracle.field(sc.pos[idx].astype(np.float64), sc.pos.astype(np.float64), m, sc.h)
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=order, fmm_leaf=leaf)
+    got = s.apply_field(m)
+    st = s.fmm_stats()
+    assert st["active"] == 1 and st["degree"] == order - 1
+    assert rel(got[idx], want) < tol
+
+
+def test_field_operator_cylinder(mf, oracle, cylinder100k):
+    sc = cylinder100k
+    m = moments(sc, seed=4)
+    idx = np.random.default_rng(5).choice(sc.n, 1000, replace=False)
+    want = oracle.field(sc.pos[idx].astype(np.float64), sc.pos.astype(np.float64), m, sc.h)
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=8, fmm_leaf=32)
+    assert rel(s.apply_field(m)[idx], want) < 1e-5
+    # the same handle on the all-pairs path
+    s.set_option("fmm", mf.FMM_OFF)
+    assert rel(s.apply_field(m)[idx], want) < 1e-6
+
+
+def test_all_near_equals_allpairs(mf, sphere40k):
+    # With a tiny aperture no box pair is accepted: the product is the near
+    # field alone (packed pairs + correction) over every leaf box.
+    sc = sphere40k
+    m = moments(sc, seed=6)
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_theta=0.02, fmm_leaf=64)
+    got = s.apply_field(m)
+    st = s.fmm_stats()
+    assert st["m2l_per_product"] == 0
+    assert st["p2p_pairs"] == float(sc.n) * sc.n
+    s.set_option("fmm", mf.FMM_OFF)
+    assert rel(got, s.apply_field(m)) < 2e-6
+
+
+def test_solve_and_force_vs_allpairs(mf, sphere40k):
+    sc = sphere40k
+    out = {}
+    for mode in (mf.FMM_ON, mf.FMM_OFF):
+        s = solver(mf, sc, fmm=mode, fmm_order=8, fmm_leaf=8, solver=mf.SOLVER_CG)
+        it, rr = s.solve(300)
+        assert rr < 1e-6
+        s.evaluate_fitted_near_foece()
+        out[mode] = (s.total_B_over_mu0, s.M, s.magnetic_bodyforce)
+        if mode == mf.FMM_ON:
+            st = s.fmm_stats()
+            assert st["field_products"] >= it and st["force_products"] == 1
+    b1, m1, f1 = out[mf.FMM_ON]
+    b2, m2, f2 = out[mf.FMM_OFF]
+    assert rel(b1, b2) < 1e-5
+    assert rel(m1, m2) < 1e-5
+    assert rel(f1, f2) < 3e-4
+
+
+def test_nlcg_with_fmm(mf, sphere40k):
+    sc = sphere40k
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=6, fmm_leaf=16)
+    s.tolerance = 1e-4
+    s.solve(40)
+    h = s.error_history()
+    assert len(h) >= 2 and h[-1] < h[0]
+
+
+def test_advance_rebuilds_tree(mf, cylinder100k):
+    # Positions move each step; the octree is rebuilt from the new positions.
+    sc = cylinder100k
+    res = {}
+    for mode in (mf.FMM_ON, mf.FMM_OFF):
+        s = solver(mf, sc, fmm=mode, fmm_order=8, fmm_leaf=32, solver=mf.SOLVER_CG)
+        for _ in range(2):
+            s.advance(1e-3, 100)
+        res[mode] = (s.xyz, s.magnetic_bodyforce)
+    assert np.max(np.abs(res[mf.FMM_ON][0] - res[mf.FMM_OFF][0])) < 1e-6
+    assert rel(res[mf.FMM_ON][1], res[mf.FMM_OFF][1]) < 3e-4
+
+
+def test_auto_mode_threshold(mf):
+    import scenes
+    small = scenes.uniform_cube(65536, seed=9, volume=1e-6, chi=1.0)
+    big = scenes.uniform_cube(65537, seed=9, volume=1e-6, chi=1.0)
+    assert solver(mf, small).fmm_stats()["active"] == 0
+    assert solver(mf, big).fmm_stats()["active"] == 1
+    s = solver(mf, big, fmm=mf.FMM_OFF)
+    assert s.fmm_stats()["active"] == 0
+
+
+def test_bad_fmm_options(mf, sphere40k):
+    s = solver(mf, sphere40k)
+    for key, v in (("fmm", 3), ("fmm_order", 3), ("fmm_order", 9), ("fmm_theta", 0.0), ("fmm_theta", 1.5),
+                   ("fmm_leaf", 0)):
+        with pytest.raises(mf.MFError):
+            s.set_option(key, v)
