@@ -62,10 +62,13 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--requests", type=int, default=24)
     ap.add_argument("--rate", type=float, default=2.0, help="served: mean Poisson arrival rate, requests/s")
-    ap.add_argument("--workload", default="allpairs65k", choices=["allpairs65k", "batch256", "plain4096", "served"],
+    ap.add_argument("--workload", default="allpairs65k",
+                    choices=["allpairs65k", "batch256", "plain4096", "served", "fmm1m"],
                     help="allpairs65k: the headline config (default); batch256: 256 scenes log-uniform "
                          "in [512, 32768] in one launch per stage vs the same scenes one at a time; "
-                         "plain4096: N=4096 uniform cube solved in FP64 to 1e-8")
+                         "plain4096: N=4096 uniform cube solved in FP64 to 1e-8; fmm1m: N=1,048,576 "
+                         "jittered-lattice cylinder through the FMM (P=8, theta=0.5)")
+    ap.add_argument("--fmm-order", type=int, default=8)
     ap.add_argument("--scenes", type=int, default=256)
     return ap.parse_args()
 
@@ -605,6 +608,144 @@ def run_served(args, rank, world, local):
     srv.close()
 
 
+def run_fmm(args, rank, world, local):
+    """Config 3: N = 1,048,576 jittered-lattice cylinder (r = 0.3, height 1,
+    h = 2 spacings, chi = 1.5, H0 = (0,0,1)) through the FMM (P = 8, theta =
+    0.5, leaf boxes of >= 64 particles).  A step is one timestep as in the
+    headline workload.  value counts effective pairs (N^2 per product, the FMM
+    convention); executed near-field pairs are reported beside it.  Errors:
+    against the FP64 oracle on 2,048 seeded targets (CPU) and against the FP32
+    all-pairs direct kernel on a seeded 65,536-target subsample (GPU)."""
+    import torch
+    import mfgb
+    import scenes
+
+    torch.cuda.set_device(local)
+    sc = scenes.config_fmm_1m(args.n if args.n != 65536 else 1 << 20)
+    n = sc.n
+    s = mfgb.Solver(n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
+    s.set_option("solver", mfgb.SOLVER_CG)
+    s.set_option("rel_tol", 1e-6)
+    s.set_option("fmm", mfgb.FMM_ON)
+    s.set_option("fmm_order", args.fmm_order)
+    s.set_option("fmm_theta", 0.5)
+    s.set_option("fmm_leaf", 64)
+    s.set_option("kernel_timing", 1)
+    t0 = time.perf_counter()
+    cold_iters, cold_res = s.solve(500)
+    torch.cuda.synchronize()
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(args.warmup):
+        s.advance(args.dt, 500)
+    torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    s.reset_counters()
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms, iters = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        iters.append(s.advance(args.dt, 500))
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ctr = s.counters()
+    st = s.fmm_stats()
+    ks = {k: s.kernel_stats(k) for k in ("field", "force", "fmm_near_field", "fmm_near_force", "fmm_far")}
+    total_ms = sum(step_ms)
+    t_max = allreduce_max(total_ms, world)
+    pairs = allreduce_sum(ctr["field_pairs"] + ctr["force_pairs"], world)
+    value = pairs / (t_max * 1e-3)
+    executed = (st["field_products"] + st["force_products"]) * st["p2p_pairs"]
+
+    peak = mfgb.probe_fp32_peak()
+    kern = {}
+    for name, fpp in (("fmm_near_field", FLOP_FIELD_PAIR), ("fmm_near_force", FLOP_FORCE_PAIR)):
+        k = ks[name]
+        if k["launches"]:
+            kern[name] = {"launches": k["launches"], "total_ms": round(k["total_ms"], 4),
+                          "avg_ms": round(k["total_ms"] / k["launches"], 4),
+                          "pairs_per_launch": k["pairs"] / k["launches"],
+                          "tflops": fpp * k["pairs"] / (k["total_ms"] * 1e-3) / 1e12}
+    far = ks["fmm_far"]
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    roofline = {"bound": "fp32", "achieved": round(kern[dom]["tflops"], 3), "peak": round(peak, 3),
+                "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": None,
+                "kernel": f"k_fmm_p2p<{'force' if dom.endswith('force') else 'field'}>",
+                "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
+                "kernels": kern,
+                "far_field": {"launches": far["launches"], "total_ms": round(far["total_ms"], 4),
+                              "m2l_per_product": st["m2l_per_product"]},
+                "products_ms": {"field": ks["field"]["total_ms"] / max(ks["field"]["launches"], 1),
+                                "force": ks["force"]["total_ms"] / max(ks["force"]["launches"], 1)},
+                "note": "near-field kernel: executed pairs x minimal far-form FLOP (32 field, 53 force) / "
+                        "its event-timed duration"}
+    errors = None
+    if rank == 0:
+        errors = sample_errors(s, sc, k=2048)
+        errors["oracle"] = "FP64 CPU oracle sums over all N at 2,048 seeded targets"
+        # 65,536 seeded targets against the FP32 all-pairs direct kernels
+        rng = np.random.default_rng(65536)
+        idx = np.sort(rng.choice(n, size=min(65536, n), replace=False))
+        pos = torch.from_numpy(s.xyz).cuda()
+        M = torch.from_numpy(s.M).cuda()
+        b = s.total_B_over_mu0[idx].astype(np.float64)
+        hext = s.Hext[idx].astype(np.float64)
+        c = sc.volume * sc.chi / (1 + sc.chi)
+        G = mfgb.direct_field(pos[idx], pos, M, sc.h).double().cpu().numpy()
+        r = b - hext - G  # fixed point b = Hext + G(c b), with M = c b
+        T = mfgb.direct_force_tensor(pos[idx], pos, M, sc.h).double().cpu().numpy().reshape(-1, 3, 3)
+        Fd = np.einsum("icr,ic->ir", T, M[idx].double().cpu().numpy())
+        F = s.magnetic_bodyforce[idx].astype(np.float64)
+        errors["subsample_65536"] = {
+            "fixed_point_rel_residual": float(np.linalg.norm(r) / np.linalg.norm(hext)),
+            "force_rel_l2": float(np.linalg.norm(F - Fd) / np.linalg.norm(Fd)),
+            "against": "FP32 all-pairs direct kernels (mf_direct_field / mf_direct_force_tensor)"}
+        del c
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(s, sc, args, world)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rf, rg, sample = cpu_pair_rates(sc.pos, s.M, sc.h, args.cpu_seconds)
+        cpu_time = ctr["field_pairs"] / rf + ctr["force_pairs"] / rg
+        cpu = {"value": (ctr["field_pairs"] + ctr["force_pairs"]) / cpu_time, "unit": UNIT,
+               "cores": cpu_threads(), "kind": "port",
+               "sample": sample + "; value = the timed step's effective field/force pairs at these direct rates "
+                                  "(the CPU evaluates them all-pairs)"}
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded jittered-lattice cylinder (the reference ships no dataset)",
+            "config": {"workload": f"fmm_fp32_{n}: jittered lattice cylinder r=0.3 height 1, N={n}, "
+                                   f"h=2*spacing={sc.h:.5f}, chi=1.5, H0=(0,0,1), FMM P={args.fmm_order} "
+                                   f"theta=0.5 leaf>=64, dt={args.dt}, CG rel tol 1e-6",
+                       "N": n, "step": "one timestep: octree rebuild, warm-started CG solve (FMM products), "
+                                       "Kelvin force (FMM), symplectic Euler",
+                       "l2": "flushed before every timed step (256 MiB write, not timed)",
+                       "parallelism": f"replicas x{world}", "pairs": "effective (N^2 per product)"},
+            "field_pairs": ctr["field_pairs"], "force_pairs": ctr["force_pairs"],
+            "executed_near_pairs": executed, "fmm": st,
+            "solve_iters_per_step": iters, "step_ms": [round(v, 4) for v in step_ms],
+            "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+            "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
+            "gpu_launches": ctr["kernel_launches"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "errors": errors, "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    s.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup()
@@ -616,6 +757,8 @@ def main():
         run_batch(args, rank, world, local)
     elif args.workload == "plain4096":
         run_plain_fp64(args, rank, world, local)
+    elif args.workload == "fmm1m":
+        run_fmm(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

@@ -201,7 +201,14 @@ mf_status mf_reset_counters(mf_solver* s);
  * CUDA events on the handle's stream while MF_OPT_KERNEL_TIMING is on.
  * Launches that found their solve already stopped are not counted.
  * Reset by mf_reset_counters.  Synchronises the handle's stream. */
-typedef enum mf_kernel_kind { MF_K_FIELD = 0, MF_K_FORCE = 1, MF_K_TENSOR = 2 } mf_kernel_kind;
+typedef enum mf_kernel_kind {
+  MF_K_FIELD = 0,           /* field products (an FMM product timed as a whole) */
+  MF_K_FORCE = 1,           /* force products (likewise) */
+  MF_K_TENSOR = 2,          /* external gradient tensor */
+  MF_K_FMM_NEAR_FIELD = 3,  /* the FMM near-field kernel of field products; pairs = executed near pairs */
+  MF_K_FMM_NEAR_FORCE = 4,  /* the FMM near-field kernel of force products */
+  MF_K_FMM_FAR = 5          /* the FMM far-field stages (gather, P2M, M2M, M2L, L2L); pairs = M2L translations */
+} mf_kernel_kind;
 typedef struct mf_kernel_stats {
   int64_t launches;
   double total_ms;

@@ -674,7 +674,7 @@ class Engine final : public EngineBase {
 
  public:
   mf_status kernel_stats(int kind, mf_kernel_stats* out) override {
-    if (kind < 0 || kind > 2 || !out) return fail(MF_ERR_INVALID_ARG, "bad kernel kind");
+    if (kind < 0 || kind >= kKinds || !out) return fail(MF_ERR_INVALID_ARG, "bad kernel kind");
     MF_CUDA_TRY(cudaStreamSynchronize(st_));
     for (TimedLaunch& t : timed_) {
       float ms = 0.f;
@@ -765,7 +765,8 @@ class Engine final : public EngineBase {
     cudaEvent_t start = nullptr, stop = nullptr;
   };
   std::vector<TimedLaunch> timed_;
-  mf_kernel_stats agg_[3] = {};
+  static constexpr int kKinds = MF_K_FMM_FAR + 1;
+  mf_kernel_stats agg_[kKinds] = {};
   bool timing_ = false;
 
   // FP32: the packed two-source kernels need the sources in pair layout, the
@@ -844,18 +845,33 @@ class Engine final : public EngineBase {
         a.add4 = add4;
         a.add4b = add4b;
       }
-      TimedLaunch t;
+      // Timing: the whole product (kind field / force), its far-field stages
+      // (gather .. L2L) and its near-field kernel, each on its own events.
+      TimedLaunch t, tf, tn;
+      cudaEvent_t marks[4] = {nullptr, nullptr, nullptr, nullptr};
       if (timing_) {
-        t.body = force ? 1 : 0;
+        t.body = force ? MF_K_FORCE : MF_K_FIELD;
         t.pairs = plan.pairs;
-        MF_CUDA_TRY(cudaEventCreate(&t.start));
-        MF_CUDA_TRY(cudaEventCreate(&t.stop));
+        tf.body = MF_K_FMM_FAR;
+        tf.pairs = fmm_.stats().m2l_per_product;
+        tn.body = force ? MF_K_FMM_NEAR_FORCE : MF_K_FMM_NEAR_FIELD;
+        tn.pairs = fmm_.stats().p2p_pairs;
+        for (TimedLaunch* x : {&t, &tf, &tn}) {
+          MF_CUDA_TRY(cudaEventCreate(&x->start));
+          MF_CUDA_TRY(cudaEventCreate(&x->stop));
+        }
         MF_CUDA_TRY(cudaEventRecord(t.start, st_));
+        marks[0] = tf.start;
+        marks[1] = tf.stop;
+        marks[2] = tn.start;
+        marks[3] = tn.stop;
       }
-      MF_TRY(fmm_.product(force, pos4(), src_mom, a, plan.host[0], st_, done));
+      MF_TRY(fmm_.product(force, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr));
       if (timing_) {
         MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
         timed_.push_back(t);
+        timed_.push_back(tf);
+        timed_.push_back(tn);
       }
       ctr_.kernel_launches += fmm_.launches_per_product() + 1;
       if (force) ++fmm_force_products_;
@@ -984,11 +1000,14 @@ class Engine final : public EngineBase {
     ctr_.field_pairs -= double(launched - executed) * plan_cgq_.pairs;
     if (timing_) {
       int64_t to_mark = launched - executed;  // the last field launches of this solve
-      for (auto it = timed_.rbegin(); it != timed_.rend() && to_mark > 0; ++it)
-        if (it->body == 0) {
+      for (auto it = timed_.rbegin(); it != timed_.rend() && to_mark > 0; ++it) {
+        if (it->body == MF_K_FIELD) {
           it->skipped = true;
           --to_mark;
+        } else if (it->body == MF_K_FMM_NEAR_FIELD || it->body == MF_K_FMM_FAR) {
+          it->skipped = true;  // stages of an FMM product that found the solve stopped
         }
+      }
     }
     if (iters_out) *iters_out = executed;
     if (err_out) *err_out = row[S_RELRES];

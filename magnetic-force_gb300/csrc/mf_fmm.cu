@@ -139,9 +139,11 @@ __global__ void k_fmm_occ_up(FmmLevel lc, FmmLevel lp, int32_t* __restrict__ occ
 // Sorted records in pair layout: slots 2p, 2p+1 as (x_a, x_b, y_a, y_b),
 // (z_a, z_b, 0, 0).  A padding slot (always the odd one) repeats its
 // partner's position (pos) or holds a zero dipole (moments).
-__global__ void k_fmm_gather_pairs(const int32_t* __restrict__ perm, const float4* __restrict__ src, int64_t n_pairs,
-                                   float4* __restrict__ dst, int is_pos, const double* __restrict__ done) {
+__global__ void k_fmm_gather_pairs(const int32_t* __restrict__ perm, const float4* __restrict__ src,
+                                   const int32_t* __restrict__ n_slots, float4* __restrict__ dst, int is_pos,
+                                   const double* __restrict__ done) {
   if (done && *done != 0.0) return;
+  const int64_t n_pairs = *n_slots / 2;
   for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n_pairs;
        p += int64_t(gridDim.x) * blockDim.x) {
     const int32_t ia = perm[2 * p], ib = perm[2 * p + 1];
@@ -170,6 +172,26 @@ __global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, co
     }
     atomicAdd(&out[0], s * unsigned(n));
     atomicMax(&out[1], (unsigned long long)n);
+    atomicAdd(&out[3], 1ull);
+  }
+}
+
+// Multipole-to-local translations of one level (occupied target and source).
+__global__ void k_fmm_m2l_stats(FmmLevel lv, const int32_t* __restrict__ occ, const int4* __restrict__ list,
+                                const int64_t* __restrict__ off, const int64_t* __restrict__ cnt,
+                                unsigned long long* __restrict__ out) {
+  for (int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; b < lv.nbox; b += int64_t(gridDim.x) * blockDim.x) {
+    if (occ[lv.box_off + b] == 0) continue;
+    const int x = int(b % lv.nx), y = int((b / lv.nx) % lv.ny), z = int(b / (int64_t(lv.nx) * lv.ny));
+    const int cls = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    unsigned long long k = 0;
+    for (int64_t e = off[cls]; e < off[cls] + cnt[cls]; ++e) {
+      const int4 d = list[e];
+      const int sx = x - d.x, sy = y - d.y, sz = z - d.z;
+      if (unsigned(sx) >= unsigned(lv.nx) || unsigned(sy) >= unsigned(lv.ny) || unsigned(sz) >= unsigned(lv.nz)) continue;
+      k += occ[lv.box_off + (int64_t(sz) * lv.ny + sy) * lv.nx + sx] > 0 ? 1 : 0;
+    }
+    atomicAdd(&out[2], k);
   }
 }
 
@@ -836,14 +858,12 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   for (int l = L - 1; l >= 0; --l)
     k_fmm_occ_up<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(lv_[size_t(l + 1)], lv_[size_t(l)], occ);
   MF_CUDA_TRY(cudaGetLastError());
-  int32_t slots = 0;
-  MF_CUDA_TRY(cudaMemcpyAsync(&slots, start_.as<int32_t>() + ncell, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  MF_CUDA_TRY(cudaStreamSynchronize(st));
-  n_slots_ = slots;
-  if (n_slots_ < n || (n_slots_ & 1)) return fail(MF_ERR_CUDA, "fmm: inconsistent binning");
+  // Slots: every box padded to an even count, so at most n + ncell; the
+  // kernels read the exact count (start[ncell]) on the device.
+  n_slots_ = n + ncell + 1;
   MF_TRY(pos2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
   MF_TRY(mom2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
-  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), pos4, n_slots_ / 2,
+  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), pos4, start_.as<int32_t>() + ncell,
                                                                 pos2s_.as<float4>(), 1, nullptr);
   MF_CUDA_TRY(cudaGetLastError());
 
@@ -909,25 +929,54 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
       }
   }
   n_rows_ = int(rows.size());
+  // Interaction lists, rows and the derivative table are uploaded only when
+  // they changed (positions that move a little keep the same grid shape).
+  // Uploads go through pinned staging that stays alive until the next build.
   const int NG = ncoef(Q + 1);
-  std::vector<float> dt(did.size() * size_t(NG));
-  {
+  std::vector<int32_t> dkey;
+  dkey.reserve(did.size() * 3 + 1);
+  dkey.push_back(Q);
+  for (const auto& kv : did) {
+    dkey.push_back(std::get<0>(kv.first));
+    dkey.push_back(std::get<1>(kv.first));
+    dkey.push_back(std::get<2>(kv.first));
+  }
+  const bool same_lists = (list == host_list_) && (rows == host_rows_);
+  const bool same_d = (dkey == host_dkey_);
+  if (!same_d) {
+    // Kernels of earlier products may still read the old tables: the
+    // uploads are ordered on the stream, from host copies kept as members.
+    MF_CUDA_TRY(cudaStreamSynchronize(st));
+    host_dt_.assign(did.size() * size_t(NG), 0.f);
     std::vector<double> D;
     for (const auto& kv : did) {
       const double R[3] = {double(std::get<0>(kv.first)), double(std::get<1>(kv.first)), double(std::get<2>(kv.first))};
       taylor_inv_r(R, Q + 1, D);
-      for (int g = 0; g < NG; ++g) dt[size_t(kv.second) * NG + g] = float(D[size_t(g)]);
+      for (int g = 0; g < NG; ++g) host_dt_[size_t(kv.second) * NG + g] = float(D[size_t(g)]);
     }
+    MF_TRY(dtab_.reserve(std::max<size_t>(1, host_dt_.size()) * sizeof(float)));
+    if (!host_dt_.empty())
+      MF_CUDA_TRY(cudaMemcpyAsync(dtab_.ptr, host_dt_.data(), host_dt_.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    host_dkey_ = dkey;
   }
-  MF_TRY(lists_.reserve(std::max<size_t>(1, list.size()) * sizeof(int4)));
-  MF_TRY(rows_.reserve(std::max<size_t>(1, rows.size()) * sizeof(int4)));
-  MF_TRY(dtab_.reserve(std::max<size_t>(1, dt.size()) * sizeof(float)));
-  if (!list.empty())
-    MF_CUDA_TRY(cudaMemcpyAsync(lists_.ptr, list.data(), list.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
-  if (!rows.empty())
-    MF_CUDA_TRY(cudaMemcpyAsync(rows_.ptr, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
-  if (!dt.empty())
-    MF_CUDA_TRY(cudaMemcpyAsync(dtab_.ptr, dt.data(), dt.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  if (!same_lists) {
+    MF_CUDA_TRY(cudaStreamSynchronize(st));
+    host_list_ = std::move(list);
+    host_rows_ = std::move(rows);
+    host_lofs_ = list_off_;
+    host_lofs_.insert(host_lofs_.end(), list_cnt_.begin(), list_cnt_.end());
+    MF_TRY(lists_.reserve(std::max<size_t>(1, host_list_.size()) * sizeof(int4)));
+    MF_TRY(rows_.reserve(std::max<size_t>(1, host_rows_.size()) * sizeof(int4)));
+    MF_TRY(lofs_.reserve(host_lofs_.size() * sizeof(int64_t)));
+    if (!host_list_.empty())
+      MF_CUDA_TRY(cudaMemcpyAsync(lists_.ptr, host_list_.data(), host_list_.size() * sizeof(int4),
+                                  cudaMemcpyHostToDevice, st));
+    if (!host_rows_.empty())
+      MF_CUDA_TRY(cudaMemcpyAsync(rows_.ptr, host_rows_.data(), host_rows_.size() * sizeof(int4),
+                                  cudaMemcpyHostToDevice, st));
+    MF_CUDA_TRY(cudaMemcpyAsync(lofs_.ptr, host_lofs_.data(), host_lofs_.size() * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, st));
+  }
 
   // Coefficients and the M2L split per level.
   const int sms = device_sms(current_device());
@@ -947,60 +996,54 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   MF_TRY(lcoef_.reserve(size_t(NC) * size_t(nbox_total) * sizeof(float)));
   MF_TRY(lpart_.reserve(size_t(lpart) * sizeof(float)));
 
-  // Statistics (one more read-back).
-  MF_TRY(stat_.reserve(2 * sizeof(unsigned long long)));
-  MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 2 * sizeof(unsigned long long), st));
+  // Statistics, counted on the device and read back lazily (stats()).
+  MF_TRY(stat_.reserve(4 * sizeof(unsigned long long)));
+  MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 4 * sizeof(unsigned long long), st));
   k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, rows_.as<int4>(), n_rows_,
                                                       stat_.as<unsigned long long>());
+  for (int l = 2; l <= L; ++l)
+    k_fmm_m2l_stats<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(
+        lv_[size_t(l)], occ, lists_.as<int4>(), lofs_.as<int64_t>() + 8 * l,
+        lofs_.as<int64_t>() + list_off_.size() + 8 * l, stat_.as<unsigned long long>());
   MF_CUDA_TRY(cudaGetLastError());
-  unsigned long long hs[2] = {0, 0};
-  std::vector<int32_t> hocc(static_cast<size_t>(ncell));
-  MF_CUDA_TRY(cudaMemcpyAsync(hs, stat_.ptr, sizeof(hs), cudaMemcpyDeviceToHost, st));
-  MF_CUDA_TRY(cudaMemcpyAsync(hocc.data(), cnt, size_t(ncell) * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  MF_CUDA_TRY(cudaStreamSynchronize(st));
+  if (!hstat_) MF_CUDA_TRY(cudaMallocHost(&hstat_, 4 * sizeof(unsigned long long)));
+  if (!stat_ev_) MF_CUDA_TRY(cudaEventCreateWithFlags(&stat_ev_, cudaEventDisableTiming));
+  MF_CUDA_TRY(cudaMemcpyAsync(hstat_, stat_.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaEventRecord(stat_ev_, st));
+  stat_pending_ = true;
   stats_ = FmmStats{};
   stats_.levels = L + 1;
   stats_.leaf_level = L;
   stats_.degree = Q;
   stats_.leaf_boxes = ncell;
-  for (int32_t c : hocc) stats_.occupied_leaves += c > 0 ? 1 : 0;
-  stats_.p2p_pairs = double(hs[0]);
-  stats_.max_leaf = int32_t(hs[1]);
   stats_.near_rows = n_rows_;
-  // M2L count from the occupancy of every level (host side, per class list).
-  {
-    std::vector<int32_t> ho(static_cast<size_t>(nbox_total));
-    MF_CUDA_TRY(cudaMemcpy(ho.data(), occ, size_t(nbox_total) * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    double m2l = 0;
-    for (int l = 2; l <= L; ++l) {
-      const FmmLevel& v = lv_[size_t(l)];
-      for (int z = 0; z < v.nz; ++z)
-        for (int y = 0; y < v.ny; ++y)
-          for (int x = 0; x < v.nx; ++x) {
-            if (ho[size_t(v.box_off + (int64_t(z) * v.ny + y) * v.nx + x)] == 0) continue;
-            const int cls = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-            for (int64_t e = 0; e < list_cnt_[size_t(8 * l + cls)]; ++e) {
-              const int4 d = list[size_t(list_off_[size_t(8 * l + cls)] + e)];
-              const int sx = x - d.x, sy = y - d.y, sz = z - d.z;
-              if (sx < 0 || sy < 0 || sz < 0 || sx >= v.nx || sy >= v.ny || sz >= v.nz) continue;
-              if (ho[size_t(v.box_off + (int64_t(sz) * v.ny + sy) * v.nx + sx)] == 0) continue;
-              m2l += 1;
-            }
-          }
-    }
-    stats_.m2l_per_product = m2l;
-  }
   return MF_OK;
 }
 
+const FmmStats& Fmm::stats() {
+  if (stat_pending_ && stat_ev_ && cudaEventSynchronize(stat_ev_) == cudaSuccess) {
+    stats_.p2p_pairs = double(hstat_[0]);
+    stats_.max_leaf = int32_t(hstat_[1]);
+    stats_.m2l_per_product = double(hstat_[2]);
+    stats_.occupied_leaves = int64_t(hstat_[3]);
+    stat_pending_ = false;
+  }
+  return stats_;
+}
+
+Fmm::~Fmm() {
+  if (hstat_) cudaFreeHost(hstat_);
+  if (stat_ev_) cudaEventDestroy(stat_ev_);
+}
+
 mf_status Fmm::product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                       const SceneDesc<float>& sc, cudaStream_t st, const double* done) {
+                       const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
   switch (degree_) {
-    case 3: return product_q<3>(force, pos4, smom, a, sc, st, done);
-    case 4: return product_q<4>(force, pos4, smom, a, sc, st, done);
-    case 5: return product_q<5>(force, pos4, smom, a, sc, st, done);
-    case 6: return product_q<6>(force, pos4, smom, a, sc, st, done);
-    case 7: return product_q<7>(force, pos4, smom, a, sc, st, done);
+    case 3: return product_q<3>(force, pos4, smom, a, sc, st, done, marks);
+    case 4: return product_q<4>(force, pos4, smom, a, sc, st, done, marks);
+    case 5: return product_q<5>(force, pos4, smom, a, sc, st, done, marks);
+    case 6: return product_q<6>(force, pos4, smom, a, sc, st, done, marks);
+    case 7: return product_q<7>(force, pos4, smom, a, sc, st, done, marks);
     default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
   }
 }
@@ -1049,7 +1092,7 @@ struct M2LVariants<7> {
 
 template <int Q>
 mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                         const SceneDesc<float>& sc, cudaStream_t st, const double* done) {
+                         const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
   constexpr int NC = ncoef(Q) - 1;
   const int L = int(lv_.size()) - 1;
   const FmmLevel& leaf = lv_[size_t(L)];
@@ -1058,7 +1101,8 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
   float* M = mcoef_.as<float>();
   float* Lc = lcoef_.as<float>();
   int nl = 0;
-  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), smom, n_slots_ / 2,
+  if (marks) MF_CUDA_TRY(cudaEventRecord(marks[0], st));
+  k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), smom, start_.as<int32_t>() + leaf.nbox,
                                                                 mom2s_.as<float4>(), 0, done);
   ++nl;
   const int sms = device_sms(current_device());
@@ -1107,11 +1151,16 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
   pp.n_rows = n_rows_;
   pp.done = done;
   if (leaf.nbox > int64_t(0x7fffffff)) return fail(MF_ERR_INVALID_ARG, "fmm: too many leaf boxes");
+  if (marks) {
+    MF_CUDA_TRY(cudaEventRecord(marks[1], st));
+    MF_CUDA_TRY(cudaEventRecord(marks[2], st));
+  }
   if (force)
     k_fmm_p2p<Q, true><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
   else
     k_fmm_p2p<Q, false><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
   ++nl;
+  if (marks) MF_CUDA_TRY(cudaEventRecord(marks[3], st));
   launches_ = nl;
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;

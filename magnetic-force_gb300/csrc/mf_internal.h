@@ -300,15 +300,23 @@ class Fmm {
   // carries the epilogue's pointers (tpos, tmom, out, out4, add4, add4b, rext,
   // corr4, err) exactly as for an all-pairs launch; `sc` its coefficients.
   // `done`: a solver stop flag; every launch is a no-op once it is non-zero.
+  // marks (optional, 4 events): recorded before and after the far-field
+  // stages (gather .. L2L), then before and after the near-field kernel.
   mf_status product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                    const SceneDesc<float>& sc, cudaStream_t st, const double* done);
-  const FmmStats& stats() const { return stats_; }
+                    const SceneDesc<float>& sc, cudaStream_t st, const double* done,
+                    cudaEvent_t* marks = nullptr);
+  // Shape and work of the last build (waits for its device counts).
+  const FmmStats& stats();
   int launches_per_product() const { return launches_; }
+  Fmm() = default;
+  Fmm(const Fmm&) = delete;
+  Fmm& operator=(const Fmm&) = delete;
+  ~Fmm();
 
  private:
   template <int Q>
   mf_status product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                      const SceneDesc<float>& sc, cudaStream_t st, const double* done);
+                      const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks);
   FmmConfig cfg_;
   FmmStats stats_;
   int degree_ = 5;
@@ -319,7 +327,14 @@ class Fmm {
   int n_rows_ = 0;
   int launches_ = 0;
   DevBuf cell_of_, cnt_, start_, cursor_, perm_tmp_, perm_, pos2s_, mom2s_;
-  DevBuf occ_, mcoef_, lcoef_, lpart_, lists_, rows_, dtab_, stat_;
+  DevBuf occ_, mcoef_, lcoef_, lpart_, lists_, rows_, dtab_, stat_, lofs_;
+  std::vector<int4> host_list_, host_rows_;  // as last uploaded
+  std::vector<int32_t> host_dkey_;           // degree and offsets of the uploaded derivative table
+  unsigned long long* hstat_ = nullptr;      // pinned: near pairs, largest leaf, M2L count, occupied leaves
+  cudaEvent_t stat_ev_ = nullptr;
+  bool stat_pending_ = false;
+  std::vector<float> host_dt_;
+  std::vector<int64_t> host_lofs_;
 };
 
 // Packed records -> pair layout (sources 2p, 2p+1 as (x_a, x_b, y_a, y_b),
@@ -328,3 +343,8 @@ void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st, const 
               int done_total = 0);
 
 }  // namespace mfgb
+
+// Element-wise equality of CUDA's int4 (host-side comparison of uploaded tables).
+inline bool operator==(const int4& a, const int4& b) { return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w; }
+inline bool operator!=(const int4& a, const int4& b) { return !(a == b); }
+

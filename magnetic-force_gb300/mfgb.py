@@ -78,7 +78,7 @@ class mf_fmm_stats(ctypes.Structure):
                 ("pad", ctypes.c_int32), ("field_products", ctypes.c_int64), ("force_products", ctypes.c_int64)]
 
 
-KERNEL = {"field": 0, "force": 1, "tensor": 2}
+KERNEL = {"field": 0, "force": 1, "tensor": 2, "fmm_near_field": 3, "fmm_near_force": 4, "fmm_far": 5}
 
 _lib = None
 
