@@ -334,7 +334,9 @@ mf_status mf_batch_reset_counters(mf_batch* b);
 /* limit allow, advances every running request by one timestep in shared   */
 /* batched launches, and retires finished requests (their final state is   */
 /* kept for mf_server_result).  Particle state stays on the device while a  */
-/* request runs.  A server is used by one host thread at a time.            */
+/* request runs.  Requests above 65,536 particles run through the FMM      */
+/* (P = 6) as their own solver on their own stream, overlapping the batch  */
+/* on the device.  A server is used by one host thread at a time.          */
 /* ---------------------------------------------------------------------- */
 typedef struct mf_server_config {
   double hbm_budget_bytes;   /* admission budget for request state (e.g. 120e9) */

@@ -521,11 +521,19 @@ class Batch {
 // ---------------------------------------------------------------------------
 // Serving with continuous batching.
 // ---------------------------------------------------------------------------
+// Requests above this many particles run as their own solver handle through
+// the FMM (P = 6, on its own stream, overlapping the batch on the device);
+// smaller ones join the all-pairs batch.
+constexpr int64_t kServeFmmMin = 65536;
+
 class Server {
   using Clock = std::chrono::steady_clock;
 
  public:
-  ~Server() { batch_.reset(); }
+  ~Server() {
+    batch_.reset();
+    for (auto& kv : reqs_) drop_solver(kv.second);
+  }
 
   mf_status init(const mf_server_config& c) {
     if (!(c.hbm_budget_bytes > 0) || c.max_active <= 0 || c.steps_per_request <= 0 || c.iters_per_step < 0 ||
@@ -535,9 +543,14 @@ class Server {
     return MF_OK;
   }
 
-  // Device bytes a running request holds: its own state (3 records per
-  // particle) plus its share of the batch buffers, cell list and scratch.
-  static double need_bytes(int64_t n) { return double(n) * 320.0 + 4.0 * 1024 * 1024; }
+  // Device bytes a running request holds.  Batch member: its own state (3
+  // records per particle) plus its share of the batch buffers, cell list and
+  // scratch.  FMM request: a solver handle's vectors, published arrays, cell
+  // list and octree.
+  static double need_bytes(int64_t n) {
+    if (n > kServeFmmMin) return double(n) * 720.0 + 64.0 * 1024 * 1024;
+    return double(n) * 320.0 + 4.0 * 1024 * 1024;
+  }
 
   mf_status submit(const mf_scene_desc& d, int64_t* id) {
     if (d.n <= 0 || !d.pos) return fail(MF_ERR_INVALID_ARG, "scene without particles");
@@ -565,6 +578,14 @@ class Server {
       Req& r = reqs_.at(queue_.front());
       const double need = need_bytes(r.d.n);
       if (used_ + need > cfg_.hbm_budget_bytes) break;
+      if (r.d.n > kServeFmmMin) {
+        MF_TRY(start_solver(r));
+        used_ += need;
+        r.phase = 1;
+        fmm_active_.push_back(r.id);
+        queue_.pop_front();
+        continue;
+      }
       const size_t bytes = size_t(r.d.n) * sizeof(float4);
       MF_TRY(r.state.reserve(3 * bytes, false, true));
       std::vector<float4> p(size_t(r.d.n));
@@ -576,11 +597,33 @@ class Server {
       queue_.pop_front();
       dirty_ = true;
     }
+    if (!active_.empty() || !fmm_active_.empty()) ++stats_.ticks;
     if (!active_.empty()) {
       if (dirty_) MF_TRY(rebatch());
-      MF_TRY(batch_->step(cfg_.dt, cfg_.iters_per_step, cfg_.rel_tol));
+      MF_TRY(batch_->step(cfg_.dt, cfg_.iters_per_step, cfg_.rel_tol));  // enqueued, not waited for
+    }
+    // FMM requests step on their own streams while the batch runs.
+    {
+      std::vector<int64_t> keep;
+      for (int64_t id : fmm_active_) {
+        Req& r = reqs_.at(id);
+        int64_t it = 0;
+        const mf_status s = mf_advance(r.solver, cfg_.dt, cfg_.iters_per_step, &it);
+        if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
+        ++r.steps;
+        if (r.steps >= cfg_.steps_per_request) {
+          MF_TRY(finish_solver(r));
+          used_ -= need_bytes(r.d.n);
+          ++completed;
+          ++stats_.completed;
+        } else {
+          keep.push_back(id);
+        }
+      }
+      fmm_active_ = keep;
+    }
+    if (!active_.empty()) {
       MF_CUDA_TRY(cudaStreamSynchronize(batch_->stream()));
-      ++stats_.ticks;
       for (int64_t id : active_) ++reqs_.at(id).steps;
       // Retire finished requests: keep their final state on the host.
       std::vector<int64_t> keep;
@@ -609,7 +652,7 @@ class Server {
     }
     const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
     stats_.busy_ms += ms;
-    if (n_active) *n_active = int32_t(active_.size() + size_t(completed));
+    if (n_active) *n_active = int32_t(active_.size() + fmm_active_.size() + size_t(completed));
     if (n_completed) *n_completed = completed;
     if (tick_ms) *tick_ms = ms;
     return MF_OK;
@@ -647,12 +690,18 @@ class Server {
 
   mf_status get_stats(mf_server_stats* out) {
     mf_server_stats s = stats_;
-    s.running = int64_t(active_.size());
+    s.running = int64_t(active_.size() + fmm_active_.size());
     s.queued = int64_t(queue_.size());
     s.bytes_in_use = used_;
     if (batch_) {
       mf_counters c{};
       MF_TRY(batch_->counters(&c));
+      s.field_pairs += c.field_pairs;
+      s.force_pairs += c.force_pairs;
+    }
+    for (int64_t id : fmm_active_) {
+      mf_counters c{};
+      MF_TRY(mf_get_counters(reqs_.at(id).solver, &c));
       s.field_pairs += c.field_pairs;
       s.force_pairs += c.force_pairs;
     }
@@ -670,7 +719,59 @@ class Server {
     int32_t steps = 0;
     Clock::time_point t_submit, t_done;
     std::vector<std::vector<float>> out;
+    mf_solver* solver = nullptr;  // FMM requests: their own solver handle
+    cudaStream_t stream = nullptr;
   };
+
+  // An FMM request: solver handle on its own non-blocking stream, CG to the
+  // server's tolerance, FMM order 6, a converged cold solve before its first step.
+  mf_status start_solver(Req& r) {
+    mf_params p{};
+    p.num_particles = r.d.n;
+    p.h = r.d.h;
+    p.ext_mag_h = r.d.h;
+    p.volume = r.d.volume;
+    p.chi = r.d.chi;
+    for (int k = 0; k < 3; ++k) p.const_ext_field[k] = r.d.H0[k];
+    p.target_pos = r.pos.data();
+    p.precision = MF_FP32;
+    p.device = cfg_.device;
+    MF_TRY(mf_create(&p, &r.solver));
+    MF_CUDA_TRY(cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking));
+    MF_TRY(mf_set_stream(r.solver, r.stream));
+    MF_TRY(mf_set_option(r.solver, MF_OPT_SOLVER, MF_SOLVER_CG));
+    MF_TRY(mf_set_option(r.solver, MF_OPT_REL_TOL, cfg_.rel_tol));
+    MF_TRY(mf_set_option(r.solver, MF_OPT_FMM, 1));
+    MF_TRY(mf_set_option(r.solver, MF_OPT_FMM_ORDER, 6));
+    int64_t it = 0;
+    double rr = 0;
+    const mf_status s = mf_solve(r.solver, 500, &it, &rr);
+    if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
+    ++stats_.rebatches;
+    return MF_OK;
+  }
+  mf_status finish_solver(Req& r) {
+    r.out.resize(5);
+    const int qs[5] = {MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0, MF_Q_FORCE};
+    for (int j = 0; j < 5; ++j) {
+      r.out[size_t(j)].resize(size_t(3 * r.d.n));
+      MF_TRY(mf_get(r.solver, qs[j], r.out[size_t(j)].data(), MF_LAYOUT_AOS, MF_HOST));
+    }
+    mf_counters c{};
+    MF_TRY(mf_get_counters(r.solver, &c));
+    stats_.field_pairs += c.field_pairs;
+    stats_.force_pairs += c.force_pairs;
+    drop_solver(r);
+    r.phase = 2;
+    r.t_done = Clock::now();
+    return MF_OK;
+  }
+  static void drop_solver(Req& r) {
+    if (r.solver) mf_destroy(r.solver);
+    if (r.stream) cudaStreamDestroy(r.stream);
+    r.solver = nullptr;
+    r.stream = nullptr;
+  }
 
   Batch::SceneState state_of(Req& r) {
     float4* base = r.state.as<float4>();
@@ -713,7 +814,7 @@ class Server {
   mf_server_config cfg_{};
   std::map<int64_t, Req> reqs_;
   std::deque<int64_t> queue_;
-  std::vector<int64_t> active_, members_;
+  std::vector<int64_t> active_, members_, fmm_active_;
   std::unique_ptr<Batch> batch_;
   bool dirty_ = false;
   double used_ = 0;

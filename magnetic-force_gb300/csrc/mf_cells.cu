@@ -167,31 +167,45 @@ __global__ void k_sort_cells(const int32_t* __restrict__ start, int64_t n_cells,
 
 __constant__ float c_fit_tbl[40] = MF_FITTED_CURVE_TABLE;
 
-// Near-field correction, one warp per cell: the cell's particles are the
-// targets, handled kT at a time, held by every lane; the lanes split the
-// candidate sources of the neighbourhood (rows of cells trimmed to the
-// cell-level distance bound of the near radius), each lane sweeping its
+// The binned particles in cell order (positions and the product's dipoles),
+// so the correction reads each row of cells as one contiguous range.
+__global__ void k_gather_sorted(const int32_t* __restrict__ perm, const float4* __restrict__ pos,
+                                const float4* __restrict__ mom, int64_t n, float4* __restrict__ spos,
+                                float4* __restrict__ smom, const int32_t* __restrict__ done_count, int done_total) {
+  if (done_count && *done_count >= done_total) return;
+  for (int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t i = perm[q];
+    spos[q] = pos[i];
+    smom[q] = mom[i];
+  }
+}
+
+// Near-field correction, one warp per cell: up to kT of the cell's particles
+// are the targets of a pass, held in shared memory (read as broadcasts); the
+// lanes split the candidate sources of the neighbourhood (rows of cells
+// trimmed to the cell-level distance bound of the near radius, each one
+// contiguous range of the cell-ordered copies), each lane sweeping its
 // sources in increasing order, and every target's sum is finished by a fixed
 // shuffle tree, so results are deterministic.
 template <bool kForce>
 __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __restrict__ grids, int n_scenes,
                                                           int64_t n_cells, const int32_t* __restrict__ perm,
                                                           const int32_t* __restrict__ start,
-                                                          const float4* __restrict__ pos,
-                                                          const float4* __restrict__ mom, float4* __restrict__ corr,
+                                                          const float4* __restrict__ spos,
+                                                          const float4* __restrict__ smom, float4* __restrict__ corr,
                                                           const int32_t* __restrict__ skip_scene,
                                                           const double* __restrict__ done_flags, int done_stride,
                                                           const int32_t* __restrict__ done_count, int done_total) {
-  // Targets held per pass: the force keeps each target's dipole too, so it
-  // holds fewer to stay clear of spills and keep more warps resident.
-  constexpr int kT = kForce ? 4 : 8;
+  constexpr int kT = 8;
   if (done_count && *done_count >= done_total) return;
   __shared__ float s_tbl[40];
+  __shared__ float4 s_tp[4][kT], s_tm[4][kT];
   if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int wi = threadIdx.x >> 5;
   const int64_t n_warps = int64_t(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_cells; c += n_warps) {
+  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + wi; c < n_cells; c += n_warps) {
     const int32_t cb = start[c], ce = start[c + 1];
     if (cb == ce) continue;
     int lo = 0, hi = n_scenes - 1;
@@ -214,16 +228,15 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
     else clamped_field_coeffs(near2, cA, cB);
     for (int32_t t0 = cb; t0 < ce; t0 += kT) {
       const int nt = min(kT, ce - t0);
-      int32_t ti[kT];
-      float4 tp[kT], tm[kT];
+      __syncwarp();
+      if (lane < nt) {
+        s_tp[wi][lane] = spos[t0 + lane];
+        if (kForce) s_tm[wi][lane] = smom[t0 + lane];
+      }
+      __syncwarp();
       float acc[kT][3];
 #pragma unroll
-      for (int t = 0; t < kT; ++t) {
-        ti[t] = perm[t0 + (t < nt ? t : 0)];
-        tp[t] = pos[ti[t]];
-        tm[t] = kForce ? mom[ti[t]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        acc[t][0] = acc[t][1] = acc[t][2] = 0.f;
-      }
+      for (int t = 0; t < kT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = 0.f;
       for (int dz = -R; dz <= R; ++dz) {
         const int cz = iz + dz;
         if (cz < 0 || cz >= g.nz) continue;
@@ -239,33 +252,36 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
           const int64_t row = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx;
           const int32_t sb = start[row + cx0], se = start[row + cx1 + 1];
           for (int32_t q = sb + lane; q < se; q += 32) {
-            const int32_t j = perm[q];
-            const float4 pj = pos[j];
-            const float4 mj = mom[j];
+            const float4 pj = spos[q];
+            const float4 mj = smom[q];
 #pragma unroll
             for (int t = 0; t < kT; ++t) {
-              const float dx = tp[t].x - pj.x, dy2 = tp[t].y - pj.y, dz2 = tp[t].z - pj.z;
-              const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-              if (t < nt && (kForce ? (r2 <= near2) : (r2 < near2))) {
-                if (kForce) {
-                  float P, Q;
-                  force_near_coeffs_fast(r2, s_tbl, inv_h, ih4k, P, Q);
-                  const float dP = P - cA, dQ = Q - cB;
-                  const float ds = dx * mj.x + dy2 * mj.y + dz2 * mj.z;
-                  const float dm = dx * tm[t].x + dy2 * tm[t].y + dz2 * tm[t].z;
-                  const float sm = mj.x * tm[t].x + mj.y * tm[t].y + mj.z * tm[t].z;
-                  const float u = dP * ds, v = dP * dm, wv = dP * sm + dQ * ds * dm;
-                  acc[t][0] += dx * wv + tm[t].x * u + mj.x * v;
-                  acc[t][1] += dy2 * wv + tm[t].y * u + mj.y * v;
-                  acc[t][2] += dz2 * wv + tm[t].z * u + mj.z * v;
-                } else {
-                  float al, be;
-                  field_near_coeffs_fast(r2, inv_h, ih3, al, be);
-                  const float t3 = 3.f * (dx * mj.x + dy2 * mj.y + dz2 * mj.z) * (al - cA);
-                  const float db = be - cB;
-                  acc[t][0] += dx * t3 - mj.x * db;
-                  acc[t][1] += dy2 * t3 - mj.y * db;
-                  acc[t][2] += dz2 * t3 - mj.z * db;
+              if (t < nt) {
+                const float4 tp = s_tp[wi][t];
+                const float dx = tp.x - pj.x, dy2 = tp.y - pj.y, dz2 = tp.z - pj.z;
+                const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
+                if (kForce ? (r2 <= near2) : (r2 < near2)) {
+                  if (kForce) {
+                    const float4 tm = s_tm[wi][t];
+                    float P, Q;
+                    force_near_coeffs_fast(r2, s_tbl, inv_h, ih4k, P, Q);
+                    const float dP = P - cA, dQ = Q - cB;
+                    const float ds = dx * mj.x + dy2 * mj.y + dz2 * mj.z;
+                    const float dm = dx * tm.x + dy2 * tm.y + dz2 * tm.z;
+                    const float sm = mj.x * tm.x + mj.y * tm.y + mj.z * tm.z;
+                    const float u = dP * ds, v = dP * dm, wv = dP * sm + dQ * ds * dm;
+                    acc[t][0] += dx * wv + tm.x * u + mj.x * v;
+                    acc[t][1] += dy2 * wv + tm.y * u + mj.y * v;
+                    acc[t][2] += dz2 * wv + tm.z * u + mj.z * v;
+                  } else {
+                    float al, be;
+                    field_near_coeffs_fast(r2, inv_h, ih3, al, be);
+                    const float t3 = 3.f * (dx * mj.x + dy2 * mj.y + dz2 * mj.z) * (al - cA);
+                    const float db = be - cB;
+                    acc[t][0] += dx * t3 - mj.x * db;
+                    acc[t][1] += dy2 * t3 - mj.y * db;
+                    acc[t][2] += dz2 * t3 - mj.z * db;
+                  }
                 }
               }
             }
@@ -275,14 +291,16 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
       const float scale = kForce ? float(kForceK) : float(kInv4Pi);
 #pragma unroll
       for (int t = 0; t < kT; ++t) {
+        if (t < nt) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          float v = acc[t][k];
+          for (int k = 0; k < 3; ++k) {
+            float v = acc[t][k];
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-          acc[t][k] = v;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            acc[t][k] = v;
+          }
+          if (lane == 0) corr[perm[t0 + t]] = make_float4(acc[t][0] * scale, acc[t][1] * scale, acc[t][2] * scale, 0.f);
         }
-        if (lane == 0 && t < nt) corr[ti[t]] = make_float4(acc[t][0] * scale, acc[t][1] * scale, acc[t][2] * scale, 0.f);
       }
     }
   }
@@ -451,6 +469,8 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
   MF_TRY(perm_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(perm_tmp_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(cell_of_.reserve(sizeof(int32_t) * size_t(n_total_)));
+  MF_TRY(spos_.reserve(sizeof(float4) * size_t(n_total_)));
+  MF_TRY(smom_.reserve(sizeof(float4) * size_t(n_total_)));
   return rebin(pos4, st);
 }
 
@@ -481,9 +501,11 @@ static unsigned cell_grid(int64_t cells) {
 mf_status CellList::field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st,
                                      const double* done_flags, int done_stride, const int32_t* done_count,
                                      int done_total) const {
+  k_gather_sorted<<<grid_for(n_total_), 256, 0, st>>>(perm_.as<int32_t>(), pos4, mom4, n_total_, spos_.as<float4>(),
+                                                      smom_.as<float4>(), done_count, done_total);
   k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
-      skip_field_.as<int32_t>(), done_flags, done_stride, done_count, done_total);
+      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
+      smom_.as<float4>(), corr, skip_field_.as<int32_t>(), done_flags, done_stride, done_count, done_total);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }
@@ -517,9 +539,11 @@ mf_status CellList::set_skips(const std::vector<int32_t>& field, const std::vect
 }
 
 mf_status CellList::force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
+  k_gather_sorted<<<grid_for(n_total_), 256, 0, st>>>(perm_.as<int32_t>(), pos4, mom4, n_total_, spos_.as<float4>(),
+                                                      smom_.as<float4>(), nullptr, 0);
   k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4, corr,
-      skip_force_.as<int32_t>(), nullptr, 0, nullptr, 0);
+      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
+      smom_.as<float4>(), corr, skip_force_.as<int32_t>(), nullptr, 0, nullptr, 0);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

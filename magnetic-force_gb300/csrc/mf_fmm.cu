@@ -176,22 +176,27 @@ __global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, co
   }
 }
 
-// Multipole-to-local translations of one level (occupied target and source).
+// Multipole-to-local translations of one level (occupied target and source),
+// one warp per target box.
 __global__ void k_fmm_m2l_stats(FmmLevel lv, const int32_t* __restrict__ occ, const int4* __restrict__ list,
                                 const int64_t* __restrict__ off, const int64_t* __restrict__ cnt,
                                 unsigned long long* __restrict__ out) {
-  for (int64_t b = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; b < lv.nbox; b += int64_t(gridDim.x) * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t b = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); b < lv.nbox; b += warps) {
     if (occ[lv.box_off + b] == 0) continue;
     const int x = int(b % lv.nx), y = int((b / lv.nx) % lv.ny), z = int(b / (int64_t(lv.nx) * lv.ny));
     const int cls = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-    unsigned long long k = 0;
-    for (int64_t e = off[cls]; e < off[cls] + cnt[cls]; ++e) {
+    unsigned k = 0;
+    for (int64_t e = off[cls] + lane; e < off[cls] + cnt[cls]; e += 32) {
       const int4 d = list[e];
       const int sx = x - d.x, sy = y - d.y, sz = z - d.z;
       if (unsigned(sx) >= unsigned(lv.nx) || unsigned(sy) >= unsigned(lv.ny) || unsigned(sz) >= unsigned(lv.nz)) continue;
-      k += occ[lv.box_off + (int64_t(sz) * lv.ny + sy) * lv.nx + sx] > 0 ? 1 : 0;
+      k += occ[lv.box_off + (int64_t(sz) * lv.ny + sy) * lv.nx + sx] > 0 ? 1u : 0u;
     }
-    atomicAdd(&out[2], k);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    if (lane == 0) atomicAdd(&out[2], (unsigned long long)k);
   }
 }
 
@@ -1002,7 +1007,7 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, rows_.as<int4>(), n_rows_,
                                                       stat_.as<unsigned long long>());
   for (int l = 2; l <= L; ++l)
-    k_fmm_m2l_stats<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(
+    k_fmm_m2l_stats<<<blocks_for(lv_[size_t(l)].nbox * 32), 256, 0, st>>>(
         lv_[size_t(l)], occ, lists_.as<int4>(), lofs_.as<int64_t>() + 8 * l,
         lofs_.as<int64_t>() + list_off_.size() + 8 * l, stat_.as<unsigned long long>());
   MF_CUDA_TRY(cudaGetLastError());

@@ -256,6 +256,7 @@ class CellList {
  private:
   DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
+  DevBuf spos_, smom_;              // positions and dipoles in cell order (per correction)
   std::vector<CellGrid> host_grids_;
   std::vector<double> host_bbox_;
   int64_t n_total_ = 0, n_cells_ = 0;

@@ -7,6 +7,13 @@ Runs mf_direct_field / mf_direct_force / mf_direct_force_tensor on a seeded
 jittered-lattice sphere of N particles (h = 2 x spacing) with random dipoles,
 times each launch with CUDA events and prints one JSON line per kernel:
 device ms per call (packing included), pairs/s and algorithmic TFLOP/s.
+
+    python magnetic-force_gb300/microbench.py --kernel fmm_field --n 262144 --reps 3
+
+``fmm_field`` / ``fmm_force`` run FMM products (P = 8, theta = 0.5) on a seeded
+jittered-lattice cylinder (r = 0.3, height 1) of N particles: the field
+operator G(m) through mf_apply_field, the force through mf_eval_force after a
+CG solve; per-stage device times come from the handle's event timing.
 """
 from __future__ import annotations
 
@@ -23,7 +30,7 @@ FLOP = {"field": 32.0, "force": 53.0, "tensor": 53.0}
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all"])
+    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force"])
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
@@ -35,6 +42,8 @@ def main():
     import mfgb
     import scenes
 
+    if args.kernel.startswith("fmm"):
+        return fmm(args, np, torch, mfgb, scenes)
     sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
     rng = np.random.default_rng(2)
     m = (rng.normal(size=(sc.n, 3)) * sc.volume).astype(np.float32)
@@ -65,6 +74,37 @@ def main():
         print(json.dumps({"kernel": kind, "n": sc.n, "ms_best": best, "ms_all": times,
                           "pairs_per_s": pairs / (best * 1e-3),
                           "tflops": FLOP[kind] * pairs / (best * 1e-3) / 1e12}), flush=True)
+
+
+def fmm(args, np, torch, mfgb, scenes):
+    sc = scenes.jittered_lattice(args.n, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=1)
+    s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
+    s.set_option("fmm", mfgb.FMM_ON)
+    s.set_option("fmm_order", 8)
+    s.set_option("solver", mfgb.SOLVER_CG)
+    rng = np.random.default_rng(2)
+    m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.volume).astype(np.float32)
+    if args.kernel == "fmm_force":
+        s.solve(200)
+    for _ in range(args.warmup):
+        s.apply_field(m) if args.kernel == "fmm_field" else s.evaluate_fitted_near_foece()
+    s.set_option("kernel_timing", 1)
+    s.reset_counters()
+    for _ in range(args.reps):
+        s.apply_field(m) if args.kernel == "fmm_field" else s.evaluate_fitted_near_foece()
+    torch.cuda.synchronize()
+    kind = "field" if args.kernel == "fmm_field" else "force"
+    whole = s.kernel_stats(kind)
+    near = s.kernel_stats("fmm_near_" + kind)
+    far = s.kernel_stats("fmm_far")
+    st = s.fmm_stats()
+    r = max(whole["launches"], 1)
+    print(json.dumps({"kernel": args.kernel, "n": sc.n, "product_ms": whole["total_ms"] / r,
+                      "near_ms": near["total_ms"] / r, "far_ms": far["total_ms"] / r,
+                      "near_pairs": st["p2p_pairs"], "m2l": st["m2l_per_product"],
+                      "near_tflops": FLOP[kind] * st["p2p_pairs"] / (near["total_ms"] / r * 1e-3) / 1e12,
+                      "effective_pairs_per_s": float(sc.n) ** 2 / (whole["total_ms"] / r * 1e-3),
+                      "fmm": st}), flush=True)
 
 
 if __name__ == "__main__":

@@ -78,3 +78,38 @@ def test_budget_enforced(mf):
         srv.step()
     assert srv.poll(a)[0] == 2
     srv.close()
+
+
+def test_fmm_request_in_the_mix(mf):
+    # A request above 65,536 particles runs as its own FMM solver (P = 6) on
+    # its own stream beside the batch; its result equals the same solver run
+    # alone with the same settings, and the small requests are unaffected.
+    import scenes
+    big = scenes.jittered_lattice(70000, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=77)
+    small = scenes_for((900, 1700), seed=51)
+    steps = 3
+    srv = mf.Server(steps_per_request=steps, dt=1e-3, rel_tol=1e-7, iters_per_step=8)
+    ids = [srv.submit(small[0]), srv.submit(big)]
+    srv.step()
+    ids.append(srv.submit(small[1]))
+    while any(srv.poll(i)[0] != 2 for i in ids):
+        srv.step()
+    st = srv.stats()
+    assert st["completed"] == 3 and st["force_pairs"] > 0
+    # the big request against a standalone FMM solver with the server's settings
+    s = mf.Solver(big.n, big.h, big.h, big.volume, big.chi, big.H0, None, None, big.pos)
+    s.set_option("solver", mf.SOLVER_CG)
+    s.set_option("rel_tol", 1e-7)
+    s.set_option("fmm", mf.FMM_ON)
+    s.set_option("fmm_order", 6)
+    s.solve(500)
+    for _ in range(steps):
+        s.advance(1e-3, 8)
+    assert s.fmm_stats()["active"] == 1
+    assert np.max(np.abs(srv.result(ids[1], "positions") - s.xyz)) < 1e-6
+    assert rel(srv.result(ids[1], "magnetic_bodyforce"), s.magnetic_bodyforce) < 1e-5
+    assert rel(srv.result(ids[1], "total_B_over_mu0"), s.total_B_over_mu0) < 1e-5
+    for k, sc in ((0, small[0]), (2, small[1])):
+        alone = run_alone(mf, sc, steps)
+        assert rel(srv.result(ids[k], "magnetic_bodyforce"), alone["magnetic_bodyforce"]) < 1e-5
+    srv.close()
