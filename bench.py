@@ -312,6 +312,7 @@ def run_ours(args, rank, world, local):
             "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
             "gpu_launches": ctr["kernel_launches"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "errors": errors, "clocks": clk,
+            "autotune": mfgb.autotune_report(),
         }
         print(json.dumps(out), flush=True)
     s.close()

@@ -98,8 +98,13 @@ typedef enum mf_option {
   MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
                                (terms of degree n < P): 4..8, default 6 (magnetic_force.cu:661) */
   MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture, default 0.5 (FMMOptions.hpp:118) */
-  MF_OPT_FMM_LEAF = 12      /* FMM leaf level: the deepest whose boxes hold at least this many
+  MF_OPT_FMM_LEAF = 12,     /* FMM leaf level: the deepest whose boxes hold at least this many
                                particles on average (default 64) */
+  MF_OPT_AUTOTUNE = 13      /* block shapes of the FP32 all-pairs launches: 0 fixed default,
+                               1 tuned (default; each new body and size class is timed once
+                               per process on the scene's own data), 2 tuned choices only when
+                               already cached.  MF_AUTOTUNE=0 in the environment makes 0 the
+                               default for handles and batches. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -215,6 +220,12 @@ typedef struct mf_kernel_stats {
   double pairs;
 } mf_kernel_stats;
 mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out);
+
+/* The autotuner's choices so far in this process, one line per (device,
+ * body, size class): the chosen block shape (threads x targets per thread /
+ * sources per tile) and the measured ms of every shape.  Writes at most cap
+ * bytes (NUL-terminated); *len gets the full length.  Not in the reference. */
+mf_status mf_autotune_report(char* buf, int64_t cap, int64_t* len);
 
 /* Shape and work of the handle's FMM (uniform octree over the current
  * positions; built on the first product after the positions change).

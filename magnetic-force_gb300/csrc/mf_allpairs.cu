@@ -1,8 +1,12 @@
 // mf_allpairs.cu -- plans, scratch and launches of the all-pairs kernel.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <type_traits>
 
 #include "mf_internal.h"
@@ -140,9 +144,19 @@ constexpr bool has_f2() {
   return std::is_same<Real, float>::value;
 }
 
-template <class Real, Body B>
+// Launch configuration: FP32 shaped bodies take shape S of kShapeTable;
+// the tensor body and FP64 keep KCfg (shape 0 only).
+template <class Real, Body B, int S, bool kShaped = std::is_same<Real, float>::value && B != Body::Tensor>
+struct LCfg : KCfg<Real, B> {};
+template <class Real, Body B, int S>
+struct LCfg<Real, B, S, true> {
+  static constexpr int TPB = kShapeTable[S].tpb, TPT = kShapeTable[S].tpt, TILE = kShapeTable[S].tile;
+  static constexpr int STAGES = 3, kOut = KCfg<Real, B>::kOut;
+};
+
+template <class Real, Body B, int S = 0>
 struct Launcher {
-  using C = KCfg<Real, B>;
+  using C = LCfg<Real, B, S>;
   using BT = typename BodyOf<Real, B>::type;
   static constexpr int TBT = C::TPB * C::TPT;
   static constexpr size_t kSmem = size_t(C::STAGES) * StageLayout<Real, C::TILE>::kBytes;
@@ -210,7 +224,13 @@ struct Launcher {
 };
 
 template <class Real>
-static void cfg_of(Body b, int* tile, int* tbt) {
+static void cfg_of(Body b, int* tile, int* tbt, int shape) {
+  if (std::is_same<Real, float>::value && shaped(b)) {
+    const Shape& sh = kShapeTable[shape];
+    *tile = sh.tile;
+    *tbt = sh.tpb * sh.tpt;
+    return;
+  }
   switch (b) {
     case Body::Field:
       *tile = KCfg<Real, Body::Field>::TILE;
@@ -245,10 +265,13 @@ static void fill_coefs(const SceneSpec& s, SceneDesc<Real>& d) {
 }
 
 template <class Real>
-mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan) {
+mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan, int shape) {
+  if (shape < 0 || shape >= kShapes || (shape != 0 && !(std::is_same<Real, float>::value && shaped(body))))
+    return fail(MF_ERR_INVALID_ARG, "build_plan: bad block shape");
   int tile = 0, tbt = 0;
-  cfg_of<Real>(body, &tile, &tbt);
+  cfg_of<Real>(body, &tile, &tbt, shape);
   plan.body = body;
+  plan.shape = shape;
   plan.host.clear();
   plan.host.reserve(specs.size());
   int64_t step = 0, tbo = 0;
@@ -292,17 +315,45 @@ mf_status refresh_plan_coefs(const std::vector<SceneSpec>& specs, Plan<Real>& pl
   return MF_OK;
 }
 
+// Shape dispatch: FP32 shaped bodies on plan.shape, everything else shape 0.
+template <class Real, Body B>
+struct Shaped {
+  static void needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
+    if constexpr (std::is_same<Real, float>::value && B != Body::Tensor) {
+      switch (plan.shape) {
+        case 1: return Launcher<Real, B, 1>::needs(plan, pd, nc);
+        case 2: return Launcher<Real, B, 2>::needs(plan, pd, nc);
+        case 3: return Launcher<Real, B, 3>::needs(plan, pd, nc);
+        default: break;
+      }
+    }
+    Launcher<Real, B, 0>::needs(plan, pd, nc);
+  }
+  static mf_status launch(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials, int32_t* counters,
+                          int32_t* err, cudaStream_t st) {
+    if constexpr (std::is_same<Real, float>::value && B != Body::Tensor) {
+      switch (plan.shape) {
+        case 1: return Launcher<Real, B, 1>::launch(plan, io, partials, counters, err, st);
+        case 2: return Launcher<Real, B, 2>::launch(plan, io, partials, counters, err, st);
+        case 3: return Launcher<Real, B, 3>::launch(plan, io, partials, counters, err, st);
+        default: break;
+      }
+    }
+    return Launcher<Real, B, 0>::launch(plan, io, partials, counters, err, st);
+  }
+};
+
 template <class Real>
 void plan_scratch_needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
   switch (plan.body) {
-    case Body::Field: Launcher<Real, Body::Field>::needs(plan, pd, nc); break;
-    case Body::Force: Launcher<Real, Body::Force>::needs(plan, pd, nc); break;
-    case Body::Tensor: Launcher<Real, Body::Tensor>::needs(plan, pd, nc); break;
+    case Body::Field: Shaped<Real, Body::Field>::needs(plan, pd, nc); break;
+    case Body::Force: Shaped<Real, Body::Force>::needs(plan, pd, nc); break;
+    case Body::Tensor: Shaped<Real, Body::Tensor>::needs(plan, pd, nc); break;
     case Body::FieldF2:
-      if constexpr (has_f2<Real>()) Launcher<float, Body::FieldF2>::needs(plan, pd, nc);
+      if constexpr (has_f2<Real>()) Shaped<float, Body::FieldF2>::needs(plan, pd, nc);
       break;
     case Body::ForceF2:
-      if constexpr (has_f2<Real>()) Launcher<float, Body::ForceF2>::needs(plan, pd, nc);
+      if constexpr (has_f2<Real>()) Shaped<float, Body::ForceF2>::needs(plan, pd, nc);
       break;
   }
 }
@@ -311,14 +362,14 @@ template <class Real>
 mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials, int32_t* counters,
                        int32_t* err, cudaStream_t st) {
   switch (plan.body) {
-    case Body::Field: return Launcher<Real, Body::Field>::launch(plan, io, partials, counters, err, st);
-    case Body::Force: return Launcher<Real, Body::Force>::launch(plan, io, partials, counters, err, st);
-    case Body::Tensor: return Launcher<Real, Body::Tensor>::launch(plan, io, partials, counters, err, st);
+    case Body::Field: return Shaped<Real, Body::Field>::launch(plan, io, partials, counters, err, st);
+    case Body::Force: return Shaped<Real, Body::Force>::launch(plan, io, partials, counters, err, st);
+    case Body::Tensor: return Shaped<Real, Body::Tensor>::launch(plan, io, partials, counters, err, st);
     case Body::FieldF2:
-      if constexpr (has_f2<Real>()) return Launcher<float, Body::FieldF2>::launch(plan, io, partials, counters, err, st);
+      if constexpr (has_f2<Real>()) return Shaped<float, Body::FieldF2>::launch(plan, io, partials, counters, err, st);
       break;
     case Body::ForceF2:
-      if constexpr (has_f2<Real>()) return Launcher<float, Body::ForceF2>::launch(plan, io, partials, counters, err, st);
+      if constexpr (has_f2<Real>()) return Shaped<float, Body::ForceF2>::launch(plan, io, partials, counters, err, st);
       break;
   }
   return fail(MF_ERR_UNSUPPORTED, "packed two-source kernels exist in FP32 only");
@@ -333,8 +384,120 @@ mf_status run_plan(const Plan<Real>& plan, const LaunchIO<Real>& io, Scratch& sc
                       scratch.err.as<int32_t>(), st);
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+namespace {
+struct TuneEntry {
+  int shape = 0;
+  float ms[kShapes] = {};
+};
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, uint32_t>, TuneEntry> g_tune;
+
+int ilog2(double v) {
+  int k = 0;
+  while (v >= 2.0 && k < 255) {
+    v *= 0.5;
+    ++k;
+  }
+  return k;
+}
+const char* body_name(Body b) {
+  switch (b) {
+    case Body::Field: return "field";
+    case Body::Force: return "force";
+    case Body::Tensor: return "tensor";
+    case Body::FieldF2: return "field_packed";
+    case Body::ForceF2: return "force_packed";
+  }
+  return "?";
+}
+}  // namespace
+
+uint32_t tune_class(const std::vector<SceneSpec>& specs) {
+  double pairs = 0;
+  for (const SceneSpec& s : specs) pairs += double(s.nt) * double(s.ns);
+  return (uint32_t(ilog2(pairs)) << 8) | uint32_t(std::min(ilog2(double(specs.size())), 255));
+}
+
+int tuned_shape(Body body, uint32_t cls) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(std::make_tuple(current_device(), int(body), cls));
+  return it == g_tune.end() ? -1 : it->second.shape;
+}
+
+Tune default_tune_mode() {
+  static const Tune mode = [] {
+    const char* e = getenv("MF_AUTOTUNE");
+    return (e && e[0] == '0') ? Tune::Off : Tune::OnMiss;
+  }();
+  return mode;
+}
+
+mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
+                     Scratch& scratch, cudaStream_t st, Tune mode) {
+  if (mode == Tune::Off || !shaped(body)) return build_plan<float>(body, specs, plan, 0);
+  const uint32_t cls = tune_class(specs);
+  const int known = tuned_shape(body, cls);
+  if (known >= 0) return build_plan<float>(body, specs, plan, known);
+  if (mode == Tune::CachedOnly) return build_plan<float>(body, specs, plan, 0);
+  TuneEntry te;
+  float best = 1e30f;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  MF_CUDA_TRY(cudaEventCreate(&e0));
+  MF_CUDA_TRY(cudaEventCreate(&e1));
+  mf_status status = MF_OK;
+  for (int s = 0; s < kShapes && status == MF_OK; ++s) {
+    Plan<float> p;
+    status = build_plan<float>(body, specs, p, s);
+    if (status != MF_OK) break;
+    status = run_plan<float>(p, io, scratch, st);  // warm-up (grows the scratch outside the timing)
+    if (status != MF_OK) break;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 2 && status == MF_OK; ++r) status = run_plan<float>(p, io, scratch, st);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) status = cuda_fail(cudaGetLastError(), "autotune timing");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    te.ms[s] = ms * 0.5f;
+    if (te.ms[s] < best) {
+      best = te.ms[s];
+      te.shape = s;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MF_TRY(status);
+  MF_TRY(scratch.check(st));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[std::make_tuple(current_device(), int(body), cls)] = te;
+  }
+  return build_plan<float>(body, specs, plan, te.shape);
+}
+
+std::string autotune_report() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string out;
+  char line[256];
+  for (const auto& kv : g_tune) {
+    const TuneEntry& e = kv.second;
+    snprintf(line, sizeof(line), "device %d %s pairs~2^%u scenes~2^%u: shape %d (%dx%d/%d) ms", std::get<0>(kv.first),
+             body_name(Body(std::get<1>(kv.first))), std::get<2>(kv.first) >> 8, std::get<2>(kv.first) & 255u,
+             e.shape, kShapeTable[e.shape].tpb, kShapeTable[e.shape].tpt, kShapeTable[e.shape].tile);
+    out += line;
+    for (int s = 0; s < kShapes; ++s) {
+      snprintf(line, sizeof(line), " %.4f", double(e.ms[s]));
+      out += line;
+    }
+    out += "\n";
+  }
+  return out;
+}
+
 #define MF_INSTANTIATE(R)                                                                                  \
-  template mf_status build_plan<R>(Body, const std::vector<SceneSpec>&, Plan<R>&);                        \
+  template mf_status build_plan<R>(Body, const std::vector<SceneSpec>&, Plan<R>&, int);                   \
   template mf_status refresh_plan_coefs<R>(const std::vector<SceneSpec>&, Plan<R>&);                      \
   template void plan_scratch_needs<R>(const Plan<R>&, size_t*, size_t*);                                  \
   template mf_status run_plan<R>(const Plan<R>&, const LaunchIO<R>&, Scratch&, cudaStream_t);             \

@@ -98,7 +98,9 @@ class Batch {
 
   // Scenes from host positions (dev == nullptr), or from device-resident
   // state (dev[s] for scene s; the descriptors' pos pointers are unused).
-  mf_status init(const mf_scene_desc* d, int n, int device, const SceneState* dev = nullptr) {
+  mf_status init(const mf_scene_desc* d, int n, int device, const SceneState* dev = nullptr,
+               Tune tune = default_tune_mode()) {
+    tune_ = tune;
     if (n <= 0 || !d) return fail(MF_ERR_INVALID_ARG, "no scenes");
     device_ = device;
     sms_ = device_sms(device);
@@ -211,9 +213,23 @@ class Batch {
     for (int p = 0; p < 2; ++p) {
       const Body fb = p ? Body::FieldF2 : Body::Field;
       const Body gb = p ? Body::ForceF2 : Body::Force;
-      if (!resid[p].empty()) MF_TRY(build_plan<float>(fb, resid[p], plan_resid_[p]));
-      if (!cgq[p].empty()) MF_TRY(build_plan<float>(fb, cgq[p], plan_cgq_[p]));
-      if (!force[p].empty()) MF_TRY(build_plan<float>(gb, force[p], plan_force_[p]));
+      // Block shapes from the autotuner, timed on these scenes (the tuning
+      // launches write the q and force scratch only).
+      LaunchIO<float> io;
+      io.tpos = pos4_.as<float4>();
+      io.spos = p ? pos2_.as<float4>() : pos4_.as<float4>();
+      io.smom = p ? mom2_.as<float4>() : mom4_.as<float4>();
+      io.corr4 = p ? corr_.as<float4>() : nullptr;
+      io.out4 = q4_.as<float4>();
+      LaunchIO<float> ig = io;
+      ig.out4 = nullptr;
+      ig.tmom = mom4_.as<float4>();
+      for (int k = 0; k < 3; ++k) ig.out[k] = fs_.as<float>() + int64_t(k) * n_alloc_;
+      if (!resid[p].empty()) {
+        MF_TRY(tuned_plan(fb, cgq[p], plan_cgq_[p], io, scr_, st_, tune_));
+        MF_TRY(build_plan<float>(fb, resid[p], plan_resid_[p], plan_cgq_[p].shape));
+      }
+      if (!force[p].empty()) MF_TRY(tuned_plan(gb, force[p], plan_force_[p], ig, scr_, st_, tune_));
       for (const Plan<float>* pl : {&plan_resid_[p], &plan_cgq_[p], &plan_force_[p]}) {
         if (pl->n_scenes == 0) continue;
         size_t pd = 0, nc = 0;
@@ -507,6 +523,7 @@ class Batch {
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
   Plan<float> plan_resid_[2], plan_cgq_[2], plan_force_[2];  // [0] exact branches, [1] packed
+  Tune tune_ = Tune::OnMiss;
   Scratch scr_;
   CellList cells_;
   mf_counters ctr_ = {};
@@ -804,7 +821,10 @@ class Server {
     }
     batch_.reset(new Batch());
     batch_->device_ = cfg_.device;
-    MF_TRY(batch_->init(descs.data(), int(descs.size()), cfg_.device, st.data()));
+    // Rebatching happens between timesteps: use tuned shapes already cached,
+    // never time new ones on the request path.
+    MF_TRY(batch_->init(descs.data(), int(descs.size()), cfg_.device, st.data(),
+                        default_tune_mode() == Tune::Off ? Tune::Off : Tune::CachedOnly));
     MF_TRY(batch_->solve(500, cfg_.rel_tol, true));
     ++stats_.rebatches;
     dirty_ = false;

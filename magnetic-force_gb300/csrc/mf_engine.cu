@@ -8,6 +8,7 @@
 // Hot products go through the all-pairs kernel (mf_allpairs.cuh); vector
 // updates and FP64 inner products through mf_vec.cuh.  Published results are
 // device SoA float arrays like the reference's cuda_abstract_vector members.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -479,6 +480,13 @@ class Engine final : public EngineBase {
         fmm_cfg_.leaf_min = int(v);
         fmm_dirty_ = true;
         return MF_OK;
+      case MF_OPT_AUTOTUNE:
+        if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "autotune mode must be 0, 1 or 2");
+        if (Tune(int(v)) != tune_) {
+          tune_ = Tune(int(v));
+          MF_TRY(build_plans());
+        }
+        return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -499,6 +507,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_ORDER: *v = fmm_cfg_.order; return MF_OK;
       case MF_OPT_FMM_THETA: *v = fmm_cfg_.theta; return MF_OK;
       case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
+      case MF_OPT_AUTOTUNE: *v = double(int(tune_)); return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -527,6 +536,7 @@ class Engine final : public EngineBase {
   FmmConfig fmm_cfg_;
   bool fmm_dirty_ = true;
   int fmm_mode_ = 0;
+  Tune tune_ = default_tune_mode();
   int64_t fmm_field_products_ = 0, fmm_force_products_ = 0;
   bool plans_ready_ = false;
   bool rext_zero_ = true;
@@ -606,22 +616,47 @@ class Engine final : public EngineBase {
     // FP32 uses the packed two-source kernels; FP64 the exact-branch kernels.
     const Body fb = (kF32 && np_ >= kPackedFieldMin) ? Body::FieldF2 : Body::Field;
     const Body gb = (kF32 && np_ >= kPackedForceMin) ? Body::ForceF2 : Body::Force;
-    MF_TRY(build_plan<Real>(fb, {s}, plan_resid_));
+    // FP32: block shapes from the autotuner, timed on this scene's own
+    // positions (the tuning launches write scratch vectors only).
+    int fshape = 0, gshape = 0;
+    if constexpr (kF32) {
+      if (tune_ != Tune::Off) {
+        LaunchIO<Real> io;
+        io.tpos = pos4();
+        io.spos = fb == Body::FieldF2 ? pos2_.template as<float4>() : pos4();
+        io.smom = fb == Body::FieldF2 ? mom2_.template as<float4>() : v4(V_B);
+        io.corr4 = fb == Body::FieldF2 ? corr_.template as<float4>() : nullptr;
+        io.out4 = v4(V_DD);
+        Plan<Real> tp;
+        MF_TRY(tuned_plan(fb, {base}, tp, io, scr_, st_, tune_));
+        fshape = tp.shape;
+        LaunchIO<Real> ig;
+        ig.tpos = pos4();
+        ig.tmom = mom4();
+        ig.spos = gb == Body::ForceF2 ? pos2_.template as<float4>() : pos4();
+        ig.smom = gb == Body::ForceF2 ? mom2_.template as<float4>() : mom4();
+        ig.corr4 = gb == Body::ForceF2 ? corr_.template as<float4>() : nullptr;
+        for (int k = 0; k < 3; ++k) ig.out[k] = pubr(MF_Q_FORCE, k);
+        MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_));
+        gshape = tp.shape;
+      }
+    }
+    MF_TRY(build_plan<Real>(fb, {s}, plan_resid_, fshape));
     // gradient g = c G(r) - r            (D_transpose, :1281-1284)
     // D(d) = c G(d) - d                  (D, :1275-1278)
     s = base;
     s.scale = c;
     s.coef_add = -1.0;
-    MF_TRY(build_plan<Real>(fb, {s}, plan_grad_));
-    MF_TRY(build_plan<Real>(fb, {s}, plan_dd_));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_grad_, fshape));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_dd_, fshape));
     // CG: q = p - c G(p)
     s = base;
     s.scale = -c;
     s.coef_add = 1.0;
-    MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_));
+    MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_, fshape));
     s = base;
-    MF_TRY(build_plan<Real>(gb, {s}, plan_force_));
-    MF_TRY(build_plan<Real>(fb, {base}, plan_apply_));  // G(m) alone
+    MF_TRY(build_plan<Real>(gb, {s}, plan_force_, gshape));
+    MF_TRY(build_plan<Real>(fb, {base}, plan_apply_, fshape));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
     return MF_OK;
@@ -1398,6 +1433,17 @@ mf_status mf_get_fmm_stats(mf_solver* s, mf_fmm_stats* out) {
 
 mf_status mf_apply_field(mf_solver* s, const float* moments, int32_t layout, int32_t where, float* out) {
   return guarded(s, [&](EngineBase& e) { return e.apply_field(moments, layout, where, out); });
+}
+
+mf_status mf_autotune_report(char* buf, int64_t cap, int64_t* len) {
+  const std::string r = mfgb::autotune_report();
+  if (len) *len = int64_t(r.size());
+  if (buf && cap > 0) {
+    const size_t n = std::min<size_t>(r.size(), size_t(cap - 1));
+    memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
+  return MF_OK;
 }
 
 mf_status mf_probe_fp32_peak(double* tflops) {

@@ -122,6 +122,17 @@ struct KCfg<double, Body::Tensor> {
   static constexpr int TPB = 128, TPT = 1, TILE = 128, STAGES = 3, kOut = 6;
 };
 
+// Block shapes of the FP32 all-pairs launches (the exact-branch Field / Force
+// bodies and the packed FieldF2 / ForceF2 ones): threads per CTA, targets per
+// thread, sources per staged tile.  Shape 0 is the default (the KCfg above);
+// the autotuner picks among all of them per body and size class.
+struct Shape {
+  int tpb, tpt, tile;
+};
+constexpr int kShapes = 4;
+constexpr Shape kShapeTable[kShapes] = {{256, 2, 256}, {128, 2, 256}, {256, 1, 256}, {128, 4, 128}};
+inline bool shaped(Body b) { return b != Body::Tensor; }
+
 // One scene of a launch before it is laid out in step space.  nt > 0, ns > 0.
 struct SceneSpec {
   int64_t t_off, nt, s_off, ns;
@@ -137,6 +148,7 @@ struct SceneSpec {
 template <class Real>
 struct Plan {
   Body body = Body::Field;
+  int shape = 0;  // FP32 shaped bodies: index into kShapeTable
   int64_t total_steps = 0;
   int64_t total_tb = 0;
   int32_t n_scenes = 0;
@@ -146,8 +158,9 @@ struct Plan {
 };
 
 // Build (and synchronously upload) a plan.  Empty scenes are rejected.
+// `shape` applies to FP32 shaped bodies (0 otherwise).
 template <class Real>
-mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan);
+mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan, int shape = 0);
 // Re-upload a plan whose per-scene coefficients (scale, coef_add*, cvec) changed.
 template <class Real>
 mf_status refresh_plan_coefs(const std::vector<SceneSpec>& specs, Plan<Real>& plan);
@@ -197,8 +210,30 @@ template <class Real>
 mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials,
                        int32_t* counters, int32_t* err, cudaStream_t st);
 
+// Builds an FP32 plan with the autotuned block shape.  On the first launch of
+// a (device, body, size class) every shape is timed on this plan's own data
+// (`io`, whose outputs are overwritten): one warm-up and two timed launches
+// each, CUDA events on `st`; the fastest is cached.  Off, or a body without
+// shapes, builds shape 0; CachedOnly uses a cached choice and never times.
+enum class Tune { Off = 0, OnMiss = 1, CachedOnly = 2 };
+mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
+                     Scratch& scratch, cudaStream_t st, Tune mode);
+// Default tuning mode of new handles and batches: OnMiss unless the
+// environment sets MF_AUTOTUNE=0.
+Tune default_tune_mode();
+
 int device_sms(int device);
 int current_device();
+
+// ---------------------------------------------------------------------------
+// Autotuner of the block shapes (mf_allpairs.cu)
+// ---------------------------------------------------------------------------
+// Size class of a launch: log2 of its pairs and of its scene count.
+uint32_t tune_class(const std::vector<SceneSpec>& specs);
+// Shape for (device, body, class): the cached choice, or -1 when not tuned yet.
+int tuned_shape(Body body, uint32_t cls);
+// Text table of the tuned choices (device, body, class, ms per shape).
+std::string autotune_report();
 
 // ---------------------------------------------------------------------------
 // Uniform-grid cell lists and the near-field correction pass (mf_cells.cu)

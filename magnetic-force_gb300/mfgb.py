@@ -40,7 +40,7 @@ Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyfor
      "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
        "crit_size": 6, "check_interval": 7, "kernel_timing": 8, "fmm": 9, "fmm_order": 10, "fmm_theta": 11,
-       "fmm_leaf": 12}
+       "fmm_leaf": 12, "autotune": 13}
 FMM_AUTO, FMM_ON, FMM_OFF = 0, 1, 2
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
@@ -123,6 +123,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_probe_fp32_peak": (i32, [ctypes.POINTER(f64)]),
         "mf_get_fmm_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
         "mf_apply_field": (i32, [vp, vp, i32, i32, vp]),
+        "mf_autotune_report": (i32, [vp, i64, ctypes.POINTER(i64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -498,6 +499,15 @@ class Server:
         s = mf_server_stats()
         check(load().mf_server_get_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in mf_server_stats._fields_}
+
+
+def autotune_report() -> list[str]:
+    """The autotuner's block-shape choices so far in this process."""
+    n = ctypes.c_int64(0)
+    check(load().mf_autotune_report(None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    check(load().mf_autotune_report(buf, n.value + 1, ctypes.byref(n)))
+    return [ln for ln in buf.value.decode().splitlines() if ln]
 
 
 def probe_fp32_peak() -> float:

@@ -213,3 +213,24 @@ def test_counters(mf):
     assert c["field_products"] == it + 1
     assert c["field_pairs"] == (it + 1) * 1024 * 1024
     assert c["force_pairs"] == 1024 * 1024
+
+
+def test_autotuned_shapes_match_default(mf):
+    # Every block shape computes the same sums (only the FP32 order of the
+    # per-tile partial sums differs): tuned and fixed-shape handles agree, and
+    # both meet the oracle bar.
+    import scenes
+    sc = scenes.jittered_lattice(20000, "sphere", radius=0.5, chi=2.0, seed=12)
+    out = {}
+    for mode in (0, 1):
+        s = make(mf, sc)
+        s.set_option("autotune", mode)
+        s.set_option("solver", mf.SOLVER_CG)
+        s.solve(200)
+        s.evaluate_fitted_near_foece()
+        out[mode] = (s.total_B_over_mu0, s.magnetic_bodyforce)
+        assert s.get_option("autotune") == mode
+    assert rel(out[1][0], out[0][0]) < 1e-6
+    assert rel(out[1][1], out[0][1]) < 1e-6
+    rep = mf.autotune_report()
+    assert any("field_packed" in ln for ln in rep) and any("force_packed" in ln for ln in rep)
