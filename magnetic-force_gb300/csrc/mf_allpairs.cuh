@@ -30,6 +30,10 @@
 
 namespace mfgb {
 
+// The fitted force curves for the FP32 exact-branch body (staged into shared
+// memory by each CTA).
+static __constant__ float c_fit_ap[40] = MF_FITTED_CURVE_TABLE;
+
 template <class Real>
 struct SceneDesc {
   int64_t t_off, nt;     // target index range
@@ -135,7 +139,10 @@ struct FieldBody : RecordItems<Real> {
                               const PairConsts<Real>& pc, Acc& acc) {
     const R4& sp = it.p;
     const R4& sm = it.m;
-    field_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc.v, acc.v + 3);
+    if constexpr (sizeof(Real) == 4)
+      field_pair_sel(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc.v, acc.v + 3);
+    else
+      field_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, pc, acc.v, acc.v + 3);
   }
   __device__ static void tile_out(const Acc& acc, Real* o) {
     const Real c = Real(kInv4Pi);
@@ -204,7 +211,10 @@ struct ForceBody : RecordItems<Real> {
                               const PairConsts<Real>& pc, Acc& acc) {
     const R4& sp = it.p;
     const R4& sm = it.m;
-    force_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc.v);
+    if constexpr (sizeof(Real) == 4)
+      force_pair_sel(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc.v);
+    else
+      force_pair<Real>(t.x - sp.x, t.y - sp.y, t.z - sp.z, sm.x, sm.y, sm.z, t.mx, t.my, t.mz, pc, acc.v);
   }
   __device__ static void tile_out(const Acc& acc, Real* o) {
     const Real c = Real(kForceK);
@@ -415,6 +425,7 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ int s_flag;
+  __shared__ float s_fit[40];
 
   const int tid = threadIdx.x;
   const int64_t T = a.total_steps;
@@ -437,6 +448,7 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
     for (int s = 0; s < STAGES; ++s) mbar_init(&full_bar[s], 1);
     fence_mbar_init();
   }
+  if (tid < 40) s_fit[tid] = c_fit_ap[tid];
   __syncthreads();
 
   // Producer (thread 0): stage the source tile of step k into stage s.
@@ -491,7 +503,8 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
     const int s = int(u % STAGES);
     const uint32_t parity = uint32_t((u / STAGES) & 1);
     const SceneDesc<Real>& sc = a.scenes[si];
-    const PairConsts<Real> pc = sc.pc;
+    PairConsts<Real> pc = sc.pc;
+    pc.tbl = s_fit;
 
     const bool ok = mbar_wait_bounded(&full_bar[s], parity);
     if (__syncthreads_or(!ok)) {

@@ -39,6 +39,9 @@ struct PairConsts {
   Real ih4_over_k;   // 1/(h^4 K): scales the fitted curves into the K-free form
   Real near2_field;  // (2h)^2: field pairs closer than this take the SPH branch
   Real near2_force;  // (4h)^2: force pairs at or inside this take the fitted branch
+  // FP32 kernels: the fitted-curve table in shared memory (set by the kernel
+  // in its own copy; null in stored scene tables).
+  const float* tbl;
 };
 
 template <class Real>
@@ -49,6 +52,7 @@ __host__ __device__ inline PairConsts<Real> make_pair_consts(double h) {
   k.ih4_over_k = Real(1.0 / (h * h * h * h * kForceK));
   k.near2_field = Real(4.0 * h * h);
   k.near2_force = Real(16.0 * h * h);
+  k.tbl = nullptr;
   return k;
 }
 
@@ -316,6 +320,47 @@ __device__ __forceinline__ void force_near_coeffs_fast(float r2, const float* __
    -6.24199554212217e-07f, 4.91807818904985e-07f,  3.79927162333632e-10f,  -6.26368404962679e-09f, \
    3.94760528277489e-08f,  -1.13580541622200e-07f, 1.27491333574323e-07f,  7.33485346367840e-10f,  \
    -9.58855788627803e-09f, 4.37085309763591e-08f,  -7.48004594092261e-08f, 2.34161209605651e-08f}
+
+// FP32 exact pair forms without a branch: the far coefficients and the fast
+// near coefficients above are both evaluated and selected by the radius, so
+// warps whose lanes straddle the near radius do not diverge.  Same
+// mathematics as field_pair / force_pair (the far value at r = 0 is infinite
+// and discarded by the select).  The force needs k.tbl.
+__device__ __forceinline__ void field_pair_sel(float dx, float dy, float dz, float sx, float sy, float sz,
+                                               const PairConsts<float>& k, float* s1, float* s2) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  float al, be;
+  field_near_coeffs_fast(r2, k.inv_h, k.ih3, al, be);
+  const float ri = rsqrt_approx(r2), ri2 = ri * ri, ri3 = ri2 * ri;
+  const bool far = r2 >= k.near2_field;
+  const float beta = far ? ri3 : be;
+  const float alpha = far ? ri3 * ri2 : al;
+  const float t = (dx * sx + dy * sy + dz * sz) * alpha;
+  s1[0] += dx * t;
+  s1[1] += dy * t;
+  s1[2] += dz * t;
+  s2[0] += sx * beta;
+  s2[1] += sy * beta;
+  s2[2] += sz * beta;
+}
+
+__device__ __forceinline__ void force_pair_sel(float dx, float dy, float dz, float sx, float sy, float sz, float mx,
+                                               float my, float mz, const PairConsts<float>& k, float* f) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  const float ds = dx * sx + dy * sy + dz * sz;
+  const float dm = dx * mx + dy * my + dz * mz;
+  const float sm = sx * mx + sy * my + sz * mz;
+  float Pn, Qn;
+  force_near_coeffs_fast(r2, k.tbl, k.inv_h, k.ih4_over_k, Pn, Qn);
+  const float ri = rsqrt_approx(r2), ri2 = ri * ri, ri5 = ri2 * ri2 * ri;
+  const bool far = r2 > k.near2_force;
+  const float P = far ? ri5 : Pn;
+  const float Q = far ? -5.f * ri5 * ri2 : Qn;
+  const float u = P * ds, v = P * dm, w = P * sm + Q * ds * dm;
+  f[0] += dx * w + mx * u + sx * v;
+  f[1] += dy * w + my * u + sy * v;
+  f[2] += dz * w + mz * u + sz * v;
+}
 
 // Correction of one near field pair (r^2 < near2): exact minus clamped,
 // accumulated as s1 (d (d.m) dalpha) and s2 (m dbeta) like the packed loop.
