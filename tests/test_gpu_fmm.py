@@ -145,3 +145,41 @@ def test_bad_fmm_options(mf, sphere40k):
                    ("fmm_leaf", 0)):
         with pytest.raises(mf.MFError):
             s.set_option(key, v)
+
+
+def _raw_scene(pos, h, chi=1.0):
+    import scenes
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    return scenes.Scene(pos=pos, h=h, volume=h ** 3 / 8, chi=chi, H0=(0.0, 0.0, 1.0), spacing=h / 2, meta={})
+
+
+@pytest.mark.parametrize("kind", ["plane", "line", "two_clusters", "tiny"])
+def test_degenerate_geometry(mf, kind):
+    # Flat and thin bounding boxes, far-apart clusters (mostly empty grid) and
+    # a scene smaller than one leaf: the FMM still equals all-pairs to its
+    # truncation error.
+    rng = np.random.default_rng(17)
+    if kind == "plane":
+        g = np.stack(np.meshgrid(np.arange(160), np.arange(160), indexing="ij"), -1).reshape(-1, 2) * 0.01
+        pos = np.c_[g + rng.uniform(-0.002, 0.002, g.shape), np.zeros(len(g))]
+        h = 0.02
+    elif kind == "line":
+        x = np.arange(6000) * 0.01
+        pos = np.c_[x, rng.uniform(-0.001, 0.001, (6000, 2))]
+        h = 0.02
+    elif kind == "two_clusters":
+        a = rng.uniform(-0.1, 0.1, (15000, 3))
+        pos = np.r_[a, a + np.array([3.0, 0.5, -1.0])]
+        h = 0.016
+    else:
+        pos = rng.uniform(0, 0.2, (50, 3))
+        h = 0.05
+    sc = _raw_scene(pos, h)
+    m = moments(sc, seed=3)
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=8, fmm_leaf=32)
+    got = s.apply_field(m)
+    assert np.all(np.isfinite(got))
+    st = s.fmm_stats()
+    assert st["active"] == 1 and st["occupied_leaves"] >= 1
+    s.set_option("fmm", mf.FMM_OFF)
+    assert rel(got, s.apply_field(m)) < 1e-5
