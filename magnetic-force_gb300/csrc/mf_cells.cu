@@ -464,8 +464,8 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
   MF_TRY(grids_.reserve(sizeof(CellGrid) * size_t(ns)));
   MF_CUDA_TRY(cudaMemcpyAsync(grids_.ptr, host_grids_.data(), sizeof(CellGrid) * size_t(ns), cudaMemcpyHostToDevice,
                               st));
-  MF_TRY(cell_start_.reserve(sizeof(int32_t) * size_t(cells + 1)));
-  MF_TRY(cursor_.reserve(sizeof(int32_t) * size_t(cells + 1)));
+  MF_TRY(cell_start_.reserve_slack(sizeof(int32_t) * size_t(cells + 1)));
+  MF_TRY(cursor_.reserve_slack(sizeof(int32_t) * size_t(cells + 1)));
   MF_TRY(perm_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(perm_tmp_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(cell_of_.reserve(sizeof(int32_t) * size_t(n_total_)));

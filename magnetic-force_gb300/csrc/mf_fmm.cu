@@ -844,14 +844,14 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   const int64_t ncell = leaf.nbox;
 
   // Bin.
-  MF_TRY(occ_.reserve(size_t(nbox_total) * sizeof(int32_t)));
+  MF_TRY(occ_.reserve_slack(size_t(nbox_total) * sizeof(int32_t)));
   int32_t* occ = occ_.as<int32_t>();
   int32_t* cnt = occ + leaf.box_off;
   MF_TRY(cell_of_.reserve(size_t(n) * sizeof(int32_t)));
-  MF_TRY(start_.reserve(size_t(ncell + 1) * sizeof(int32_t)));
-  MF_TRY(cursor_.reserve(size_t(ncell + 1) * sizeof(int32_t)));
-  MF_TRY(perm_tmp_.reserve(size_t(n + ncell + 2) * sizeof(int32_t)));
-  MF_TRY(perm_.reserve(size_t(n + ncell + 2) * sizeof(int32_t)));
+  MF_TRY(start_.reserve_slack(size_t(ncell + 1) * sizeof(int32_t)));
+  MF_TRY(cursor_.reserve_slack(size_t(ncell + 1) * sizeof(int32_t)));
+  MF_TRY(perm_tmp_.reserve_slack(size_t(n + ncell + 2) * sizeof(int32_t)));
+  MF_TRY(perm_.reserve_slack(size_t(n + ncell + 2) * sizeof(int32_t)));
   MF_CUDA_TRY(cudaMemsetAsync(cnt, 0, size_t(ncell) * sizeof(int32_t), st));
   k_fmm_count<<<blocks_for(n), 256, 0, st>>>(pos4, n, leaf, cell_of_.as<int32_t>(), cnt);
   k_fmm_scan<<<1, 1024, 0, st>>>(cnt, ncell, start_.as<int32_t>());
@@ -866,8 +866,8 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   // Slots: every box padded to an even count, so at most n + ncell; the
   // kernels read the exact count (start[ncell]) on the device.
   n_slots_ = n + ncell + 1;
-  MF_TRY(pos2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
-  MF_TRY(mom2s_.reserve(size_t(n_slots_ + 2) * sizeof(float4)));
+  MF_TRY(pos2s_.reserve_slack(size_t(n_slots_ + 2) * sizeof(float4)));
+  MF_TRY(mom2s_.reserve_slack(size_t(n_slots_ + 2) * sizeof(float4)));
   k_fmm_gather_pairs<<<blocks_for(n_slots_ / 2), 256, 0, st>>>(perm_.as<int32_t>(), pos4, start_.as<int32_t>() + ncell,
                                                                 pos2s_.as<float4>(), 1, nullptr);
   MF_CUDA_TRY(cudaGetLastError());
@@ -959,7 +959,7 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
       taylor_inv_r(R, Q + 1, D);
       for (int g = 0; g < NG; ++g) host_dt_[size_t(kv.second) * NG + g] = float(D[size_t(g)]);
     }
-    MF_TRY(dtab_.reserve(std::max<size_t>(1, host_dt_.size()) * sizeof(float)));
+    MF_TRY(dtab_.reserve_slack(std::max<size_t>(1, host_dt_.size()) * sizeof(float)));
     if (!host_dt_.empty())
       MF_CUDA_TRY(cudaMemcpyAsync(dtab_.ptr, host_dt_.data(), host_dt_.size() * sizeof(float), cudaMemcpyHostToDevice, st));
     host_dkey_ = dkey;
@@ -970,9 +970,9 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
     host_rows_ = std::move(rows);
     host_lofs_ = list_off_;
     host_lofs_.insert(host_lofs_.end(), list_cnt_.begin(), list_cnt_.end());
-    MF_TRY(lists_.reserve(std::max<size_t>(1, host_list_.size()) * sizeof(int4)));
-    MF_TRY(rows_.reserve(std::max<size_t>(1, host_rows_.size()) * sizeof(int4)));
-    MF_TRY(lofs_.reserve(host_lofs_.size() * sizeof(int64_t)));
+    MF_TRY(lists_.reserve_slack(std::max<size_t>(1, host_list_.size()) * sizeof(int4)));
+    MF_TRY(rows_.reserve_slack(std::max<size_t>(1, host_rows_.size()) * sizeof(int4)));
+    MF_TRY(lofs_.reserve_slack(host_lofs_.size() * sizeof(int64_t)));
     if (!host_list_.empty())
       MF_CUDA_TRY(cudaMemcpyAsync(lists_.ptr, host_list_.data(), host_list_.size() * sizeof(int4),
                                   cudaMemcpyHostToDevice, st));
@@ -997,9 +997,9 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
     chunks_[size_t(l)] = int32_t(ch);
     lpart = std::max(lpart, ch * NC * v.nbox);
   }
-  MF_TRY(mcoef_.reserve(size_t(NC) * size_t(nbox_total) * sizeof(float)));
-  MF_TRY(lcoef_.reserve(size_t(NC) * size_t(nbox_total) * sizeof(float)));
-  MF_TRY(lpart_.reserve(size_t(lpart) * sizeof(float)));
+  MF_TRY(mcoef_.reserve_slack(size_t(NC) * size_t(nbox_total) * sizeof(float)));
+  MF_TRY(lcoef_.reserve_slack(size_t(NC) * size_t(nbox_total) * sizeof(float)));
+  MF_TRY(lpart_.reserve_slack(size_t(lpart) * sizeof(float)));
 
   // Statistics, counted on the device and read back lazily (stats()).
   MF_TRY(stat_.reserve(4 * sizeof(unsigned long long)));

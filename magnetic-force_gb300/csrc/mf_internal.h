@@ -62,6 +62,10 @@ struct DevBuf {
   // Ensure at least `want` bytes.  keep: preserve the old contents on growth;
   // zero: clear bytes beyond the preserved prefix.
   mf_status reserve(size_t want, bool keep = false, bool zero = false);
+  // Same, with a quarter of headroom when it has to grow: for buffers sized
+  // by the particles' current extent (cell and box grids), which change a
+  // little every timestep and would otherwise reallocate often.
+  mf_status reserve_slack(size_t want) { return want <= bytes ? MF_OK : reserve(want + want / 4 + 256); }
   template <class T>
   T* as() const {
     return static_cast<T*>(ptr);
