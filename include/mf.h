@@ -290,6 +290,24 @@ mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h
 mf_status mf_release_scratch(void);
 
 /* ---------------------------------------------------------------------- */
+/* FMM matrix over a source set and a target set: the replacement of       */
+/* fmmtl::kernel_matrix<DipoleBSpherical>(kernel, sources, targets) and    */
+/* its operator* (fmmtl/KernelMatrix.hpp:26-164, :127-131).  The octree,   */
+/* lists and near-field cell list are built once at creation; each product */
+/* takes new charges.  Host AoS float arrays.                              */
+/* ---------------------------------------------------------------------- */
+typedef struct mf_fmm mf_fmm;
+/* targets may be NULL (nt ignored): the targets are the sources.  order is
+ * P as the reference counts it (4..8), theta the acceptance aperture,
+ * leaf_min the mean particles per leaf box. */
+mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, int64_t nt, float h, int32_t order,
+                        double theta, int32_t leaf_min, int32_t device, mf_fmm** out);
+mf_status mf_fmm_destroy(mf_fmm* f);
+/* results[nt][3] = sum_j DipoleBKernel{h}(targets_i, sources_j) * charges_j */
+mf_status mf_fmm_field(mf_fmm* f, const float* charges, float* results);
+mf_status mf_fmm_get_stats(mf_fmm* f, mf_fmm_stats* out);
+
+/* ---------------------------------------------------------------------- */
 /* Batched scenes.  Not in the reference, which solves one object per       */
 /* cuda_magnet_cgOptimizer instance: here many independent objects (each   */
 /* the reference's problem with its own particles, h, V, chi and uniform    */

@@ -848,7 +848,7 @@ class Engine final : public EngineBase {
     if constexpr (kF32) {
       MF_TRY(ensure_cells());
       if (fmm_dirty_) {
-        MF_TRY(fmm_.build(pos4(), np_, h_, cells_.bbox(0), fmm_cfg_, st_));
+        MF_TRY(fmm_.build(pos4(), np_, nullptr, 0, h_, cells_.bbox(0), fmm_cfg_, st_));
         ctr_.kernel_launches += 8;
         fmm_dirty_ = false;
       }

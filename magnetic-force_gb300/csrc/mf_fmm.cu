@@ -30,6 +30,9 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <memory>
+#include <new>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -155,10 +158,10 @@ __global__ void k_fmm_gather_pairs(const int32_t* __restrict__ perm, const float
 }
 
 // Executed near-field pairs (real targets x real sources) and the largest leaf.
-__global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, const int4* __restrict__ rows,
-                                int n_rows, unsigned long long* __restrict__ out) {
+__global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, const int32_t* __restrict__ tcnt,
+                                const int4* __restrict__ rows, int n_rows, unsigned long long* __restrict__ out) {
   for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < lv.nbox; c += int64_t(gridDim.x) * blockDim.x) {
-    const int32_t n = cnt[c];
+    const int32_t n = tcnt[c];
     if (n == 0) continue;
     const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
     unsigned long long s = 0;
@@ -176,15 +179,15 @@ __global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, co
   }
 }
 
-// Multipole-to-local translations of one level (occupied target and source),
-// one warp per target box.
-__global__ void k_fmm_m2l_stats(FmmLevel lv, const int32_t* __restrict__ occ, const int4* __restrict__ list,
-                                const int64_t* __restrict__ off, const int64_t* __restrict__ cnt,
-                                unsigned long long* __restrict__ out) {
+// Multipole-to-local translations of one level (target box holding targets,
+// source box holding sources), one warp per target box.
+__global__ void k_fmm_m2l_stats(FmmLevel lv, const int32_t* __restrict__ occ, const int32_t* __restrict__ tocc,
+                                const int4* __restrict__ list, const int64_t* __restrict__ off,
+                                const int64_t* __restrict__ cnt, unsigned long long* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
   for (int64_t b = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); b < lv.nbox; b += warps) {
-    if (occ[lv.box_off + b] == 0) continue;
+    if (tocc[lv.box_off + b] == 0) continue;
     const int x = int(b % lv.nx), y = int((b / lv.nx) % lv.ny), z = int(b / (int64_t(lv.nx) * lv.ny));
     const int cls = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
     unsigned k = 0;
@@ -396,7 +399,8 @@ __device__ __forceinline__ void m2l_apply(float* acc, const float* M, const floa
 
 struct M2LArgs {
   FmmLevel lv;
-  const int32_t* occ;
+  const int32_t* occ;   // sources per box
+  const int32_t* tocc;  // targets per box
   const float* M;     // this level's multipoles (NC rows of nbox)
   float* Lp;          // [chunks][NC][nbox] partial locals
   const int4* list;   // (dx, dy, dz, row of dtab)
@@ -430,7 +434,7 @@ __global__ void __launch_bounds__(128) k_fmm_m2l(const M2LArgs p) {
   const int tx = 2 * hi + (cls & 1), ty = 2 * hj + ((cls >> 1) & 1), tz = 2 * int(hk) + (cls >> 2);
   if (tx >= lv.nx || ty >= lv.ny || tz >= lv.nz) return;
   const int64_t tb = (int64_t(tz) * lv.ny + ty) * lv.nx + tx;
-  if (p.occ[lv.box_off + tb] == 0) return;
+  if (p.tocc[lv.box_off + tb] == 0) return;
   const int64_t n = p.list_cnt[cls];
   const int64_t e0 = p.list_off[cls] + n * ch / p.chunks;
   const int64_t e1 = p.list_off[cls] + n * (ch + 1) / p.chunks;
@@ -456,6 +460,7 @@ __global__ void __launch_bounds__(128) k_fmm_m2l(const M2LArgs p) {
 
 // Locals of a level: the M2L partials plus the parent's locals shifted to the
 // child centre,  L^c_beta += 2^(-2-|beta|) sum_delta L^p_(beta+delta) v_c^delta / delta!.
+// `occ` counts targets: boxes without targets need no locals.
 template <int Q>
 __global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_t* __restrict__ occ,
                           const float* __restrict__ Lpart, int chunks, float* __restrict__ L,
@@ -504,9 +509,12 @@ constexpr int kP2PSmem = kP2PStages * 2 * kP2PTile * int(sizeof(float4));
 
 struct P2PArgs {
   FmmLevel lv;
-  const int32_t* start;
+  const int32_t* start;   // sources: box starts (even-padded slots), counts, slot -> index
   const int32_t* cnt;
   const int32_t* perm;
+  const int32_t* tstart;  // targets: box starts, counts, slot -> index (the same arrays
+  const int32_t* tcnt;    //   when the targets are the sources)
+  const int32_t* tperm;
   const float4* pos2s;
   const float4* mom2s;
   const float* L;     // leaf locals, NC rows of nbox
@@ -528,11 +536,11 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   if (p.done && *p.done != 0.0) return;
   const FmmLevel& lv = p.lv;
   const int64_t c = blockIdx.x;
-  const int32_t n = p.cnt[c];
+  const int32_t n = p.tcnt[c];
   if (n == 0) return;
   const int tid = threadIdx.x;
   const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
-  const int32_t st0 = p.start[c];
+  const int32_t st0 = p.tstart[c];
   for (int k = tid; k < NC; k += kP2PThreads) s_L[k] = p.L[int64_t(k) * lv.nbox + c];
   auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + s * 2 * kP2PTile; };
   auto stage_mom = [&](int s) { return stage_pos(s) + kP2PTile; };
@@ -584,7 +592,7 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   int fail_k = 0, fail_ns = 0;
   for (int t0 = 0; t0 < n && !failed; t0 += kP2PThreads) {
     const bool act = t0 + tid < n;
-    const int32_t i = p.perm[st0 + (act ? t0 + tid : 0)];
+    const int32_t i = p.tperm[st0 + (act ? t0 + tid : 0)];
     typename Body::TData td;
     Body::load(a, i, td);
     float run[3] = {0.f, 0.f, 0.f}, cmp[3] = {0.f, 0.f, 0.f};
@@ -759,10 +767,13 @@ void taylor_inv_r(const double R[3], int nmax, std::vector<double>& D) {
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox, const FmmConfig& cfg,
-                     cudaStream_t st) {
+mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t nt, double h, const double* bbox,
+                     const FmmConfig& cfg, cudaStream_t st) {
   if (n <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no particles");
-  if (n >= (int64_t(1) << 30)) return fail(MF_ERR_INVALID_ARG, "fmm: too many particles");
+  if (n >= (int64_t(1) << 30) || nt >= (int64_t(1) << 30)) return fail(MF_ERR_INVALID_ARG, "fmm: too many particles");
+  if (tpos4 && nt <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no targets");
+  separate_ = tpos4 != nullptr;
+  nt_ = separate_ ? nt : n;
   if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 8]");
   if (!(cfg.theta > 0.0 && cfg.theta <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm: theta must be in (0, 1]");
   if (cfg.leaf_min < 1) return fail(MF_ERR_INVALID_ARG, "fmm: leaf_min must be >= 1");
@@ -863,6 +874,30 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   for (int l = L - 1; l >= 0; --l)
     k_fmm_occ_up<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(lv_[size_t(l + 1)], lv_[size_t(l)], occ);
   MF_CUDA_TRY(cudaGetLastError());
+  // Separate targets: their own binning into the same leaf boxes (lists in
+  // increasing index, padded like the sources), and their own occupancy.
+  if (separate_) {
+    MF_TRY(tocc_.reserve_slack(size_t(nbox_total) * sizeof(int32_t)));
+    int32_t* tocc = tocc_.as<int32_t>();
+    int32_t* tcnt = tocc + leaf.box_off;
+    MF_TRY(tcell_of_.reserve(size_t(nt) * sizeof(int32_t)));
+    MF_TRY(tstart_.reserve_slack(size_t(ncell + 1) * sizeof(int32_t)));
+    MF_TRY(tcursor_.reserve_slack(size_t(ncell + 1) * sizeof(int32_t)));
+    MF_TRY(tperm_tmp_.reserve_slack(size_t(nt + ncell + 2) * sizeof(int32_t)));
+    MF_TRY(tperm_.reserve_slack(size_t(nt + ncell + 2) * sizeof(int32_t)));
+    MF_CUDA_TRY(cudaMemsetAsync(tcnt, 0, size_t(ncell) * sizeof(int32_t), st));
+    k_fmm_count<<<blocks_for(nt), 256, 0, st>>>(tpos4, nt, leaf, tcell_of_.as<int32_t>(), tcnt);
+    k_fmm_scan<<<1, 1024, 0, st>>>(tcnt, ncell, tstart_.as<int32_t>());
+    MF_CUDA_TRY(cudaMemcpyAsync(tcursor_.ptr, tstart_.ptr, size_t(ncell) * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                                st));
+    k_fmm_scatter<<<blocks_for(nt), 256, 0, st>>>(tcell_of_.as<int32_t>(), nt, tcursor_.as<int32_t>(),
+                                                   tperm_tmp_.as<int32_t>());
+    k_fmm_sort<<<blocks_for(ncell * 32), 256, 0, st>>>(tstart_.as<int32_t>(), tcnt, ncell, tperm_tmp_.as<int32_t>(),
+                                                        tperm_.as<int32_t>());
+    for (int l = L - 1; l >= 0; --l)
+      k_fmm_occ_up<<<blocks_for(lv_[size_t(l)].nbox), 256, 0, st>>>(lv_[size_t(l + 1)], lv_[size_t(l)], tocc);
+    MF_CUDA_TRY(cudaGetLastError());
+  }
   // Slots: every box padded to an even count, so at most n + ncell; the
   // kernels read the exact count (start[ncell]) on the device.
   n_slots_ = n + ncell + 1;
@@ -1004,11 +1039,12 @@ mf_status Fmm::build(const float4* pos4, int64_t n, double h, const double* bbox
   // Statistics, counted on the device and read back lazily (stats()).
   MF_TRY(stat_.reserve(4 * sizeof(unsigned long long)));
   MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 4 * sizeof(unsigned long long), st));
-  k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, rows_.as<int4>(), n_rows_,
+  const int32_t* tocc_all = separate_ ? tocc_.as<int32_t>() : occ;
+  k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, tocc_all + leaf.box_off, rows_.as<int4>(), n_rows_,
                                                       stat_.as<unsigned long long>());
   for (int l = 2; l <= L; ++l)
     k_fmm_m2l_stats<<<blocks_for(lv_[size_t(l)].nbox * 32), 256, 0, st>>>(
-        lv_[size_t(l)], occ, lists_.as<int4>(), lofs_.as<int64_t>() + 8 * l,
+        lv_[size_t(l)], occ, tocc_all, lists_.as<int4>(), lofs_.as<int64_t>() + 8 * l,
         lofs_.as<int64_t>() + list_off_.size() + 8 * l, stat_.as<unsigned long long>());
   MF_CUDA_TRY(cudaGetLastError());
   if (!hstat_) MF_CUDA_TRY(cudaMallocHost(&hstat_, 4 * sizeof(unsigned long long)));
@@ -1103,6 +1139,7 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
   const FmmLevel& leaf = lv_[size_t(L)];
   int32_t* occ = occ_.as<int32_t>();
   const int32_t* cnt = occ + leaf.box_off;
+  const int32_t* tocc = separate_ ? tocc_.as<int32_t>() : occ;
   float* M = mcoef_.as<float>();
   float* Lc = lcoef_.as<float>();
   int nl = 0;
@@ -1124,6 +1161,7 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
     M2LArgs p{};
     p.lv = v;
     p.occ = occ;
+    p.tocc = tocc;
     p.M = M + v.box_off * NC;
     p.Lp = lpart_.as<float>();
     p.list = lists_.as<int4>();
@@ -1141,7 +1179,7 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
     const int64_t threads = int64_t(p.chunks) * 8 * p.per_class;
     M2LVariants<Q>::launch(p, unsigned((threads + 127) / 128), st, &nl);
     k_fmm_l2l<Q><<<blocks_for(int64_t(NC) * v.nbox, 256, int64_t(sms) * 32), 256, 0, st>>>(
-        v, lv_[size_t(l - 1)], l > 2 ? 1 : 0, occ, lpart_.as<float>(), p.chunks, Lc, done);
+        v, lv_[size_t(l - 1)], l > 2 ? 1 : 0, tocc, lpart_.as<float>(), p.chunks, Lc, done);
     ++nl;
   }
   P2PArgs pp{};
@@ -1149,6 +1187,9 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
   pp.start = start_.as<int32_t>();
   pp.cnt = cnt;
   pp.perm = perm_.as<int32_t>();
+  pp.tstart = separate_ ? tstart_.as<int32_t>() : pp.start;
+  pp.tcnt = tocc + leaf.box_off;
+  pp.tperm = separate_ ? tperm_.as<int32_t>() : pp.perm;
   pp.pos2s = pos2s_.as<float4>();
   pp.mom2s = mom2s_.as<float4>();
   pp.L = Lc + leaf.box_off * NC;
@@ -1172,3 +1213,181 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
 }
 
 }  // namespace mfgb
+
+// ===========================================================================
+// C ABI: an FMM matrix over a source set and a target set
+// ===========================================================================
+struct mf_fmm {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  mfgb::Fmm fmm;
+  mfgb::CellList cells;  // over the sources: the near-field correction
+  mfgb::Scratch scr;
+  mfgb::DevBuf spos, smom, tpos, corr, out4, staging;
+  int64_t ns = 0, nt = 0;
+  bool same = true;
+  mfgb::SceneDesc<float> sc{};
+  ~mf_fmm() {
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  }
+};
+
+namespace mfgb {
+namespace {
+__global__ void k_aos_to_f4(const float* __restrict__ src, int64_t n, float4* __restrict__ dst,
+                            int32_t* __restrict__ bad) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const float x = src[3 * i], y = src[3 * i + 1], z = src[3 * i + 2];
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicExch(bad, 1);
+    dst[i] = make_float4(x, y, z, 0.f);
+  }
+}
+__global__ void k_f4_to_aos(const float4* __restrict__ src, int64_t n, float* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const float4 v = src[i];
+    dst[3 * i] = v.x;
+    dst[3 * i + 1] = v.y;
+    dst[3 * i + 2] = v.z;
+  }
+}
+
+// Host AoS float[n][3] -> device float4 records (through `staging`); checks finiteness.
+mf_status upload_f4(mf_fmm& f, const float* host, int64_t n, DevBuf& dst) {
+  MF_TRY(f.staging.reserve(size_t(3 * n) * sizeof(float) + 16));
+  MF_TRY(dst.reserve(size_t(n + 2) * sizeof(float4), false, true));
+  int32_t* bad = reinterpret_cast<int32_t*>(f.staging.as<char>() + size_t(3 * n) * sizeof(float));
+  MF_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), f.st));
+  MF_CUDA_TRY(cudaMemcpyAsync(f.staging.ptr, host, size_t(3 * n) * sizeof(float), cudaMemcpyHostToDevice, f.st));
+  k_aos_to_f4<<<blocks_for(n), 256, 0, f.st>>>(f.staging.as<float>(), n, dst.as<float4>(), bad);
+  MF_CUDA_TRY(cudaGetLastError());
+  int32_t hb = 0;
+  MF_CUDA_TRY(cudaMemcpyAsync(&hb, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, f.st));
+  MF_CUDA_TRY(cudaStreamSynchronize(f.st));
+  if (hb) return fail(MF_ERR_INVALID_ARG, "non-finite input value");
+  return MF_OK;
+}
+
+template <class F>
+mf_status fguard(mf_fmm* f, F&& fn) {
+  if (!f) return fail(MF_ERR_INVALID_ARG, "NULL fmm handle");
+  try {
+    cudaError_t e = cudaSetDevice(f->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return fn(*f);
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  } catch (...) {
+    return fail(MF_ERR_CUDA, "unexpected exception");
+  }
+}
+}  // namespace
+}  // namespace mfgb
+
+using namespace mfgb;
+
+extern "C" {
+
+mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, int64_t nt, float h, int32_t order,
+                        double theta, int32_t leaf_min, int32_t device, mf_fmm** out) {
+  if (!out || !sources || ns <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no sources");
+  *out = nullptr;
+  if (targets && nt <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no targets");
+  if (!(h > 0.f) || !std::isfinite(h)) return fail(MF_ERR_INVALID_ARG, "fmm: h must be finite and > 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MF_ERR_UNSUPPORTED, "no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(MF_ERR_INVALID_ARG, "bad device ordinal");
+  try {
+    MF_CUDA_TRY(cudaSetDevice(device));
+    std::unique_ptr<mf_fmm> f(new mf_fmm);
+    f->device = device;
+    MF_CUDA_TRY(cudaStreamCreateWithFlags(&f->st, cudaStreamNonBlocking));
+    f->ns = ns;
+    f->same = targets == nullptr;
+    f->nt = f->same ? ns : nt;
+    MF_TRY(upload_f4(*f, sources, ns, f->spos));
+    if (!f->same) MF_TRY(upload_f4(*f, targets, nt, f->tpos));
+    MF_TRY(f->cells.build(f->spos.as<float4>(), {CellSceneSpec{0, ns, double(h)}}, f->st));
+    double bbox[6];
+    for (int k = 0; k < 6; ++k) bbox[k] = f->cells.bbox(0)[k];
+    if (!f->same)
+      for (int64_t i = 0; i < nt; ++i)
+        for (int k = 0; k < 3; ++k) {
+          bbox[k] = std::min(bbox[k], double(targets[3 * i + k]));
+          bbox[3 + k] = std::max(bbox[3 + k], double(targets[3 * i + k]));
+        }
+    FmmConfig cfg;
+    cfg.order = order;
+    cfg.theta = theta;
+    cfg.leaf_min = leaf_min;
+    MF_TRY(f->fmm.build(f->spos.as<float4>(), ns, f->same ? nullptr : f->tpos.as<float4>(), f->nt, double(h), bbox,
+                        cfg, f->st));
+    MF_TRY(f->corr.reserve(size_t(f->nt + 2) * sizeof(float4), false, true));
+    MF_TRY(f->out4.reserve(size_t(f->nt + 2) * sizeof(float4), false, true));
+    MF_TRY(f->scr.ensure(0, 0));
+    f->sc.pc = make_pair_consts<float>(double(h));
+    f->sc.scale = 1.f;
+    MF_CUDA_TRY(cudaStreamSynchronize(f->st));
+    *out = f.release();
+    return MF_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(MF_ERR_OOM, "host allocation failed");
+  }
+}
+
+mf_status mf_fmm_destroy(mf_fmm* f) {
+  if (!f) return MF_OK;
+  cudaSetDevice(f->device);
+  delete f;
+  return MF_OK;
+}
+
+mf_status mf_fmm_field(mf_fmm* f, const float* charges, float* results) {
+  return fguard(f, [&](mf_fmm& x) {
+    if (!charges || !results) return fail(MF_ERR_INVALID_ARG, "NULL argument");
+    MF_TRY(upload_f4(x, charges, x.ns, x.smom));
+    const float4* tp = x.same ? x.spos.as<float4>() : x.tpos.as<float4>();
+    if (x.same)
+      MF_TRY(x.cells.field_correction(x.spos.as<float4>(), x.smom.as<float4>(), x.corr.as<float4>(), x.st));
+    else
+      MF_TRY(x.cells.field_correction_at(tp, x.nt, x.spos.as<float4>(), x.smom.as<float4>(), x.corr.as<float4>(),
+                                         x.st));
+    AllPairsArgs<float> a{};
+    a.tpos = tp;
+    a.corr4 = x.corr.as<float4>();
+    a.out4 = x.out4.as<float4>();
+    a.err = x.scr.err.as<int32_t>();
+    MF_TRY(x.fmm.product(false, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
+    MF_TRY(x.staging.reserve(size_t(3 * x.nt) * sizeof(float) + 16));
+    k_f4_to_aos<<<blocks_for(x.nt), 256, 0, x.st>>>(x.out4.as<float4>(), x.nt, x.staging.as<float>());
+    MF_CUDA_TRY(cudaGetLastError());
+    MF_CUDA_TRY(cudaMemcpyAsync(results, x.staging.ptr, size_t(3 * x.nt) * sizeof(float), cudaMemcpyDeviceToHost,
+                                x.st));
+    MF_CUDA_TRY(cudaStreamSynchronize(x.st));
+    return x.scr.check(x.st);
+  });
+}
+
+mf_status mf_fmm_get_stats(mf_fmm* f, mf_fmm_stats* out) {
+  return fguard(f, [&](mf_fmm& x) {
+    if (!out) return fail(MF_ERR_INVALID_ARG, "NULL");
+    *out = mf_fmm_stats{};
+    const FmmStats& s = x.fmm.stats();
+    out->active = 1;
+    out->levels = s.levels;
+    out->leaf_level = s.leaf_level;
+    out->degree = s.degree;
+    out->leaf_boxes = s.leaf_boxes;
+    out->occupied_leaves = s.occupied_leaves;
+    out->max_leaf = s.max_leaf;
+    out->near_rows = s.near_rows;
+    out->p2p_pairs = s.p2p_pairs;
+    out->m2l_per_product = s.m2l_per_product;
+    out->launches_per_product = x.fmm.launches_per_product();
+    return MF_OK;
+  });
+}
+
+}  // extern "C"

@@ -333,10 +333,13 @@ class Fmm {
   // Builds the box grids, bins the particles of pos4[0..n) into leaf boxes
   // and lays out the interaction lists.  Synchronises `st` (the bounding box
   // and the leaf occupancy are read on the host).
-  mf_status build(const float4* pos4, int64_t n, double h, const double* bbox, const FmmConfig& cfg,
-                  cudaStream_t st);
+  // tpos4[0..nt): separate targets (null: the targets are the sources).
+  // bbox (lo xyz, hi xyz) must hold the sources and the targets.
+  mf_status build(const float4* pos4, int64_t n, const float4* tpos4, int64_t nt, double h, const double* bbox,
+                  const FmmConfig& cfg, cudaStream_t st);
   // out = epilogue(far field + near field + corr4) of the field (kForce false)
-  // or Kelvin force (kForce true) of the dipoles smom at every particle.  `a`
+  // or Kelvin force (kForce true) of the dipoles smom at every target (every
+  // particle when the targets are the sources; `a.tpos` holds the targets).  `a`
   // carries the epilogue's pointers (tpos, tmom, out, out4, add4, add4b, rext,
   // corr4, err) exactly as for an all-pairs launch; `sc` its coefficients.
   // `done`: a solver stop flag; every launch is a no-op once it is non-zero.
@@ -368,6 +371,10 @@ class Fmm {
   int launches_ = 0;
   DevBuf cell_of_, cnt_, start_, cursor_, perm_tmp_, perm_, pos2s_, mom2s_;
   DevBuf occ_, mcoef_, lcoef_, lpart_, lists_, rows_, dtab_, stat_, lofs_;
+  // Separate targets: occupancy per level and leaf binning.
+  DevBuf tocc_, tcell_of_, tstart_, tcursor_, tperm_tmp_, tperm_;
+  bool separate_ = false;
+  int64_t nt_ = 0;
   std::vector<int4> host_list_, host_rows_;  // as last uploaded
   std::vector<int32_t> host_dkey_;           // degree and offsets of the uploaded derivative table
   unsigned long long* hstat_ = nullptr;      // pinned: near pairs, largest leaf, M2L count, occupied leaves

@@ -124,6 +124,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_get_fmm_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
         "mf_apply_field": (i32, [vp, vp, i32, i32, vp]),
         "mf_autotune_report": (i32, [vp, i64, ctypes.POINTER(i64)]),
+        "mf_fmm_create": (i32, [vp, i64, vp, i64, f32, i32, f64, i32, i32, ctypes.POINTER(vp)]),
+        "mf_fmm_destroy": (i32, [vp]),
+        "mf_fmm_field": (i32, [vp, vp, vp]),
+        "mf_fmm_get_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -499,6 +503,48 @@ class Server:
         s = mf_server_stats()
         check(load().mf_server_get_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in mf_server_stats._fields_}
+
+
+class FmmMatrix:
+    """FMM matrix of the field kernel over a source set and a target set: the
+    replacement of fmmtl::kernel_matrix<DipoleBSpherical>(kernel, sources,
+    targets) and its operator* (fmmtl/KernelMatrix.hpp:127-131).  targets=None
+    means the targets are the sources."""
+
+    def __init__(self, sources, h, targets=None, order=8, theta=0.5, leaf_min=64, device=0):
+        self._h = None
+        src = _f32(sources)
+        tgt = None if targets is None else _f32(targets)
+        self.ns = len(src)
+        self.nt = self.ns if tgt is None else len(tgt)
+        h_ = ctypes.c_void_p()
+        check(load().mf_fmm_create(src.ctypes.data, self.ns, None if tgt is None else tgt.ctypes.data,
+                                   0 if tgt is None else self.nt, float(h), int(order), float(theta), int(leaf_min),
+                                   int(device), ctypes.byref(h_)))
+        self._h = h_
+
+    def field(self, charges) -> np.ndarray:
+        c = _f32(charges)
+        assert len(c) == self.ns
+        out = np.empty((self.nt, 3), np.float32)
+        check(load().mf_fmm_field(self._h, c.ctypes.data, out.ctypes.data))
+        return out
+
+    def stats(self) -> dict:
+        st = mf_fmm_stats()
+        check(load().mf_fmm_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_ if f != "pad"}
+
+    def close(self):
+        if self._h is not None:
+            load().mf_fmm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def autotune_report() -> list[str]:

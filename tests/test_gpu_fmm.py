@@ -183,3 +183,32 @@ def test_degenerate_geometry(mf, kind):
     assert st["active"] == 1 and st["occupied_leaves"] >= 1
     s.set_option("fmm", mf.FMM_OFF)
     assert rel(got, s.apply_field(m)) < 1e-5
+
+
+def test_fmm_matrix_separate_targets(mf, oracle, sphere40k):
+    # The kernel_matrix form: sources and a separate target set (inside,
+    # around and far from the sources, some on source positions).
+    sc = sphere40k
+    rng = np.random.default_rng(8)
+    tg = np.r_[rng.uniform(-0.6, 0.6, (3000, 3)), sc.pos[:500], rng.uniform(2.0, 2.5, (200, 3))].astype(np.float32)
+    m = moments(sc, seed=9)
+    A = mf.FmmMatrix(sc.pos, sc.h, targets=tg, order=8, theta=0.5, leaf_min=16)
+    got = A.field(m)
+    want = oracle.field(tg.astype(np.float64), sc.pos.astype(np.float64), m, sc.h)
+    assert rel(got, want) < 1e-5
+    st = A.stats()
+    assert st["active"] == 1 and st["m2l_per_product"] > 0
+    # a second product on the same matrix with new charges
+    m2 = moments(sc, seed=10)
+    want2 = oracle.field(tg.astype(np.float64), sc.pos.astype(np.float64), m2, sc.h)
+    assert rel(A.field(m2), want2) < 1e-5
+    A.close()
+
+
+def test_fmm_matrix_same_targets(mf, sphere40k):
+    sc = sphere40k
+    m = moments(sc, seed=11)
+    A = mf.FmmMatrix(sc.pos, sc.h, order=8, leaf_min=16)
+    s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=8, fmm_leaf=16)
+    assert rel(A.field(m), s.apply_field(m)) < 1e-6
+    A.close()
