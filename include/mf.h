@@ -305,6 +305,10 @@ mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, 
 mf_status mf_fmm_destroy(mf_fmm* f);
 /* results[nt][3] = sum_j DipoleBKernel{h}(targets_i, sources_j) * charges_j */
 mf_status mf_fmm_field(mf_fmm* f, const float* charges, float* results);
+/* results9[nt][9] = sum_j DipoleHessianKernel{h}(targets_i, sources_j) * charges_j, the 3x3 force
+ * tensor per target in glm column-major order (results9[i*9 + c*3 + r]), as mf_direct_force_tensor:
+ * the kernel_matrix<DipoleHessianSpherical> product. */
+mf_status mf_fmm_hessian(mf_fmm* f, const float* charges, float* results9);
 mf_status mf_fmm_get_stats(mf_fmm* f, mf_fmm_stats* out);
 
 /* ---------------------------------------------------------------------- */

@@ -388,6 +388,51 @@ struct ForceF2Body : PairItems {
   }
 };
 
+// Packed force tensor (the FMM matrix of the Hessian kernel at separate
+// targets).  The near-field correction comes as two records per target in
+// corr4: (xx, yy, zz, -), (xy, xz, yz, -).
+struct TensorF2Body : PairItems {
+  static constexpr int kOut = 6;
+  struct TData {
+    float2 x, y, z;
+  };
+  struct Acc {
+    float2 t[6];
+    __device__ void zero() {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) t[k] = make_float2(0.f, 0.f);
+    }
+  };
+  __device__ static void load(const AllPairsArgs<float>& a, int64_t i, TData& t) {
+    const float4 p = a.tpos[i];
+    t.x = f2_dup(p.x);
+    t.y = f2_dup(p.y);
+    t.z = f2_dup(p.z);
+  }
+  __device__ static void pair(const TData& t, const Item& it, const PairConsts<float>& pc, Acc& acc) {
+    tensor_pair2(t.x, t.y, t.z, it.x, it.y, it.z, it.mx, it.my, it.mz, pc.near2_force, acc.t);
+  }
+  __device__ static void tile_out(const Acc& acc, float* o) {
+    const float c = float(kForceK);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = (acc.t[k].x + acc.t[k].y) * c;
+  }
+  __device__ static void epilogue(const AllPairsArgs<float>& a, const SceneDesc<float>& sc, int64_t i,
+                                  const TData&, const double* vin) {
+    double v[6] = {vin[0], vin[1], vin[2], vin[3], vin[4], vin[5]};
+    if (a.corr4) {
+      const float4 c0 = a.corr4[2 * i], c1 = a.corr4[2 * i + 1];
+      v[0] += c0.x;
+      v[1] += c0.y;
+      v[2] += c0.z;
+      v[3] += c1.x;
+      v[4] += c1.y;
+      v[5] += c1.z;
+    }
+    TensorBody<float>::epilogue(a, sc, i, TensorBody<float>::TData{}, v);
+  }
+};
+
 // ----------------------------------------------------------------------------
 // Step-space helpers.
 // ----------------------------------------------------------------------------

@@ -367,6 +367,52 @@ __global__ void __launch_bounds__(128) k_correction(const CellGrid* __restrict__
   }
 }
 
+// Tensor correction at separate targets (single-scene list): corr[2i] =
+// (xx, yy, zz, 0), corr[2i + 1] = (xy, xz, yz, 0) of the exact minus the
+// clamped force tensor over the sources within 4h, in the output units.
+__global__ void __launch_bounds__(128) k_tensor_correction(const CellGrid* __restrict__ grids, int64_t nt,
+                                                           const int32_t* __restrict__ perm,
+                                                           const int32_t* __restrict__ start,
+                                                           const float4* __restrict__ pos,
+                                                           const float4* __restrict__ mom,
+                                                           const float4* __restrict__ tpos,
+                                                           float4* __restrict__ corr) {
+  const CellGrid& g = grids[0];
+  const int R = g.reach_force;
+  const float near2 = g.pc.near2_force;
+  float cA, cB;
+  clamped_force_coeffs(near2, cA, cB);
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nt; i += int64_t(gridDim.x) * blockDim.x) {
+    const float4 pi = tpos[i];
+    int ix, iy, iz;
+    cell_coords(g, pi.x, pi.y, pi.z, ix, iy, iz);
+    float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int dz = -R; dz <= R; ++dz) {
+      const int cz = iz + dz;
+      if (cz < 0 || cz >= g.nz) continue;
+      for (int dy = -R; dy <= R; ++dy) {
+        const int cy = iy + dy;
+        if (cy < 0 || cy >= g.ny) continue;
+        const int cx0 = max(ix - R, 0), cx1 = min(ix + R, g.nx - 1);
+        const int64_t row = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx;
+        const int32_t b = start[row + cx0], e = start[row + cx1 + 1];
+        for (int32_t q = b; q < e; ++q) {
+          const int32_t j = perm[q];
+          const float4 pj = pos[j];
+          const float dx = pi.x - pj.x, dy2 = pi.y - pj.y, dz2 = pi.z - pj.z;
+          if (dx * dx + dy2 * dy2 + dz2 * dz2 <= near2) {
+            const float4 mj = mom[j];
+            tensor_near_correction(dx, dy2, dz2, mj.x, mj.y, mj.z, g.pc, cA, cB, t);
+          }
+        }
+      }
+    }
+    const float c = float(kForceK);
+    corr[2 * i] = make_float4(t[0] * c, t[1] * c, t[2] * c, 0.f);
+    corr[2 * i + 1] = make_float4(t[3] * c, t[4] * c, t[5] * c, 0.f);
+  }
+}
+
 __global__ void k_to_pairs(const float4* __restrict__ src, float4* __restrict__ dst, int64_t n,
                            const int32_t* __restrict__ done_count, int done_total) {
   if (done_count && *done_count >= done_total) return;
@@ -516,6 +562,15 @@ mf_status CellList::field_correction_at(const float4* tpos4, int64_t nt, const f
   k_correction<false><<<grid_for(nt, 128), 128, 0, st>>>(grids_.as<CellGrid>(), n_scenes_, nt,
                                                           perm_.as<int32_t>(), cell_start_.as<int32_t>(), pos4, mom4,
                                                           tpos4, corr);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+
+mf_status CellList::tensor_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
+                                         float4* corr2, cudaStream_t st) const {
+  if (n_scenes_ != 1) return fail(MF_ERR_INVALID_ARG, "separate targets need a single-scene cell list");
+  k_tensor_correction<<<grid_for(nt, 128), 128, 0, st>>>(grids_.as<CellGrid>(), nt, perm_.as<int32_t>(),
+                                                         cell_start_.as<int32_t>(), pos4, mom4, tpos4, corr2);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

@@ -126,6 +126,11 @@ __device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
   return f2_from(r);
 }
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+  return f2_from(r);
+}
 __device__ __forceinline__ float2 f2_dup(float v) { return make_float2(v, v); }
 
 // Packed 4-wide particle record (x, y, z, pad): 16 B for FP32, 32 B for FP64,

@@ -901,7 +901,7 @@ class Engine final : public EngineBase {
         marks[2] = tn.start;
         marks[3] = tn.stop;
       }
-      MF_TRY(fmm_.product(force, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr));
+      MF_TRY(fmm_.product(force ? 1 : 0, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr));
       if (timing_) {
         MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
         timed_.push_back(t);

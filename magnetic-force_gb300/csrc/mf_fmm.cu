@@ -523,10 +523,14 @@ struct P2PArgs {
   const double* done;
 };
 
-template <int Q, bool kForce>
+// kKind: 0 field (H), 1 Kelvin force (contracted with the target dipole),
+// 2 force tensor (the Hessian kernel's 3x3 at each target).
+template <int Q, int kKind>
 __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const AllPairsArgs<float> a,
                                                          const SceneDesc<float> sc) {
-  using Body = std::conditional_t<kForce, ForceF2Body, FieldF2Body>;
+  using Body = std::conditional_t<kKind == 0, FieldF2Body, std::conditional_t<kKind == 1, ForceF2Body, TensorF2Body>>;
+  constexpr bool kForce = kKind == 1;
+  constexpr int kOut = Body::kOut;
   constexpr int NC = ncoef(Q) - 1;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar[kP2PStages];
@@ -595,7 +599,9 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
     const int32_t i = p.tperm[st0 + (act ? t0 + tid : 0)];
     typename Body::TData td;
     Body::load(a, i, td);
-    float run[3] = {0.f, 0.f, 0.f}, cmp[3] = {0.f, 0.f, 0.f};
+    float run[kOut], cmp[kOut];
+#pragma unroll
+    for (int q = 0; q < kOut; ++q) run[q] = cmp[q] = 0.f;
     if (tid == 0) {
       s_row = 0;
       s_pos = -1;
@@ -625,10 +631,10 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
         acc.zero();
 #pragma unroll 4
         for (int j = 0; j < n_items; ++j) Body::pair(td, Body::load_item(sp, sm, j), sc.pc, acc);
-        float o[3];
+        float o[kOut];
         Body::tile_out(acc, o);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) comp_add(run[q], cmp[q], o[q]);
+        for (int q = 0; q < kOut; ++q) comp_add(run[q], cmp[q], o[q]);
         __syncthreads();  // stage s is free
         if (tid == 0 && k + kP2PStages < ns) {
           fence_proxy_async_smem();
@@ -657,9 +663,9 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
         pw[(ax * Q + k) * kP2PThreads + tid] = v;
       }
     }
-    double v[3];
-    for (int q = 0; q < 3; ++q) v[q] = double(run[q]) + double(cmp[q]);
-    if constexpr (!kForce) {
+    double v[kOut];
+    for (int q = 0; q < kOut; ++q) v[q] = double(run[q]) + double(cmp[q]);
+    if constexpr (kKind == 0) {
       // H = -grad phi = -1/(4 pi s^3) sum_g L_(g + e_k) w^g / g!
       float h0 = 0.f, h1 = 0.f, h2 = 0.f;
       for (int g = 0; g < ncoef(Q - 1); ++g) {
@@ -690,10 +696,20 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
       }
       const double is2 = double(inv_s) * double(inv_s);
       const double f = -kMu0 * kInv4Pi * is2 * is2;
-      const float4 tm = a.tmom[i];
-      v[0] += f * (double(hxx) * tm.x + double(hxy) * tm.y + double(hxz) * tm.z);
-      v[1] += f * (double(hxy) * tm.x + double(hyy) * tm.y + double(hyz) * tm.z);
-      v[2] += f * (double(hxz) * tm.x + double(hyz) * tm.y + double(hzz) * tm.z);
+      if constexpr (kForce) {
+        const float4 tm = a.tmom[i];
+        v[0] += f * (double(hxx) * tm.x + double(hxy) * tm.y + double(hxz) * tm.z);
+        v[1] += f * (double(hxy) * tm.x + double(hyy) * tm.y + double(hyz) * tm.z);
+        v[2] += f * (double(hxz) * tm.x + double(hyz) * tm.y + double(hzz) * tm.z);
+      } else {
+        // T = -mu0 Hess phi, entries xx, yy, zz, xy, xz, yz
+        v[0] += f * double(hxx);
+        v[1] += f * double(hyy);
+        v[2] += f * double(hzz);
+        v[3] += f * double(hxy);
+        v[4] += f * double(hxz);
+        v[5] += f * double(hyz);
+      }
     }
     if (act) Body::epilogue(a, sc, i, td, v);
   }
@@ -1077,14 +1093,15 @@ Fmm::~Fmm() {
   if (stat_ev_) cudaEventDestroy(stat_ev_);
 }
 
-mf_status Fmm::product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+mf_status Fmm::product(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
                        const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
+  if (kind < 0 || kind > 2) return fail(MF_ERR_INVALID_ARG, "fmm: unknown product kind");
   switch (degree_) {
-    case 3: return product_q<3>(force, pos4, smom, a, sc, st, done, marks);
-    case 4: return product_q<4>(force, pos4, smom, a, sc, st, done, marks);
-    case 5: return product_q<5>(force, pos4, smom, a, sc, st, done, marks);
-    case 6: return product_q<6>(force, pos4, smom, a, sc, st, done, marks);
-    case 7: return product_q<7>(force, pos4, smom, a, sc, st, done, marks);
+    case 3: return product_q<3>(kind, pos4, smom, a, sc, st, done, marks);
+    case 4: return product_q<4>(kind, pos4, smom, a, sc, st, done, marks);
+    case 5: return product_q<5>(kind, pos4, smom, a, sc, st, done, marks);
+    case 6: return product_q<6>(kind, pos4, smom, a, sc, st, done, marks);
+    case 7: return product_q<7>(kind, pos4, smom, a, sc, st, done, marks);
     default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
   }
 }
@@ -1132,7 +1149,7 @@ struct M2LVariants<7> {
 }  // namespace
 
 template <int Q>
-mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
                          const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
   constexpr int NC = ncoef(Q) - 1;
   const int L = int(lv_.size()) - 1;
@@ -1201,10 +1218,12 @@ mf_status Fmm::product_q(bool force, const float4* pos4, const float4* smom, con
     MF_CUDA_TRY(cudaEventRecord(marks[1], st));
     MF_CUDA_TRY(cudaEventRecord(marks[2], st));
   }
-  if (force)
-    k_fmm_p2p<Q, true><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+  if (kind == 1)
+    k_fmm_p2p<Q, 1><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+  else if (kind == 2)
+    k_fmm_p2p<Q, 2><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
   else
-    k_fmm_p2p<Q, false><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+    k_fmm_p2p<Q, 0><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
   ++nl;
   if (marks) MF_CUDA_TRY(cudaEventRecord(marks[3], st));
   launches_ = nl;
@@ -1223,7 +1242,7 @@ struct mf_fmm {
   mfgb::Fmm fmm;
   mfgb::CellList cells;  // over the sources: the near-field correction
   mfgb::Scratch scr;
-  mfgb::DevBuf spos, smom, tpos, corr, out4, staging;
+  mfgb::DevBuf spos, smom, tpos, corr, out4, out9, staging;
   int64_t ns = 0, nt = 0;
   bool same = true;
   mfgb::SceneDesc<float> sc{};
@@ -1244,6 +1263,12 @@ __global__ void k_aos_to_f4(const float* __restrict__ src, int64_t n, float4* __
     if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicExch(bad, 1);
     dst[i] = make_float4(x, y, z, 0.f);
   }
+}
+// 9 SoA arrays (k = column * 3 + row) -> [n][9] in the same order per target.
+__global__ void k_soa9_to_aos(const float* __restrict__ src, int64_t n, float* __restrict__ dst) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dst[9 * i + k] = src[int64_t(k) * n + i];
 }
 __global__ void k_f4_to_aos(const float4* __restrict__ src, int64_t n, float* __restrict__ dst) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
@@ -1359,11 +1384,36 @@ mf_status mf_fmm_field(mf_fmm* f, const float* charges, float* results) {
     a.corr4 = x.corr.as<float4>();
     a.out4 = x.out4.as<float4>();
     a.err = x.scr.err.as<int32_t>();
-    MF_TRY(x.fmm.product(false, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
+    MF_TRY(x.fmm.product(0, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
     MF_TRY(x.staging.reserve(size_t(3 * x.nt) * sizeof(float) + 16));
     k_f4_to_aos<<<blocks_for(x.nt), 256, 0, x.st>>>(x.out4.as<float4>(), x.nt, x.staging.as<float>());
     MF_CUDA_TRY(cudaGetLastError());
     MF_CUDA_TRY(cudaMemcpyAsync(results, x.staging.ptr, size_t(3 * x.nt) * sizeof(float), cudaMemcpyDeviceToHost,
+                                x.st));
+    MF_CUDA_TRY(cudaStreamSynchronize(x.st));
+    return x.scr.check(x.st);
+  });
+}
+
+mf_status mf_fmm_hessian(mf_fmm* f, const float* charges, float* results9) {
+  return fguard(f, [&](mf_fmm& x) {
+    if (!charges || !results9) return fail(MF_ERR_INVALID_ARG, "NULL argument");
+    MF_TRY(upload_f4(x, charges, x.ns, x.smom));
+    const float4* tp = x.same ? x.spos.as<float4>() : x.tpos.as<float4>();
+    MF_TRY(x.corr.reserve(size_t(2 * x.nt + 2) * sizeof(float4), false, true));
+    MF_TRY(x.cells.tensor_correction_at(tp, x.nt, x.spos.as<float4>(), x.smom.as<float4>(), x.corr.as<float4>(),
+                                        x.st));
+    MF_TRY(x.out9.reserve(size_t(9 * x.nt) * sizeof(float)));
+    AllPairsArgs<float> a{};
+    a.tpos = tp;
+    a.corr4 = x.corr.as<float4>();
+    for (int k = 0; k < 9; ++k) a.out[k] = x.out9.as<float>() + size_t(k) * size_t(x.nt);
+    a.err = x.scr.err.as<int32_t>();
+    MF_TRY(x.fmm.product(2, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
+    MF_TRY(x.staging.reserve(size_t(9 * x.nt) * sizeof(float) + 16));
+    k_soa9_to_aos<<<blocks_for(x.nt), 256, 0, x.st>>>(x.out9.as<float>(), x.nt, x.staging.as<float>());
+    MF_CUDA_TRY(cudaGetLastError());
+    MF_CUDA_TRY(cudaMemcpyAsync(results9, x.staging.ptr, size_t(9 * x.nt) * sizeof(float), cudaMemcpyDeviceToHost,
                                 x.st));
     MF_CUDA_TRY(cudaStreamSynchronize(x.st));
     return x.scr.check(x.st);

@@ -286,6 +286,10 @@ class CellList {
   // Field correction at separate targets tpos4[0..nt) (single-scene lists).
   mf_status field_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
                                 float4* corr, cudaStream_t st) const;
+  // Force-tensor correction at separate targets: corr2[2i] = (xx, yy, zz, 0),
+  // corr2[2i + 1] = (xy, xz, yz, 0).
+  mf_status tensor_correction_at(const float4* tpos4, int64_t nt, const float4* pos4, const float4* mom4,
+                                 float4* corr2, cudaStream_t st) const;
   int64_t particles() const { return n_total_; }
   int64_t cells() const { return n_cells_; }
   const std::vector<CellGrid>& grids() const { return host_grids_; }
@@ -345,7 +349,9 @@ class Fmm {
   // `done`: a solver stop flag; every launch is a no-op once it is non-zero.
   // marks (optional, 4 events): recorded before and after the far-field
   // stages (gather .. L2L), then before and after the near-field kernel.
-  mf_status product(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+  // kind: 0 field, 1 Kelvin force, 2 force tensor (6 entries through the
+  // tensor epilogue; a.corr4 then holds two records per target).
+  mf_status product(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
                     const SceneDesc<float>& sc, cudaStream_t st, const double* done,
                     cudaEvent_t* marks = nullptr);
   // Shape and work of the last build (waits for its device counts).
@@ -358,7 +364,7 @@ class Fmm {
 
  private:
   template <int Q>
-  mf_status product_q(bool force, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
+  mf_status product_q(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
                       const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks);
   FmmConfig cfg_;
   FmmStats stats_;

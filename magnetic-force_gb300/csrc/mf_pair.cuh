@@ -255,6 +255,28 @@ __device__ __forceinline__ void force_pair2(float2 tx, float2 ty, float2 tz, flo
   f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_fma(smz, v, f[2])));
 }
 
+// Packed two-source force tensor (6 unique entries xx, yy, zz, xy, xz, yz of
+// T(d, s) / K), clamped far form: P = r^-5, Q = -5 r^-7 at max(r^2, near2).
+__device__ __forceinline__ void tensor_pair2(float2 tx, float2 ty, float2 tz, float2 sx, float2 sy, float2 sz,
+                                             float2 smx, float2 smy, float2 smz, float near2, float2* t) {
+  const float2 dx = f2_sub(tx, sx), dy = f2_sub(ty, sy), dz = f2_sub(tz, sz);
+  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+  const float2 ri = clamp_rsqrt2(r2, near2);
+  const float2 ri2 = f2_mul(ri, ri);
+  const float2 P = f2_mul(f2_mul(ri2, ri2), ri);
+  const float2 Q = f2_mul(f2_mul(ri2, P), f2_dup(-5.f));
+  const float2 ds = f2_fma(dz, smz, f2_fma(dy, smy, f2_mul(dx, smx)));
+  const float2 pd = f2_mul(P, ds), qd = f2_mul(Q, ds);
+  const float2 ax = f2_mul(P, smx), ay = f2_mul(P, smy), az = f2_mul(P, smz);
+  const float2 two = f2_dup(2.f);
+  t[0] = f2_fma(f2_mul(qd, dx), dx, f2_fma(f2_mul(two, ax), dx, f2_add(pd, t[0])));
+  t[1] = f2_fma(f2_mul(qd, dy), dy, f2_fma(f2_mul(two, ay), dy, f2_add(pd, t[1])));
+  t[2] = f2_fma(f2_mul(qd, dz), dz, f2_fma(f2_mul(two, az), dz, f2_add(pd, t[2])));
+  t[3] = f2_fma(f2_mul(qd, dx), dy, f2_fma(ax, dy, f2_fma(ay, dx, t[3])));
+  t[4] = f2_fma(f2_mul(qd, dx), dz, f2_fma(ax, dz, f2_fma(az, dx, t[4])));
+  t[5] = f2_fma(f2_mul(qd, dy), dz, f2_fma(ay, dz, f2_fma(az, dy, t[5])));
+}
+
 // The clamped far coefficients every near pair received in the packed loop
 // (the same rsqrt and products; equal to within rounding).
 __device__ __forceinline__ void clamped_field_coeffs(float near2, float& alpha, float& beta) {
@@ -381,6 +403,25 @@ __device__ __forceinline__ void field_near_correction(float dx, float dy, float 
 }
 
 // Correction of one near force pair (r^2 <= near2), contracted with m.
+// Tensor correction of one near pair (r^2 <= near2): exact minus clamped,
+// the 6 entries (xx, yy, zz, xy, xz, yz) of T / K.
+__device__ __forceinline__ void tensor_near_correction(float dx, float dy, float dz, float sx, float sy, float sz,
+                                                       const PairConsts<float>& pc, float P_c, float Q_c, float* t) {
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  float P, Q;
+  force_near_coeffs<float>(r2, pc, P, Q);
+  const float dP = P - P_c, dQ = Q - Q_c;
+  const float ds = dx * sx + dy * sy + dz * sz;
+  const float pd = dP * ds, qd = dQ * ds;
+  const float ax = dP * sx, ay = dP * sy, az = dP * sz;
+  t[0] += pd + 2.f * ax * dx + qd * dx * dx;
+  t[1] += pd + 2.f * ay * dy + qd * dy * dy;
+  t[2] += pd + 2.f * az * dz + qd * dz * dz;
+  t[3] += ax * dy + ay * dx + qd * dx * dy;
+  t[4] += ax * dz + az * dx + qd * dx * dz;
+  t[5] += ay * dz + az * dy + qd * dy * dz;
+}
+
 __device__ __forceinline__ void force_near_correction(float dx, float dy, float dz, float sx, float sy, float sz,
                                                       float mx, float my, float mz, const PairConsts<float>& pc,
                                                       float P_c, float Q_c, float* f) {

@@ -127,6 +127,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_fmm_create": (i32, [vp, i64, vp, i64, f32, i32, f64, i32, i32, ctypes.POINTER(vp)]),
         "mf_fmm_destroy": (i32, [vp]),
         "mf_fmm_field": (i32, [vp, vp, vp]),
+        "mf_fmm_hessian": (i32, [vp, vp, vp]),
         "mf_fmm_get_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
     }
     for name, (res, args) in sig.items():
@@ -528,6 +529,14 @@ class FmmMatrix:
         assert len(c) == self.ns
         out = np.empty((self.nt, 3), np.float32)
         check(load().mf_fmm_field(self._h, c.ctypes.data, out.ctypes.data))
+        return out
+
+    def hessian(self, charges) -> np.ndarray:
+        """[nt][9] force tensors, glm column-major (entry c*3 + r)."""
+        c = _f32(charges)
+        assert len(c) == self.ns
+        out = np.empty((self.nt, 9), np.float32)
+        check(load().mf_fmm_hessian(self._h, c.ctypes.data, out.ctypes.data))
         return out
 
     def stats(self) -> dict:

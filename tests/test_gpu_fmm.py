@@ -212,3 +212,21 @@ def test_fmm_matrix_same_targets(mf, sphere40k):
     s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=8, fmm_leaf=16)
     assert rel(A.field(m), s.apply_field(m)) < 1e-6
     A.close()
+
+
+def test_fmm_matrix_hessian(mf, oracle, sphere40k):
+    # The kernel_matrix<DipoleHessianSpherical> form: 3x3 force tensors at a
+    # separate target set, glm column-major like mf_direct_force_tensor.
+    sc = sphere40k
+    rng = np.random.default_rng(12)
+    tg = np.r_[rng.uniform(-0.55, 0.55, (1500, 3)), sc.pos[:300]].astype(np.float32)
+    m = moments(sc, seed=13)
+    A = mf.FmmMatrix(sc.pos, sc.h, targets=tg, order=8, theta=0.5, leaf_min=16)
+    got = A.hessian(m)
+    want = oracle.tensor_sum(tg.astype(np.float64), sc.pos.astype(np.float64), m, sc.h).reshape(-1, 9)
+    assert got.shape == (len(tg), 9)
+    assert rel(got, want) < 3e-4
+    # symmetric 3x3 per target
+    g3 = got.reshape(-1, 3, 3)
+    assert np.allclose(g3, np.transpose(g3, (0, 2, 1)), rtol=0, atol=1e-6 * np.abs(g3).max())
+    A.close()
