@@ -461,10 +461,14 @@ class Engine final : public EngineBase {
         check_interval_set_ = true;
         return MF_OK;
       case MF_OPT_KERNEL_TIMING: timing_ = v != 0.0; return MF_OK;
-      case MF_OPT_FMM:
+      case MF_OPT_FMM: {
         if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "fmm mode must be 0, 1 or 2");
+        const bool was = use_fmm();
         fmm_mode_ = int(v);
+        // all-pairs from now on: its plans were built untuned
+        if (was && !use_fmm() && plans_ready_ && tune_ != Tune::Off) MF_TRY(build_plans());
         return MF_OK;
+      }
       case MF_OPT_FMM_ORDER:
         if (v < 4 || v > 8 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..8");
         fmm_cfg_.order = int(v);
@@ -620,7 +624,9 @@ class Engine final : public EngineBase {
     // positions (the tuning launches write scratch vectors only).
     int fshape = 0, gshape = 0;
     if constexpr (kF32) {
-      if (tune_ != Tune::Off) {
+      // A handle on the FMM path launches no all-pairs product: its plans
+      // only carry the epilogue coefficients, so they are not timed.
+      if (tune_ != Tune::Off && !use_fmm()) {
         LaunchIO<Real> io;
         io.tpos = pos4();
         io.spos = fb == Body::FieldF2 ? pos2_.template as<float4>() : pos4();

@@ -14,6 +14,19 @@ device ms per call (packing included), pairs/s and algorithmic TFLOP/s.
 jittered-lattice cylinder (r = 0.3, height 1) of N particles: the field
 operator G(m) through mf_apply_field, the force through mf_eval_force after a
 CG solve; per-stage device times come from the handle's event timing.
+
+    python magnetic-force_gb300/microbench.py --kernel engine_field --n 65536 --reps 5
+
+``engine_field`` / ``engine_force`` run the all-pairs products of a Solver
+handle (the same jittered-lattice sphere, FP32, block shapes from the
+autotuner) with the handle's event timing: G(m) through mf_apply_field and
+the force through mf_eval_force.  This is the launch shape the solver and
+the bench use.
+
+Every mode brackets its measured repetitions with the CUDA profiler range
+(cudaProfilerStart / cudaProfilerStop), so an Nsight Compute capture given
+``--profile-from-start off`` sees those launches only, not the warm-up or
+tuning launches.
 """
 from __future__ import annotations
 
@@ -30,7 +43,8 @@ FLOP = {"field": 32.0, "force": 53.0, "tensor": 53.0}
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force"])
+    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force",
+                                                      "engine_field", "engine_force"])
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
@@ -44,6 +58,8 @@ def main():
 
     if args.kernel.startswith("fmm"):
         return fmm(args, np, torch, mfgb, scenes)
+    if args.kernel.startswith("engine"):
+        return engine(args, np, torch, mfgb, scenes)
     sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
     rng = np.random.default_rng(2)
     m = (rng.normal(size=(sc.n, 3)) * sc.volume).astype(np.float32)
@@ -61,6 +77,8 @@ def main():
         for _ in range(args.warmup):
             call()
         times = []
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
         for _ in range(args.reps):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -69,6 +87,7 @@ def main():
             e1.record()
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
+        torch.cuda.profiler.stop()
         best = min(times)
         pairs = float(sc.n) * sc.n
         print(json.dumps({"kernel": kind, "n": sc.n, "ms_best": best, "ms_all": times,
@@ -90,9 +109,12 @@ def fmm(args, np, torch, mfgb, scenes):
         s.apply_field(m) if args.kernel == "fmm_field" else s.evaluate_fitted_near_foece()
     s.set_option("kernel_timing", 1)
     s.reset_counters()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
     for _ in range(args.reps):
         s.apply_field(m) if args.kernel == "fmm_field" else s.evaluate_fitted_near_foece()
     torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     kind = "field" if args.kernel == "fmm_field" else "force"
     whole = s.kernel_stats(kind)
     near = s.kernel_stats("fmm_near_" + kind)
@@ -105,6 +127,35 @@ def fmm(args, np, torch, mfgb, scenes):
                       "near_tflops": FLOP[kind] * st["p2p_pairs"] / (near["total_ms"] / r * 1e-3) / 1e12,
                       "effective_pairs_per_s": float(sc.n) ** 2 / (whole["total_ms"] / r * 1e-3),
                       "fmm": st}), flush=True)
+
+
+def engine(args, np, torch, mfgb, scenes):
+    sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
+    s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
+    s.set_option("fmm", mfgb.FMM_OFF)
+    rng = np.random.default_rng(2)
+    m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.volume).astype(np.float32)
+    field = args.kernel == "engine_field"
+    if not field:
+        s.solve(50)
+    for _ in range(args.warmup):
+        s.apply_field(m) if field else s.evaluate_fitted_near_foece()
+    s.set_option("kernel_timing", 1)
+    s.reset_counters()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    for _ in range(args.reps):
+        s.apply_field(m) if field else s.evaluate_fitted_near_foece()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    kind = "field" if field else "force"
+    st = s.kernel_stats(kind)
+    r = max(st["launches"], 1)
+    ms = st["total_ms"] / r
+    pairs = float(sc.n) * sc.n
+    print(json.dumps({"kernel": args.kernel, "n": sc.n, "kernel_ms": ms, "pairs_per_s": pairs / (ms * 1e-3),
+                      "tflops": FLOP[kind] * pairs / (ms * 1e-3) / 1e12,
+                      "autotune": mfgb.autotune_report()}), flush=True)
 
 
 if __name__ == "__main__":
