@@ -181,12 +181,15 @@ __global__ void k_gather_sorted(const int32_t* __restrict__ perm, const float4* 
 }
 
 // Near-field correction, one warp per cell: up to kT of the cell's particles
-// are the targets of a pass, held in shared memory (read as broadcasts); the
-// lanes split the candidate sources of the neighbourhood (rows of cells
-// trimmed to the cell-level distance bound of the near radius, each one
-// contiguous range of the cell-ordered copies), each lane sweeping its
-// sources in increasing order, and every target's sum is finished by a fixed
-// shuffle tree, so results are deterministic.
+// are the targets of a pass, held in shared memory (read as broadcasts).  The
+// candidate sources of the neighbourhood are rows of cells trimmed to the
+// cell-level distance bound of the near radius, each one contiguous range of
+// the cell-ordered copies.  The rows are listed once per cell (start and
+// prefix offset in shared memory) and their ranges are concatenated, so the
+// lanes split one flat candidate index space: every sweep of the warp covers
+// 32 candidates whatever the rows' lengths.  Each lane sweeps its candidates
+// in increasing order, and every target's sum is finished by a fixed shuffle
+// tree, so results are deterministic.
 template <bool kForce>
 __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __restrict__ grids, int n_scenes,
                                                           int64_t n_cells, const int32_t* __restrict__ perm,
@@ -197,9 +200,11 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
                                                           const double* __restrict__ done_flags, int done_stride,
                                                           const int32_t* __restrict__ done_count, int done_total) {
   constexpr int kT = 8;
+  constexpr int kRows = 81;  // (2R + 1)^2 row slots, R <= 4 (cells are at least h wide)
   if (done_count && *done_count >= done_total) return;
   __shared__ float s_tbl[40];
   __shared__ float4 s_tp[4][kT], s_tm[4][kT];
+  __shared__ int32_t s_rb[4][kRows], s_ro[4][kRows + 1];
   if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -226,6 +231,41 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
     float cA, cB;
     if (kForce) clamped_force_coeffs(near2, cA, cB);
     else clamped_field_coeffs(near2, cA, cB);
+    // Row list of this cell: slot i = (dy, dz) in row-major order; a row
+    // outside the grid or beyond the near radius has length 0.
+    const int side = 2 * R + 1, n_slots = side * side;
+    int32_t total = 0;
+    __syncwarp();
+    for (int i0 = 0; i0 < n_slots; i0 += 32) {
+      const int i = i0 + lane;
+      int32_t sb = 0, len = 0;
+      if (i < n_slots) {
+        const int dy = i % side - R, dz = i / side - R;
+        const int cy = iy + dy, cz = iz + dz;
+        const float gy = float(max(abs(dy) - 1, 0)) * cs, gz = float(max(abs(dz) - 1, 0)) * cs;
+        const float rem = near2 - gz * gz - gy * gy;
+        if (cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz && rem >= 0.f) {
+          const int dxm = min(R, int(sqrtf(rem) * g.inv_cs) + 1);
+          const int cx0 = max(ix - dxm, 0), cx1 = min(ix + dxm, g.nx - 1);
+          const int64_t row = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx;
+          sb = start[row + cx0];
+          len = start[row + cx1 + 1] - sb;
+        }
+      }
+      int32_t inc = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+      }
+      if (i < n_slots) {
+        s_rb[wi][i] = sb;
+        s_ro[wi][i] = total + inc - len;
+      }
+      total += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) s_ro[wi][n_slots] = total;
+    __syncwarp();
     for (int32_t t0 = cb; t0 < ce; t0 += kT) {
       const int nt = min(kT, ce - t0);
       __syncwarp();
@@ -237,21 +277,12 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
       float acc[kT][3];
 #pragma unroll
       for (int t = 0; t < kT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = 0.f;
-      for (int dz = -R; dz <= R; ++dz) {
-        const int cz = iz + dz;
-        if (cz < 0 || cz >= g.nz) continue;
-        const float gz = float(max(abs(dz) - 1, 0)) * cs;
-        for (int dy = -R; dy <= R; ++dy) {
-          const int cy = iy + dy;
-          if (cy < 0 || cy >= g.ny) continue;
-          const float gy = float(max(abs(dy) - 1, 0)) * cs;
-          const float rem = near2 - gz * gz - gy * gy;
-          if (rem < 0.f) continue;  // the whole row lies beyond the near radius
-          const int dxm = min(R, int(sqrtf(rem) * g.inv_cs) + 1);
-          const int cx0 = max(ix - dxm, 0), cx1 = min(ix + dxm, g.nx - 1);
-          const int64_t row = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx;
-          const int32_t sb = start[row + cx0], se = start[row + cx1 + 1];
-          for (int32_t q = sb + lane; q < se; q += 32) {
+      {
+        int r = 0;  // this lane's row cursor (its candidates only increase)
+        for (int32_t k = lane; k < total; k += 32) {
+          while (s_ro[wi][r + 1] <= k) ++r;
+          const int32_t q = s_rb[wi][r] + (k - s_ro[wi][r]);
+          {
             const float4 pj = spos[q];
             const float4 mj = smom[q];
 #pragma unroll
