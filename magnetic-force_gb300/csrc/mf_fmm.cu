@@ -596,9 +596,6 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   int fail_k = 0, fail_ns = 0;
   for (int t0 = 0; t0 < n && !failed; t0 += kP2PThreads) {
     const bool act = t0 + tid < n;
-    // A warp without a live target skips the pair sweeps (it still takes
-    // part in every barrier and wait).
-    const bool warp_live = t0 + (tid & ~31) < n;
     const int32_t i = p.tperm[st0 + (act ? t0 + tid : 0)];
     typename Body::TData td;
     Body::load(a, i, td);
@@ -627,7 +624,7 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
           fail_ns = ns;
           break;
         }
-        const int n_items = warp_live ? (s_steps[k].y >> 1) : 0;
+        const int n_items = s_steps[k].y >> 1;
         const float4* __restrict__ sp = stage_pos(s);
         const float4* __restrict__ sm = stage_mom(s);
         typename Body::Acc acc;

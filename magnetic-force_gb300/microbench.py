@@ -15,6 +15,12 @@ jittered-lattice cylinder (r = 0.3, height 1) of N particles: the field
 operator G(m) through mf_apply_field, the force through mf_eval_force after a
 CG solve; per-stage device times come from the handle's event timing.
 
+    python magnetic-force_gb300/microbench.py --kernel fmm_step --n 1048576 --reps 1
+
+``fmm_step`` runs whole timesteps (mf_advance: octree rebuild from the moved
+positions, CG solve, force) of the same cylinder through the FMM, so a
+capture sees the tree and expansion passes as well as the products.
+
     python magnetic-force_gb300/microbench.py --kernel engine_field --n 65536 --reps 5
 
 ``engine_field`` / ``engine_force`` run the all-pairs products of a Solver
@@ -43,7 +49,7 @@ FLOP = {"field": 32.0, "force": 53.0, "tensor": 53.0}
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force",
+    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force", "fmm_step",
                                                       "engine_field", "engine_force"])
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
@@ -105,6 +111,8 @@ def fmm(args, np, torch, mfgb, scenes):
     m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.volume).astype(np.float32)
     if args.kernel == "fmm_force":
         s.solve(200)
+    if args.kernel == "fmm_step":
+        return fmm_step(args, s, sc, torch)
     for _ in range(args.warmup):
         s.apply_field(m) if args.kernel == "fmm_field" else s.evaluate_fitted_near_foece()
     s.set_option("kernel_timing", 1)
@@ -127,6 +135,27 @@ def fmm(args, np, torch, mfgb, scenes):
                       "near_tflops": FLOP[kind] * st["p2p_pairs"] / (near["total_ms"] / r * 1e-3) / 1e12,
                       "effective_pairs_per_s": float(sc.n) ** 2 / (whole["total_ms"] / r * 1e-3),
                       "fmm": st}), flush=True)
+
+
+def fmm_step(args, s, sc, torch):
+    s.solve(200)
+    for _ in range(args.warmup):
+        s.advance(1e-4, 500)
+    s.set_option("kernel_timing", 1)
+    s.reset_counters()
+    torch.cuda.synchronize()
+    times = []
+    torch.cuda.profiler.start()
+    for _ in range(args.reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        s.advance(1e-4, 500)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.profiler.stop()
+    print(json.dumps({"kernel": args.kernel, "n": sc.n, "step_ms": times, "counters": s.counters()}), flush=True)
 
 
 def engine(args, np, torch, mfgb, scenes):
