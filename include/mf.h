@@ -368,8 +368,10 @@ mf_status mf_batch_reset_counters(mf_batch* b);
 /* batched launches, and retires finished requests (their final state is   */
 /* kept for mf_server_result).  Particle state stays on the device while a  */
 /* request runs.  Requests above 65,536 particles run through the FMM      */
-/* (P = 6) as their own solver on their own stream, overlapping the batch  */
-/* on the device.  A server is used by one host thread at a time.          */
+/* (P = 6) as their own solver, on a host thread and a stream of their own */
+/* started at admission: their timesteps overlap the batch on the device   */
+/* and do not wait for ticks; a tick retires them once finished.  A server */
+/* is used by one host thread at a time.                                   */
 /* ---------------------------------------------------------------------- */
 typedef struct mf_server_config {
   double hbm_budget_bytes;   /* admission budget for request state (e.g. 120e9) */
@@ -396,15 +398,25 @@ mf_status mf_server_destroy(mf_server* s);
 /* Queues a copy of the scene.  MF_ERR_BUDGET if it alone exceeds the budget. */
 mf_status mf_server_submit(mf_server* s, const mf_scene_desc* scene, int64_t* request_id);
 /* One tick; *active gets the requests that ran, *completed those retired.
- * *tick_ms (may be NULL) gets the tick's wall time. */
+ * *tick_ms (may be NULL) gets the tick's wall time.  mf_server_stats.ticks
+ * counts the ticks in which the batch took a timestep.  With only FMM
+ * requests running and none finished, a tick waits about 0.5 ms. */
 mf_status mf_server_step(mf_server* s, int32_t* active, int32_t* completed, double* tick_ms);
-/* state: 0 queued, 1 running, 2 done.  *latency_ms: submit to done (done only). */
+/* state: 0 queued, 1 running, 2 done, 3 failed (its error was returned by
+ * the mf_server_step that found it).  *latency_ms: submit to done (done only). */
 mf_status mf_server_poll(mf_server* s, int64_t request_id, int32_t* state, int32_t* steps_done,
                          double* latency_ms);
 /* Final MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0 or MF_Q_FORCE of a
  * done request, host AoS [n][3]. */
 mf_status mf_server_result(mf_server* s, int64_t request_id, int32_t quantity, float* dst);
 mf_status mf_server_get_stats(mf_server* s, mf_server_stats* out);
+/* Wall time (ms) of each timestep a request has taken so far, oldest first:
+ * for a batch member, its tick from the start until its step was done on the
+ * device (a rebatch in that tick included); for a request above 65,536
+ * particles (run by the FMM on a host thread and stream of its own), each
+ * timestep until its stream was idle.  Copies min(count, capacity) values;
+ * *count gets the number of steps taken. */
+mf_status mf_server_step_times(mf_server* s, int64_t request_id, double* ms, int32_t capacity, int32_t* count);
 
 /* mf_direct_field without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc -- hosts that

@@ -13,14 +13,18 @@
 //     a launch does nothing once all scenes have stopped, so a fixed number of
 //     iterations can be captured in a CUDA graph.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "mf_internal.h"
@@ -539,8 +543,9 @@ class Batch {
 // Serving with continuous batching.
 // ---------------------------------------------------------------------------
 // Requests above this many particles run as their own solver handle through
-// the FMM (P = 6, on its own stream, overlapping the batch on the device);
-// smaller ones join the all-pairs batch.
+// the FMM (P = 6), each on a host thread and a stream of its own, so their
+// kernels overlap the batch's on the device and their host-side waits never
+// hold up the serving loop; smaller ones join the all-pairs batch.
 constexpr int64_t kServeFmmMin = 65536;
 
 class Server {
@@ -548,8 +553,11 @@ class Server {
 
  public:
   ~Server() {
+    for (auto& kv : reqs_)
+      if (kv.second.job) kv.second.job->cancel.store(true);
+    for (auto& kv : reqs_)
+      if (kv.second.job && kv.second.job->th.joinable()) kv.second.job->th.join();
     batch_.reset();
-    for (auto& kv : reqs_) drop_solver(kv.second);
   }
 
   mf_status init(const mf_server_config& c) {
@@ -596,7 +604,9 @@ class Server {
       const double need = need_bytes(r.d.n);
       if (used_ + need > cfg_.hbm_budget_bytes) break;
       if (r.d.n > kServeFmmMin) {
-        MF_TRY(start_solver(r));
+        r.job.reset(new FmmJob());
+        FmmJob* j = r.job.get();
+        j->th = std::thread(fmm_worker, j, r.d, r.pos.data(), cfg_);
         used_ += need;
         r.phase = 1;
         fmm_active_.push_back(r.id);
@@ -614,34 +624,55 @@ class Server {
       queue_.pop_front();
       dirty_ = true;
     }
-    if (!active_.empty() || !fmm_active_.empty()) ++stats_.ticks;
     if (!active_.empty()) {
+      ++stats_.ticks;
       if (dirty_) MF_TRY(rebatch());
       MF_TRY(batch_->step(cfg_.dt, cfg_.iters_per_step, cfg_.rel_tol));  // enqueued, not waited for
     }
-    // FMM requests step on their own streams while the batch runs.
+    // FMM requests run on their own threads: retire the finished ones.
     {
       std::vector<int64_t> keep;
       for (int64_t id : fmm_active_) {
         Req& r = reqs_.at(id);
-        int64_t it = 0;
-        const mf_status s = mf_advance(r.solver, cfg_.dt, cfg_.iters_per_step, &it);
-        if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
-        ++r.steps;
-        if (r.steps >= cfg_.steps_per_request) {
-          MF_TRY(finish_solver(r));
-          used_ -= need_bytes(r.d.n);
-          ++completed;
-          ++stats_.completed;
-        } else {
+        FmmJob* j = r.job.get();
+        if (!j->done.load(std::memory_order_acquire)) {
           keep.push_back(id);
+          continue;
         }
+        j->th.join();
+        if (j->status != MF_OK) {
+          const mf_status st = j->status;
+          const std::string msg = "served FMM request: " + j->err;
+          r.job.reset();
+          r.phase = 3;
+          r.t_done = Clock::now();
+          used_ -= need_bytes(r.d.n);
+          fmm_active_.erase(std::find(fmm_active_.begin(), fmm_active_.end(), id));
+          return fail(st, msg);  // returns at once: the loop's iterator is not used again
+        }
+        r.out = std::move(j->out);
+        r.step_ms = std::move(j->step_ms);
+        r.steps = j->steps.load();
+        r.t_done = j->t_done;
+        stats_.field_pairs += j->ctr.field_pairs;
+        stats_.force_pairs += j->ctr.force_pairs;
+        r.job.reset();
+        r.phase = 2;
+        used_ -= need_bytes(r.d.n);
+        ++completed;
+        ++stats_.completed;
       }
       fmm_active_ = keep;
     }
     if (!active_.empty()) {
       MF_CUDA_TRY(cudaStreamSynchronize(batch_->stream()));
-      for (int64_t id : active_) ++reqs_.at(id).steps;
+      // each member's step latency: from the tick's start to its step done
+      const double step_ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+      for (int64_t id : active_) {
+        Req& r = reqs_.at(id);
+        ++r.steps;
+        r.step_ms.push_back(step_ms);
+      }
       // Retire finished requests: keep their final state on the host.
       std::vector<int64_t> keep;
       for (size_t k = 0; k < members_.size(); ++k) {
@@ -666,6 +697,10 @@ class Server {
         }
       }
       active_ = keep;
+    } else if (!fmm_active_.empty() && completed == 0) {
+      // Only FMM requests running and none finished: give their threads the
+      // host for a moment instead of returning to a caller that polls.
+      std::this_thread::sleep_for(std::chrono::microseconds(500));
     }
     const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
     stats_.busy_ms += ms;
@@ -680,7 +715,7 @@ class Server {
     if (it == reqs_.end()) return fail(MF_ERR_INVALID_ARG, "unknown request");
     const Req& r = it->second;
     if (phase) *phase = r.phase;
-    if (steps) *steps = r.steps;
+    if (steps) *steps = r.job ? r.job->steps.load() : r.steps;
     if (latency_ms)
       *latency_ms = r.phase == 2 ? std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count() : -1.0;
     return MF_OK;
@@ -690,6 +725,7 @@ class Server {
     auto it = reqs_.find(id);
     if (it == reqs_.end()) return fail(MF_ERR_INVALID_ARG, "unknown request");
     const Req& r = it->second;
+    if (r.phase == 3) return fail(MF_ERR_INVALID_ARG, "request failed");
     if (r.phase != 2) return fail(MF_ERR_INVALID_ARG, "request not done");
     if (!dst) return fail(MF_ERR_INVALID_ARG, "dst is NULL");
     int j = -1;
@@ -716,17 +752,47 @@ class Server {
       s.field_pairs += c.field_pairs;
       s.force_pairs += c.force_pairs;
     }
-    for (int64_t id : fmm_active_) {
-      mf_counters c{};
-      MF_TRY(mf_get_counters(reqs_.at(id).solver, &c));
-      s.field_pairs += c.field_pairs;
-      s.force_pairs += c.force_pairs;
-    }
     *out = s;
     return MF_OK;
   }
 
+  // Wall time of each timestep a request has taken so far: for a batch
+  // member, the tick from its start until the member's step was done on the
+  // device (a rebatch in that tick included); for an FMM request, each
+  // mf_advance on its thread until its stream was idle.
+  mf_status step_times(int64_t id, double* ms, int32_t cap, int32_t* count) {
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) return fail(MF_ERR_INVALID_ARG, "unknown request");
+    if (cap < 0 || (cap > 0 && !ms)) return fail(MF_ERR_INVALID_ARG, "bad output buffer");
+    Req& r = it->second;
+    std::vector<double> v;
+    if (r.job) {
+      std::lock_guard<std::mutex> lk(r.job->mu);
+      v = r.job->step_ms;
+    } else {
+      v = r.step_ms;
+    }
+    if (count) *count = int32_t(v.size());
+    std::copy(v.begin(), v.begin() + std::min<size_t>(v.size(), size_t(cap)), ms);
+    return MF_OK;
+  }
+
  private:
+  // An FMM request's thread and what it hands back.  Until `done` is set the
+  // serving loop reads only `steps` and, under `mu`, `step_ms`.
+  struct FmmJob {
+    std::thread th;
+    std::atomic<bool> done{false}, cancel{false};
+    std::atomic<int32_t> steps{0};
+    std::mutex mu;
+    std::vector<double> step_ms;
+    std::vector<std::vector<float>> out;
+    mf_counters ctr{};
+    mf_status status = MF_OK;
+    std::string err;
+    Clock::time_point t_done;
+  };
+
   struct Req {
     int64_t id = 0;
     mf_scene_desc d{};
@@ -736,58 +802,75 @@ class Server {
     int32_t steps = 0;
     Clock::time_point t_submit, t_done;
     std::vector<std::vector<float>> out;
-    mf_solver* solver = nullptr;  // FMM requests: their own solver handle
-    cudaStream_t stream = nullptr;
+    std::vector<double> step_ms;  // wall time of each timestep taken
+    std::unique_ptr<FmmJob> job;  // FMM requests while they run
   };
 
-  // An FMM request: solver handle on its own non-blocking stream, CG to the
-  // server's tolerance, FMM order 6, a converged cold solve before its first step.
-  mf_status start_solver(Req& r) {
-    mf_params p{};
-    p.num_particles = r.d.n;
-    p.h = r.d.h;
-    p.ext_mag_h = r.d.h;
-    p.volume = r.d.volume;
-    p.chi = r.d.chi;
-    for (int k = 0; k < 3; ++k) p.const_ext_field[k] = r.d.H0[k];
-    p.target_pos = r.pos.data();
-    p.precision = MF_FP32;
-    p.device = cfg_.device;
-    MF_TRY(mf_create(&p, &r.solver));
-    MF_CUDA_TRY(cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking));
-    MF_TRY(mf_set_stream(r.solver, r.stream));
-    MF_TRY(mf_set_option(r.solver, MF_OPT_SOLVER, MF_SOLVER_CG));
-    MF_TRY(mf_set_option(r.solver, MF_OPT_REL_TOL, cfg_.rel_tol));
-    MF_TRY(mf_set_option(r.solver, MF_OPT_FMM, 1));
-    MF_TRY(mf_set_option(r.solver, MF_OPT_FMM_ORDER, 6));
-    int64_t it = 0;
-    double rr = 0;
-    const mf_status s = mf_solve(r.solver, 500, &it, &rr);
-    if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
-    ++stats_.rebatches;
-    return MF_OK;
-  }
-  mf_status finish_solver(Req& r) {
-    r.out.resize(5);
-    const int qs[5] = {MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0, MF_Q_FORCE};
-    for (int j = 0; j < 5; ++j) {
-      r.out[size_t(j)].resize(size_t(3 * r.d.n));
-      MF_TRY(mf_get(r.solver, qs[j], r.out[size_t(j)].data(), MF_LAYOUT_AOS, MF_HOST));
+  // The thread of an FMM request: a solver handle on its own non-blocking
+  // stream (CG to the server's tolerance, FMM order 6), a converged cold
+  // solve, the request's timesteps, then the read-back of its final state.
+  static void fmm_worker(FmmJob* j, mf_scene_desc d, const float* pos, mf_server_config cfg) {
+    mf_solver* sv = nullptr;
+    cudaStream_t stream = nullptr;
+    auto run = [&]() -> mf_status {
+      MF_CUDA_TRY(cudaSetDevice(cfg.device));
+      mf_params p{};
+      p.num_particles = d.n;
+      p.h = d.h;
+      p.ext_mag_h = d.h;
+      p.volume = d.volume;
+      p.chi = d.chi;
+      for (int k = 0; k < 3; ++k) p.const_ext_field[k] = d.H0[k];
+      p.target_pos = pos;
+      p.precision = MF_FP32;
+      p.device = cfg.device;
+      MF_TRY(mf_create(&p, &sv));
+      MF_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+      MF_TRY(mf_set_stream(sv, stream));
+      MF_TRY(mf_set_option(sv, MF_OPT_SOLVER, MF_SOLVER_CG));
+      MF_TRY(mf_set_option(sv, MF_OPT_REL_TOL, cfg.rel_tol));
+      MF_TRY(mf_set_option(sv, MF_OPT_FMM, 1));
+      MF_TRY(mf_set_option(sv, MF_OPT_FMM_ORDER, 6));
+      int64_t it = 0;
+      double rr = 0;
+      mf_status s = mf_solve(sv, 500, &it, &rr);
+      if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
+      for (int k = 0; k < cfg.steps_per_request; ++k) {
+        if (j->cancel.load()) return MF_OK;
+        const auto t0 = Clock::now();
+        s = mf_advance(sv, cfg.dt, cfg.iters_per_step, &it);
+        if (s != MF_OK && s != MF_ERR_NOT_CONVERGED) return s;
+        MF_CUDA_TRY(cudaStreamSynchronize(stream));
+        const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        {
+          std::lock_guard<std::mutex> lk(j->mu);
+          j->step_ms.push_back(ms);
+        }
+        j->steps.fetch_add(1);
+      }
+      j->out.resize(5);
+      const int qs[5] = {MF_Q_POSITIONS, MF_Q_VELOCITY, MF_Q_M, MF_Q_B_OVER_MU0, MF_Q_FORCE};
+      for (int q = 0; q < 5; ++q) {
+        j->out[size_t(q)].resize(size_t(3 * d.n));
+        MF_TRY(mf_get(sv, qs[q], j->out[size_t(q)].data(), MF_LAYOUT_AOS, MF_HOST));
+      }
+      MF_TRY(mf_get_counters(sv, &j->ctr));
+      return MF_OK;
+    };
+    mf_status s = MF_OK;
+    try {
+      s = run();
+    } catch (const std::bad_alloc&) {
+      s = fail(MF_ERR_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+      s = fail(MF_ERR_CUDA, e.what());
     }
-    mf_counters c{};
-    MF_TRY(mf_get_counters(r.solver, &c));
-    stats_.field_pairs += c.field_pairs;
-    stats_.force_pairs += c.force_pairs;
-    drop_solver(r);
-    r.phase = 2;
-    r.t_done = Clock::now();
-    return MF_OK;
-  }
-  static void drop_solver(Req& r) {
-    if (r.solver) mf_destroy(r.solver);
-    if (r.stream) cudaStreamDestroy(r.stream);
-    r.solver = nullptr;
-    r.stream = nullptr;
+    if (s != MF_OK) j->err = mf_last_error();
+    if (sv) mf_destroy(sv);
+    if (stream) cudaStreamDestroy(stream);
+    j->status = s;
+    j->t_done = Clock::now();
+    j->done.store(true, std::memory_order_release);
   }
 
   Batch::SceneState state_of(Req& r) {
@@ -921,6 +1004,10 @@ mf_status mf_server_get_stats(mf_server* s, mf_server_stats* out) {
     if (!out) return fail(MF_ERR_INVALID_ARG, "NULL");
     return x.get_stats(out);
   });
+}
+
+mf_status mf_server_step_times(mf_server* s, int64_t request_id, double* ms, int32_t capacity, int32_t* count) {
+  return sguard(s, [&](Server& x) { return x.step_times(request_id, ms, capacity, count); });
 }
 
 }  // extern "C"

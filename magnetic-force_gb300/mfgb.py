@@ -451,7 +451,8 @@ class Server:
                 ("mf_server_step", i32, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(f64)]),
                 ("mf_server_poll", i32, [vp, i64, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(f64)]),
                 ("mf_server_result", i32, [vp, i64, i32, vp]),
-                ("mf_server_get_stats", i32, [vp, ctypes.POINTER(mf_server_stats)])):
+                ("mf_server_get_stats", i32, [vp, ctypes.POINTER(mf_server_stats)]),
+                ("mf_server_step_times", i32, [vp, i64, ctypes.POINTER(f64), i32, ctypes.POINTER(i32)])):
             f = getattr(lib, name)
             f.restype = res
             f.argtypes = args
@@ -494,6 +495,15 @@ class Server:
         st, steps, lat = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_double(0)
         check(load().mf_server_poll(self._h, int(rid), ctypes.byref(st), ctypes.byref(steps), ctypes.byref(lat)))
         return st.value, steps.value, lat.value
+
+    def step_times(self, rid) -> np.ndarray:
+        """Wall time (ms) of each timestep the request has taken so far."""
+        n = ctypes.c_int32(0)
+        check(load().mf_server_step_times(self._h, int(rid), None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), dtype=np.float64)
+        check(load().mf_server_step_times(self._h, int(rid), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          len(out), ctypes.byref(n)))
+        return out[:n.value]
 
     def result(self, rid, quantity: str) -> np.ndarray:
         out = np.empty((self.sizes[rid], 3), dtype=np.float32)

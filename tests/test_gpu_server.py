@@ -49,6 +49,9 @@ def test_alone_equals_in_the_mix(mf):
         srv.step()
     st = srv.stats()
     assert st["completed"] == len(scs) and st["rebatches"] >= 2
+    for i in ids:
+        t = srv.step_times(i)
+        assert len(t) == steps and np.all(t > 0)
     for k in (0, 2, 3):
         alone = run_alone(mf, scs[k], steps)
         for q, v in alone.items():
@@ -82,8 +85,9 @@ def test_budget_enforced(mf):
 
 def test_fmm_request_in_the_mix(mf):
     # A request above 65,536 particles runs as its own FMM solver (P = 6) on
-    # its own stream beside the batch; its result equals the same solver run
-    # alone with the same settings, and the small requests are unaffected.
+    # a host thread and a stream of its own beside the batch; its result
+    # equals the same solver run alone with the same settings, and the small
+    # requests are unaffected.
     import scenes
     big = scenes.jittered_lattice(70000, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=77)
     small = scenes_for((900, 1700), seed=51)
@@ -96,6 +100,9 @@ def test_fmm_request_in_the_mix(mf):
         srv.step()
     st = srv.stats()
     assert st["completed"] == 3 and st["force_pairs"] > 0
+    # the FMM request took its timesteps on its own thread, each timed
+    t = srv.step_times(ids[1])
+    assert len(t) == steps and np.all(t > 0)
     # the big request against a standalone FMM solver with the server's settings
     s = mf.Solver(big.n, big.h, big.h, big.volume, big.chi, big.H0, None, None, big.pos)
     s.set_option("solver", mf.SOLVER_CG)
