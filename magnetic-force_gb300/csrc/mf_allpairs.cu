@@ -66,8 +66,8 @@ mf_status DevBuf::reserve(size_t want, bool keep, bool zero) {
 }
 
 mf_status Scratch::ensure(size_t partial_doubles, size_t n_counters) {
-  MF_TRY(partials.reserve(partial_doubles * sizeof(double)));
-  MF_TRY(counters.reserve(n_counters * sizeof(int32_t), /*keep=*/true, /*zero=*/true));
+  MF_TRY(partials.reserve_grow(partial_doubles * sizeof(double)));
+  MF_TRY(counters.reserve_grow(n_counters * sizeof(int32_t), /*keep=*/true, /*zero=*/true));
   MF_TRY(err.reserve(16, true, true));
   return MF_OK;
 }
@@ -301,7 +301,7 @@ mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>&
   plan.n_scenes = int32_t(plan.host.size());
   plan.pairs = pairs;
   const size_t bytes = plan.host.size() * sizeof(SceneDesc<Real>);
-  MF_TRY(plan.d_scenes.reserve(bytes));
+  MF_TRY(plan.d_scenes.reserve_grow(bytes));
   if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
   return MF_OK;
 }

@@ -130,14 +130,19 @@ class Batch {
       max_n = std::max(max_n, x.n);
     }
     n_alloc_ = off;
-    MF_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+    if (!own_stream_) MF_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
     st_ = own_stream_;
-    MF_CUDA_TRY(cudaMallocHost(&pinned_, 64));
+    if (!pinned_) MF_CUDA_TRY(cudaMallocHost(&pinned_, 64));
 
+    // Buffers may come from an earlier layout (adopt_buffers): clear them.
     const size_t v4 = size_t(n_alloc_ + 2) * sizeof(float4);
-    for (DevBuf* b : {&pos4_, &pos2_, &vel4_, &b4_, &r4_, &p4_, &q4_, &hext4_, &mom4_, &mom2_, &corr_})
-      MF_TRY(b->reserve(v4, false, true));
-    MF_TRY(fs_.reserve(size_t(3 * n_alloc_) * sizeof(float), false, true));
+    for (DevBuf* b : {&pos4_, &pos2_, &vel4_, &b4_, &r4_, &p4_, &q4_, &hext4_, &mom4_, &mom2_, &corr_}) {
+      MF_TRY(b->reserve_grow(v4));
+      MF_CUDA_TRY(cudaMemsetAsync(b->ptr, 0, v4, st_));
+    }
+    MF_TRY(fs_.reserve_grow(size_t(3 * n_alloc_) * sizeof(float)));
+    MF_CUDA_TRY(cudaMemsetAsync(fs_.ptr, 0, size_t(3 * n_alloc_) * sizeof(float), st_));
+    MF_CUDA_TRY(cudaStreamSynchronize(st_));
 
     // Positions, external field, solver constants.
     std::vector<float4> hp(size_t(n_alloc_ + 2), make_float4(0.f, 0.f, 0.f, 0.f));
@@ -174,14 +179,16 @@ class Batch {
       MF_CUDA_TRY(cudaStreamSynchronize(st_));
     }
     MF_CUDA_TRY(cudaMemcpy(hext4_.ptr, hh.data(), v4, cudaMemcpyHostToDevice));
-    MF_TRY(scal_.reserve(rows.size() * sizeof(double)));
+    MF_TRY(scal_.reserve_grow(rows.size() * sizeof(double)));
     MF_CUDA_TRY(cudaMemcpy(scal_.ptr, rows.data(), rows.size() * sizeof(double), cudaMemcpyHostToDevice));
-    MF_TRY(ranges_.reserve(rg.size() * sizeof(VecRange)));
+    MF_TRY(ranges_.reserve_grow(rg.size() * sizeof(VecRange)));
     MF_CUDA_TRY(cudaMemcpy(ranges_.ptr, rg.data(), rg.size() * sizeof(VecRange), cudaMemcpyHostToDevice));
     red_gx_ = int(std::min<int64_t>((max_n + 255) / 256, 16));
-    MF_TRY(red_part_.reserve(size_t(n) * red_gx_ * 2 * sizeof(double)));
-    MF_TRY(red_tickets_.reserve(size_t(n) * sizeof(int32_t), false, true));
-    MF_TRY(done_count_.reserve(16, false, true));
+    MF_TRY(red_part_.reserve_grow(size_t(n) * red_gx_ * 2 * sizeof(double)));
+    MF_TRY(red_tickets_.reserve_grow(size_t(n) * sizeof(int32_t)));
+    MF_CUDA_TRY(cudaMemsetAsync(red_tickets_.ptr, 0, size_t(n) * sizeof(int32_t), st_));
+    MF_TRY(done_count_.reserve(16));
+    MF_CUDA_TRY(cudaMemsetAsync(done_count_.ptr, 0, 16, st_));
 
     // Launch plans, one scene table per kind of product and path: [0] the
     // exact-branch kernels for scenes below kPacked*Min, [1] the packed
@@ -256,6 +263,36 @@ class Batch {
   void set_stream(cudaStream_t s) {
     st_ = s ? s : own_stream_;
     drop_graph();
+  }
+
+  // Takes over another batch's device buffers, stream and pinned word (a
+  // serving rebatch, with `o` idle): init() then grows only what is too
+  // small, so a membership change usually frees and allocates nothing --
+  // cudaFree would wait for every stream of the device, the FMM requests'
+  // included.
+  void adopt_buffers(Batch& o) {
+    std::swap(own_stream_, o.own_stream_);
+    st_ = own_stream_;
+    std::swap(pinned_, o.pinned_);
+    for (auto pr : {std::make_pair(&pos4_, &o.pos4_), std::make_pair(&pos2_, &o.pos2_),
+                    std::make_pair(&vel4_, &o.vel4_), std::make_pair(&b4_, &o.b4_), std::make_pair(&r4_, &o.r4_),
+                    std::make_pair(&p4_, &o.p4_), std::make_pair(&q4_, &o.q4_), std::make_pair(&hext4_, &o.hext4_),
+                    std::make_pair(&mom4_, &o.mom4_), std::make_pair(&mom2_, &o.mom2_),
+                    std::make_pair(&corr_, &o.corr_), std::make_pair(&fs_, &o.fs_),
+                    std::make_pair(&scal_, &o.scal_), std::make_pair(&ranges_, &o.ranges_),
+                    std::make_pair(&red_part_, &o.red_part_), std::make_pair(&red_tickets_, &o.red_tickets_),
+                    std::make_pair(&done_count_, &o.done_count_)})
+      *pr.first = std::move(*pr.second);
+    scr_ = std::move(o.scr_);
+    cells_ = std::move(o.cells_);
+    for (int p = 0; p < 2; ++p) {  // launch plans: their device tables
+      for (auto pr : {std::make_pair(&plan_resid_[p], &o.plan_resid_[p]), std::make_pair(&plan_cgq_[p], &o.plan_cgq_[p]),
+                      std::make_pair(&plan_force_[p], &o.plan_force_[p])}) {
+        *pr.first = std::move(*pr.second);
+        pr.first->n_scenes = 0;
+        pr.first->host.clear();
+      }
+    }
   }
   int scenes() const { return int(sc_.size()); }
 
@@ -614,7 +651,7 @@ class Server {
         continue;
       }
       const size_t bytes = size_t(r.d.n) * sizeof(float4);
-      MF_TRY(r.state.reserve(3 * bytes, false, true));
+      MF_TRY(take_state(r.state, 3 * bytes));
       std::vector<float4> p(size_t(r.d.n));
       for (int64_t i = 0; i < r.d.n; ++i) p[size_t(i)] = make_float4(r.pos[3 * i], r.pos[3 * i + 1], r.pos[3 * i + 2], 0.f);
       MF_CUDA_TRY(cudaMemcpy(r.state.ptr, p.data(), bytes, cudaMemcpyHostToDevice));
@@ -685,7 +722,7 @@ class Server {
             r.out[size_t(j)].resize(size_t(3 * r.d.n));
             MF_TRY(batch_->get(s, qs[j], r.out[size_t(j)].data()));
           }
-          r.state.release();
+          give_state(std::move(r.state));
           used_ -= need_bytes(r.d.n);
           r.phase = 2;
           r.t_done = Clock::now();
@@ -873,6 +910,34 @@ class Server {
     j->done.store(true, std::memory_order_release);
   }
 
+  // Device state of retired batch members is kept for later admissions:
+  // cudaFree would wait for every stream of the device, the FMM requests'
+  // included.  At most kPoolMax buffers are kept; they are not counted in
+  // the admission budget (the requests that used them were).
+  static constexpr size_t kPoolMax = 16;
+  mf_status take_state(DevBuf& dst, size_t bytes) {
+    size_t best = pool_.size();
+    for (size_t k = 0; k < pool_.size(); ++k)
+      if (pool_[k].bytes >= bytes && (best == pool_.size() || pool_[k].bytes < pool_[best].bytes)) best = k;
+    if (best < pool_.size()) {
+      dst = std::move(pool_[best]);
+      pool_.erase(pool_.begin() + std::ptrdiff_t(best));
+    } else {
+      MF_TRY(dst.reserve(bytes));
+    }
+    MF_CUDA_TRY(cudaMemset(dst.ptr, 0, bytes));
+    return MF_OK;
+  }
+  void give_state(DevBuf&& b) {
+    pool_.push_back(std::move(b));
+    if (pool_.size() > kPoolMax) {  // drop the smallest
+      size_t k = 0;
+      for (size_t j = 1; j < pool_.size(); ++j)
+        if (pool_[j].bytes < pool_[k].bytes) k = j;
+      pool_.erase(pool_.begin() + std::ptrdiff_t(k));
+    }
+  }
+
   Batch::SceneState state_of(Req& r) {
     float4* base = r.state.as<float4>();
     return Batch::SceneState{base, base + r.d.n, base + 2 * r.d.n};
@@ -892,7 +957,6 @@ class Server {
       MF_TRY(batch_->counters(&c));
       stats_.field_pairs += c.field_pairs;
       stats_.force_pairs += c.force_pairs;
-      batch_.reset();
     }
     members_ = active_;
     std::vector<mf_scene_desc> descs;
@@ -902,7 +966,12 @@ class Server {
       descs.push_back(r.d);
       st.push_back(state_of(r));
     }
-    batch_.reset(new Batch());
+    std::unique_ptr<Batch> nb(new Batch());
+    if (batch_) {
+      nb->adopt_buffers(*batch_);
+      batch_.reset();
+    }
+    batch_ = std::move(nb);
     batch_->device_ = cfg_.device;
     // Rebatching happens between timesteps: use tuned shapes already cached,
     // never time new ones on the request path.
@@ -919,6 +988,7 @@ class Server {
   std::deque<int64_t> queue_;
   std::vector<int64_t> active_, members_, fmm_active_;
   std::unique_ptr<Batch> batch_;
+  std::vector<DevBuf> pool_;  // device state of retired batch members, for reuse
   bool dirty_ = false;
   double used_ = 0;
   int64_t next_id_ = 1;

@@ -582,7 +582,7 @@ mf_status CellList::field_correction(const float4* pos4, const float4* mom4, flo
                                                       smom_.as<float4>(), done_count, done_total);
   k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip_field_.as<int32_t>(), done_flags, done_stride, done_count, done_total);
+      smom_.as<float4>(), corr, skip_field_on_ ? skip_field_.as<int32_t>() : nullptr, done_flags, done_stride, done_count, done_total);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }
@@ -607,20 +607,20 @@ mf_status CellList::tensor_correction_at(const float4* tpos4, int64_t nt, const 
 }
 
 mf_status CellList::set_skips(const std::vector<int32_t>& field, const std::vector<int32_t>& force) {
-  auto put = [&](const std::vector<int32_t>& v, DevBuf& b) -> mf_status {
+  // A list without skips is not passed to the kernels; its buffer is kept
+  // (freeing would wait for every stream of the device).
+  auto put = [&](const std::vector<int32_t>& v, DevBuf& b, bool& on) -> mf_status {
     bool any = false;
     for (int32_t x : v) any = any || x != 0;
-    if (!any) {
-      b.release();
-      return MF_OK;
-    }
+    on = any;
+    if (!any) return MF_OK;
     if (int(v.size()) != n_scenes_) return fail(MF_ERR_INVALID_ARG, "skip list size");
     MF_TRY(b.reserve(v.size() * sizeof(int32_t)));
     MF_CUDA_TRY(cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     return MF_OK;
   };
-  MF_TRY(put(field, skip_field_));
-  MF_TRY(put(force, skip_force_));
+  MF_TRY(put(field, skip_field_, skip_field_on_));
+  MF_TRY(put(force, skip_force_, skip_force_on_));
   return MF_OK;
 }
 
@@ -629,7 +629,7 @@ mf_status CellList::force_correction(const float4* pos4, const float4* mom4, flo
                                                       smom_.as<float4>(), nullptr, 0);
   k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip_force_.as<int32_t>(), nullptr, 0, nullptr, 0);
+      smom_.as<float4>(), corr, skip_force_on_ ? skip_force_.as<int32_t>() : nullptr, nullptr, 0, nullptr, 0);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -66,6 +67,13 @@ struct DevBuf {
   // by the particles' current extent (cell and box grids), which change a
   // little every timestep and would otherwise reallocate often.
   mf_status reserve_slack(size_t want) { return want <= bytes ? MF_OK : reserve(want + want / 4 + 256); }
+  // Same, at least doubling when it has to grow: for buffers whose size
+  // follows a changing set of scenes (batch layouts, launch plans, scratch),
+  // so that growth -- whose cudaFree waits for every stream of the device --
+  // happens a logarithmic number of times.
+  mf_status reserve_grow(size_t want, bool keep = false, bool zero = false) {
+    return want <= bytes ? MF_OK : reserve(std::max(want, 2 * bytes), keep, zero);
+  }
   template <class T>
   T* as() const {
     return static_cast<T*>(ptr);
@@ -299,6 +307,7 @@ class CellList {
  private:
   DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
+  bool skip_field_on_ = false, skip_force_on_ = false;  // a list is in use
   DevBuf spos_, smom_;              // positions and dipoles in cell order (per correction)
   std::vector<CellGrid> host_grids_;
   std::vector<double> host_bbox_;
