@@ -272,7 +272,7 @@ def run_ours(args, rank, world, local):
                 "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
                 "kernels": kern,
                 "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores; "
-                        "HBM traffic per launch is ~1 MB of particle records"}
+                        "DRAM traffic per launch: the 2 MB of pair-layout records, read about twice (L2 absorbs the rest)"}
 
     # accuracy on a sample: fixed-point residual and force, FP64 oracle
     errors = None
@@ -694,8 +694,12 @@ def run_fmm(args, rank, world, local):
                           "tflops": fpp * k["pairs"] / (k["total_ms"] * 1e-3) / 1e12}
     far = ks["fmm_far"]
     dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath) and n == 1 << 20:
+        traffic = json.load(open(tpath)).get(f"fmm_p2p_{'force' if dom.endswith('force') else 'field'}_fp32_{n}")
     roofline = {"bound": "fp32", "achieved": round(kern[dom]["tflops"], 3), "peak": round(peak, 3),
-                "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": None,
+                "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": traffic,
                 "kernel": f"k_fmm_p2p<{'force' if dom.endswith('force') else 'field'}>",
                 "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
                 "kernels": kern,
