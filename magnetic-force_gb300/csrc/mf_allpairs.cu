@@ -158,6 +158,7 @@ template <class Real, Body B, int S = 0>
 struct Launcher {
   using C = LCfg<Real, B, S>;
   using BT = typename BodyOf<Real, B>::type;
+  static_assert(BT::kOut == C::kOut, "partial-sum slots must match the body's outputs");
   static constexpr int TBT = C::TPB * C::TPT;
   static constexpr size_t kSmem = size_t(C::STAGES) * StageLayout<Real, C::TILE>::kBytes;
 

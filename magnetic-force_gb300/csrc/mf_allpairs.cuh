@@ -352,16 +352,20 @@ struct FieldF2Body : PairItems {
   }
 };
 
+// Outputs: the three force sums without the target-dipole term, and the
+// scalar sum u of r^-5 (d.s) that the epilogue multiplies by the target's
+// dipole (force_pair2).
 struct ForceF2Body : PairItems {
-  static constexpr int kOut = 3;
+  static constexpr int kOut = 4;
   struct TData {
     float2 x, y, z, mx, my, mz;
   };
   struct Acc {
-    float2 f[3];
+    float2 f[3], u;
     __device__ void zero() {
 #pragma unroll
       for (int k = 0; k < 3; ++k) f[k] = make_float2(0.f, 0.f);
+      u = make_float2(0.f, 0.f);
     }
   };
   __device__ static void load(const AllPairsArgs<float>& a, int64_t i, TData& t) {
@@ -375,16 +379,20 @@ struct ForceF2Body : PairItems {
     t.mz = f2_dup(m.z);
   }
   __device__ static void pair(const TData& t, const Item& it, const PairConsts<float>& pc, Acc& acc) {
-    force_pair2(t.x, t.y, t.z, t.mx, t.my, t.mz, it.x, it.y, it.z, it.mx, it.my, it.mz, pc.near2_force, acc.f);
+    force_pair2(t.x, t.y, t.z, t.mx, t.my, t.mz, it.x, it.y, it.z, it.mx, it.my, it.mz, pc.near2_force, acc.f,
+                acc.u);
   }
   __device__ static void tile_out(const Acc& acc, float* o) {
     const float c = float(kForceK);
 #pragma unroll
     for (int k = 0; k < 3; ++k) o[k] = (acc.f[k].x + acc.f[k].y) * c;
+    o[3] = (acc.u.x + acc.u.y) * c;
   }
   __device__ static void epilogue(const AllPairsArgs<float>& a, const SceneDesc<float>& sc, int64_t i,
                                   const TData& t, const double* v) {
-    force_epilogue<float>(a, sc, i, double(t.mx.x), double(t.my.x), double(t.mz.x), v);
+    const double mx = double(t.mx.x), my = double(t.my.x), mz = double(t.mz.x);
+    const double f[3] = {v[0] + mx * v[3], v[1] + my * v[3], v[2] + mz * v[3]};
+    force_epilogue<float>(a, sc, i, mx, my, mz, f);
   }
 };
 

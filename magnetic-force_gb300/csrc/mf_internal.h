@@ -118,7 +118,7 @@ struct KCfg<float, Body::FieldF2> {
 };
 template <>
 struct KCfg<float, Body::ForceF2> {
-  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 3;
+  static constexpr int TPB = 256, TPT = 2, TILE = 256, STAGES = 3, kOut = 4;
 };
 // FP64: 128 threads x 1 target, 128-source tiles of 32-byte records.
 template <>

@@ -234,10 +234,13 @@ __device__ __forceinline__ void field_pair2(float2 tx, float2 ty, float2 tz, flo
   s2[2] = f2_fma(mz, beta, s2[2]);
 }
 
-// f += T(d, s) m / K with the far (P, Q) = (r^-5, -5 r^-7) of the clamped distance.
+// f += T(d, s) m / K with the far (P, Q) = (r^-5, -5 r^-7) of the clamped
+// distance, in two parts: f gets d w + s v, and u the scalar sum of
+// r^-5 (d.s) whose product with the target's dipole m completes the force
+// (the caller applies it once per tile: 3 packed operations fewer per pair).
 __device__ __forceinline__ void force_pair2(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
                                             float2 sx, float2 sy, float2 sz, float2 smx, float2 smy, float2 smz,
-                                            float near2, float2* f) {
+                                            float near2, float2* f, float2& u) {
   const float2 dx = f2_sub(tx, sx), dy = f2_sub(ty, sy), dz = f2_sub(tz, sz);
   const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
   const float2 ri = clamp_rsqrt2(r2, near2);
@@ -246,13 +249,13 @@ __device__ __forceinline__ void force_pair2(float2 tx, float2 ty, float2 tz, flo
   const float2 ds = f2_fma(dz, smz, f2_fma(dy, smy, f2_mul(dx, smx)));
   const float2 dm = f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx)));
   const float2 sm = f2_fma(smz, tmz, f2_fma(smy, tmy, f2_mul(smx, tmx)));
-  const float2 u = f2_mul(ds, ri5);
   const float2 v = f2_mul(dm, ri5);
   const float2 e = f2_mul(f2_mul(ri2, ds), f2_dup(-5.f));
   const float2 w = f2_fma(e, v, f2_mul(sm, ri5));
-  f[0] = f2_fma(dx, w, f2_fma(tmx, u, f2_fma(smx, v, f[0])));
-  f[1] = f2_fma(dy, w, f2_fma(tmy, u, f2_fma(smy, v, f[1])));
-  f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_fma(smz, v, f[2])));
+  u = f2_fma(ds, ri5, u);
+  f[0] = f2_fma(dx, w, f2_fma(smx, v, f[0]));
+  f[1] = f2_fma(dy, w, f2_fma(smy, v, f[1]));
+  f[2] = f2_fma(dz, w, f2_fma(smz, v, f[2]));
 }
 
 // Packed two-source force tensor (6 unique entries xx, yy, zz, xy, xz, yz of
