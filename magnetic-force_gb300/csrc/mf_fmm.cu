@@ -596,6 +596,9 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   int fail_k = 0, fail_ns = 0;
   for (int t0 = 0; t0 < n && !failed; t0 += kP2PThreads) {
     const bool act = t0 + tid < n;
+    // A warp without a live target (the last warps of a small box) skips
+    // the pair sweeps; it still takes part in every barrier and wait.
+    const bool warp_live = __any_sync(0xffffffffu, act);
     const int32_t i = p.tperm[st0 + (act ? t0 + tid : 0)];
     typename Body::TData td;
     Body::load(a, i, td);
@@ -627,14 +630,16 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
         const int n_items = s_steps[k].y >> 1;
         const float4* __restrict__ sp = stage_pos(s);
         const float4* __restrict__ sm = stage_mom(s);
-        typename Body::Acc acc;
-        acc.zero();
+        if (warp_live) {
+          typename Body::Acc acc;
+          acc.zero();
 #pragma unroll 4
-        for (int j = 0; j < n_items; ++j) Body::pair(td, Body::load_item(sp, sm, j), sc.pc, acc);
-        float o[kOut];
-        Body::tile_out(acc, o);
+          for (int j = 0; j < n_items; ++j) Body::pair(td, Body::load_item(sp, sm, j), sc.pc, acc);
+          float o[kOut];
+          Body::tile_out(acc, o);
 #pragma unroll
-        for (int q = 0; q < kOut; ++q) comp_add(run[q], cmp[q], o[q]);
+          for (int q = 0; q < kOut; ++q) comp_add(run[q], cmp[q], o[q]);
+        }
         __syncthreads();  // stage s is free
         if (tid == 0 && k + kP2PStages < ns) {
           fence_proxy_async_smem();
