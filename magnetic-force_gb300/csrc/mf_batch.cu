@@ -205,7 +205,7 @@ class Batch {
       b.h = si.h;
       b.flag_index = int32_t(k);
       const int pf = si.n >= kPackedFieldMin ? 1 : 0;
-      const int pg = si.n >= kPackedForceMin ? 1 : 0;
+      const int pg = si.n >= kBatchPackedForceMin ? 1 : 0;
       const double c = si.V * si.chi / (1.0 + si.chi);
       SceneSpec r = b;  // r = c G b + Hext - b
       r.scale = c;
@@ -616,6 +616,13 @@ class Server {
 
   mf_status submit(const mf_scene_desc& d, int64_t* id) {
     if (d.n <= 0 || !d.pos) return fail(MF_ERR_INVALID_ARG, "scene without particles");
+    // The same checks as a batch layout or a solver handle makes, here so a
+    // bad request is refused alone instead of failing a rebuild or its thread.
+    if (!(d.h > 0.f) || !(d.volume > 0.f) || !std::isfinite(d.h) || !std::isfinite(d.volume))
+      return fail(MF_ERR_INVALID_ARG, "scene h and volume must be finite and > 0");
+    if (!std::isfinite(d.chi) || d.chi <= -1.f) return fail(MF_ERR_INVALID_ARG, "scene chi must be > -1");
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(d.H0[k])) return fail(MF_ERR_INVALID_ARG, "scene H0 must be finite");
     if (need_bytes(d.n) > cfg_.hbm_budget_bytes) return fail(MF_ERR_BUDGET, "scene exceeds the HBM budget");
     for (int64_t i = 0; i < 3 * d.n; ++i)
       if (!std::isfinite(d.pos[i])) return fail(MF_ERR_INVALID_ARG, "non-finite particle position");

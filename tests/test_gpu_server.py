@@ -120,3 +120,22 @@ def test_fmm_request_in_the_mix(mf):
         alone = run_alone(mf, sc, steps)
         assert rel(srv.result(ids[k], "magnetic_bodyforce"), alone["magnetic_bodyforce"]) < 1e-5
     srv.close()
+
+
+def test_submit_rejects_bad_scenes(mf):
+    # Bad parameters are refused at submission, before they can fail a batch
+    # rebuild or an FMM request's thread; the server keeps serving.
+    import dataclasses
+    import scenes
+    sc = scenes.jittered_lattice(1000, "sphere", radius=0.3, chi=1.0, seed=7)
+    srv = mf.Server(steps_per_request=2)
+    for bad in (dict(h=0.0), dict(h=float("nan")), dict(volume=-1.0), dict(chi=-1.0), dict(chi=float("inf")),
+                dict(H0=(0.0, float("nan"), 1.0))):
+        with pytest.raises(mf.MFError) as e:
+            srv.submit(dataclasses.replace(sc, **bad))
+        assert e.value.status == 1  # MF_ERR_INVALID_ARG
+    rid = srv.submit(sc)
+    while srv.poll(rid)[0] != 2:
+        srv.step()
+    assert srv.stats()["completed"] == 1
+    srv.close()
