@@ -358,7 +358,7 @@ class Batch {
     MF_TRY(cells_.rebin(pos4_.as<float4>(), st_));
     to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
     MF_CUDA_TRY(cudaGetLastError());
-    ctr_.kernel_launches += 6;
+    ctr_.kernel_launches += 8;
     return MF_OK;
   }
 

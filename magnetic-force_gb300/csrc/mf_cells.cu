@@ -105,29 +105,92 @@ __global__ void k_count(const float4* __restrict__ pos, const CellGrid* __restri
   }
 }
 
-// Exclusive scan of counts[0..n) into start[0..n], one CTA of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan(const int32_t* __restrict__ counts, int64_t n,
-                                               int32_t* __restrict__ start) {
-  __shared__ int32_t sh[1024];
-  const int t = threadIdx.x;
-  const int64_t chunk = (n + 1023) / 1024;
-  const int64_t b = t * chunk, e = min(n, b + chunk);
-  int32_t s = 0;
-  for (int64_t i = b; i < e; ++i) s += counts[i];
-  sh[t] = s;
+// Exclusive scan of counts[0..n) into start[0..n], in three launches:
+// per-tile sums, a scan of the tile sums, and each tile's scan plus its
+// offset.  Tiles are kScanTile consecutive counts; integer sums, so the
+// result does not depend on the split.
+constexpr int kScanThreads = 256, kScanPer = 16, kScanTile = kScanThreads * kScanPer;
+
+// Exclusive prefix of v over the block (blockDim.x == kScanThreads); *total
+// gets the block's sum.  Uses `ws` (kScanThreads / 32 ints of shared memory).
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t v, int32_t* ws, int32_t* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int kW = kScanThreads / 32;
+  int32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  __syncthreads();  // ws is free (an earlier call may still read it)
+  if (lane == 31) ws[w] = inc;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    const int32_t v = t >= o ? sh[t - o] : 0;
-    __syncthreads();
-    sh[t] += v;
-    __syncthreads();
+  if (w == 0) {
+    const int32_t x = lane < kW ? ws[lane] : 0;
+    int32_t xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
+    }
+    if (lane < kW) ws[lane] = xi - x;
+    if (lane == kW - 1) ws[kW] = xi;
   }
-  int32_t run = sh[t] - s;  // exclusive prefix of this chunk
-  for (int64_t i = b; i < e; ++i) {
-    start[i] = run;
-    run += counts[i];
+  __syncthreads();
+  *total = ws[kW];
+  return inc - v + ws[w];
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ counts, int64_t n,
+                                                             int32_t* __restrict__ tile_sum) {
+  __shared__ int32_t ws[kScanThreads / 32 + 1];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile;
+  int32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    const int64_t i = base + int64_t(k) * kScanThreads + threadIdx.x;
+    if (i < n) s += counts[i];
   }
-  if (t == 1023) start[n] = sh[1023];
+  int32_t total;
+  block_exclusive_scan(s, ws, &total);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// One block: tile sums -> exclusive tile offsets (in place); start[n] = total.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int32_t* __restrict__ tile_sum, int64_t n_tiles,
+                                                                 int32_t* __restrict__ start, int64_t n) {
+  __shared__ int32_t ws[kScanThreads / 32 + 1];
+  int32_t run = 0;
+  for (int64_t b0 = 0; b0 < n_tiles; b0 += kScanThreads) {
+    const int64_t b = b0 + threadIdx.x;
+    const int32_t v = b < n_tiles ? tile_sum[b] : 0;
+    int32_t total;
+    const int32_t ex = block_exclusive_scan(v, ws, &total);
+    if (b < n_tiles) tile_sum[b] = run + ex;
+    run += total;
+  }
+  if (threadIdx.x == 0) start[n] = run;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t* __restrict__ counts, int64_t n,
+                                                             const int32_t* __restrict__ tile_off,
+                                                             int32_t* __restrict__ start) {
+  __shared__ int32_t ws[kScanThreads / 32 + 1];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanPer;
+  int32_t c[kScanPer];
+  int32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    c[k] = base + k < n ? counts[base + k] : 0;
+    s += c[k];
+  }
+  int32_t total;
+  int32_t run = tile_off[blockIdx.x] + block_exclusive_scan(s, ws, &total);
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (base + k < n) start[base + k] = run;
+    run += c[k];
+  }
 }
 
 __global__ void k_scatter(const CellGrid* __restrict__ grids, int n_scenes, int64_t n_total,
@@ -543,6 +606,7 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
                               st));
   MF_TRY(cell_start_.reserve_slack(sizeof(int32_t) * size_t(cells + 1)));
   MF_TRY(cursor_.reserve_slack(sizeof(int32_t) * size_t(cells + 1)));
+  MF_TRY(scan_tiles_.reserve_slack(sizeof(int32_t) * size_t((cells + kScanTile - 1) / kScanTile + 1)));
   MF_TRY(perm_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(perm_tmp_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(cell_of_.reserve(sizeof(int32_t) * size_t(n_total_)));
@@ -558,7 +622,13 @@ mf_status CellList::rebin(const float4* pos4, cudaStream_t st) {
   MF_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * size_t(cells + 1), st));
   const CellGrid* dg = grids_.as<CellGrid>();
   k_count<<<grid_for(n_total_), 256, 0, st>>>(pos4, dg, ns, n_total_, counts, cell_of_.as<int32_t>());
-  k_scan<<<1, 1024, 0, st>>>(counts, cells, cell_start_.as<int32_t>());
+  {
+    const int64_t tiles = (cells + kScanTile - 1) / kScanTile;
+    int32_t* tsum = scan_tiles_.as<int32_t>();
+    if (tiles > 0) k_scan_tiles<<<unsigned(tiles), kScanThreads, 0, st>>>(counts, cells, tsum);
+    k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(tsum, tiles, cell_start_.as<int32_t>(), cells);
+    if (tiles > 0) k_scan_apply<<<unsigned(tiles), kScanThreads, 0, st>>>(counts, cells, tsum, cell_start_.as<int32_t>());
+  }
   MF_CUDA_TRY(cudaMemcpyAsync(cursor_.ptr, cell_start_.ptr, sizeof(int32_t) * size_t(cells), cudaMemcpyDeviceToDevice,
                               st));
   k_scatter<<<grid_for(n_total_), 256, 0, st>>>(dg, ns, n_total_, cell_of_.as<int32_t>(), cursor_.as<int32_t>(),

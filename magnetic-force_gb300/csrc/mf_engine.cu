@@ -817,7 +817,7 @@ class Engine final : public EngineBase {
     if constexpr (kF32) {
       if (cells_dirty_) {
         MF_TRY(cells_.build(pos4(), {CellSceneSpec{0, np_, h_}}, st_));
-        ctr_.kernel_launches += 7;
+        ctr_.kernel_launches += 9;
         cells_dirty_ = false;
       }
     }

@@ -313,6 +313,7 @@ class CellList {
 
  private:
   DevBuf grids_, bbox_, cell_start_, cursor_, perm_, perm_tmp_, cell_of_;
+  DevBuf scan_tiles_;  // tile sums / offsets of the cell-count scan
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
   bool skip_field_on_ = false, skip_force_on_ = false;  // a list is in use
   DevBuf spos_, smom_;              // positions and dipoles in cell order (per correction)
