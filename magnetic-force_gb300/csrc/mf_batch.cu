@@ -130,7 +130,11 @@ class Batch {
       max_n = std::max(max_n, x.n);
     }
     n_alloc_ = off;
-    if (!own_stream_) MF_CUDA_TRY(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+    if (!own_stream_) {
+      int lo = 0, hi = 0;  // numerically lower is the higher priority
+      MF_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      MF_CUDA_TRY(cudaStreamCreateWithPriority(&own_stream_, cudaStreamNonBlocking, priority_ ? hi : lo));
+    }
     st_ = own_stream_;
     if (!pinned_) MF_CUDA_TRY(cudaMallocHost(&pinned_, 64));
 
@@ -264,6 +268,9 @@ class Batch {
     st_ = s ? s : own_stream_;
     drop_graph();
   }
+  // Before init: create the batch's own stream at the device's highest
+  // priority (the served loop's shared batch, ahead of its FMM requests).
+  void set_high_priority() { priority_ = true; }
 
   // Takes over another batch's device buffers, stream and pinned word (a
   // serving rebatch, with `o` idle): init() then grows only what is too
@@ -560,6 +567,7 @@ class Batch {
   int sms_ = 1;
   int red_gx_ = 1;
   cudaStream_t st_ = nullptr, own_stream_ = nullptr;
+  bool priority_ = false;
   void* pinned_ = nullptr;
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
@@ -869,7 +877,11 @@ class Server {
       p.precision = MF_FP32;
       p.device = cfg.device;
       MF_TRY(mf_create(&p, &sv));
-      MF_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+      {
+        int lo = 0, hi = 0;  // the lowest priority: the shared batch goes first
+        MF_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        MF_CUDA_TRY(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, lo));
+      }
       MF_TRY(mf_set_stream(sv, stream));
       MF_TRY(mf_set_option(sv, MF_OPT_SOLVER, MF_SOLVER_CG));
       MF_TRY(mf_set_option(sv, MF_OPT_REL_TOL, cfg.rel_tol));
@@ -974,6 +986,7 @@ class Server {
       st.push_back(state_of(r));
     }
     std::unique_ptr<Batch> nb(new Batch());
+    nb->set_high_priority();
     if (batch_) {
       nb->adopt_buffers(*batch_);
       batch_.reset();
