@@ -504,7 +504,7 @@ __global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_
 constexpr int kP2PThreads = 128;
 constexpr int kP2PTile = 256;  // sources (slots) per stage
 constexpr int kP2PStages = 3;
-constexpr int kP2PMaxSteps = 1024;
+constexpr int kP2PMaxSteps = 128;  // tile steps per refill of the row walk (1 KB of shared memory)
 constexpr int kP2PSmem = kP2PStages * 2 * kP2PTile * int(sizeof(float4));
 
 struct P2PArgs {
