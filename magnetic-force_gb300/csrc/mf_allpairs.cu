@@ -325,6 +325,7 @@ struct Shaped {
         case 1: return Launcher<Real, B, 1>::needs(plan, pd, nc);
         case 2: return Launcher<Real, B, 2>::needs(plan, pd, nc);
         case 3: return Launcher<Real, B, 3>::needs(plan, pd, nc);
+        case 4: return Launcher<Real, B, 4>::needs(plan, pd, nc);
         default: break;
       }
     }
@@ -337,6 +338,7 @@ struct Shaped {
         case 1: return Launcher<Real, B, 1>::launch(plan, io, partials, counters, err, st);
         case 2: return Launcher<Real, B, 2>::launch(plan, io, partials, counters, err, st);
         case 3: return Launcher<Real, B, 3>::launch(plan, io, partials, counters, err, st);
+        case 4: return Launcher<Real, B, 4>::launch(plan, io, partials, counters, err, st);
         default: break;
       }
     }

@@ -148,8 +148,8 @@ struct KCfg<double, Body::Tensor> {
 struct Shape {
   int tpb, tpt, tile;
 };
-constexpr int kShapes = 4;
-constexpr Shape kShapeTable[kShapes] = {{256, 2, 256}, {128, 2, 256}, {256, 1, 256}, {128, 4, 128}};
+constexpr int kShapes = 5;
+constexpr Shape kShapeTable[kShapes] = {{256, 2, 256}, {128, 2, 256}, {256, 1, 256}, {128, 4, 128}, {128, 4, 256}};
 inline bool shaped(Body b) { return b != Body::Tensor; }
 
 // One scene of a launch before it is laid out in step space.  nt > 0, ns > 0.
