@@ -21,6 +21,12 @@ CG solve; per-stage device times come from the handle's event timing.
 positions, CG solve, force) of the same cylinder through the FMM, so a
 capture sees the tree and expansion passes as well as the products.
 
+    python magnetic-force_gb300/microbench.py --kernel batch --reps 2
+
+``batch`` runs the batched bench's 256 scenes (512..32,768 particles): cold
+solve, three graph-captured warm-up timesteps, then --reps timesteps without
+the graph (so a capture lists every launch) inside the profiler range.
+
     python magnetic-force_gb300/microbench.py --kernel engine_field --n 65536 --reps 5
 
 ``engine_field`` / ``engine_force`` run the all-pairs products of a Solver
@@ -49,7 +55,7 @@ FLOP = {"field": 32.0, "force": 53.0, "tensor": 53.0}
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force", "fmm_step",
+    ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force", "fmm_step", "batch",
                                                       "engine_field", "engine_force"])
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
@@ -66,6 +72,8 @@ def main():
         return fmm(args, np, torch, mfgb, scenes)
     if args.kernel.startswith("engine"):
         return engine(args, np, torch, mfgb, scenes)
+    if args.kernel == "batch":
+        return batch(args, torch, mfgb, scenes)
     sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
     rng = np.random.default_rng(2)
     m = (rng.normal(size=(sc.n, 3)) * sc.volume).astype(np.float32)
@@ -156,6 +164,21 @@ def fmm_step(args, s, sc, torch):
         times.append(e0.elapsed_time(e1))
     torch.cuda.profiler.stop()
     print(json.dumps({"kernel": args.kernel, "n": sc.n, "step_ms": times, "counters": s.counters()}), flush=True)
+
+
+def batch(args, torch, mfgb, scenes):
+    import time
+    b = mfgb.Batch(scenes.batched_scenes(256, seed=7))
+    b.solve(500, 1e-6)
+    b.advance(1e-4, 3, iters_per_step=4, rel_tol=1e-6, graph=True)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    b.advance(1e-4, args.reps, iters_per_step=4, rel_tol=1e-6, graph=False)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / max(args.reps, 1)
+    torch.cuda.profiler.stop()
+    print(json.dumps({"kernel": "batch", "scenes": 256, "ms_per_step": ms, "counters": b.counters()}), flush=True)
 
 
 def engine(args, np, torch, mfgb, scenes):
