@@ -276,6 +276,7 @@ class Engine final : public EngineBase {
       if (!std::isfinite(sp[i]) || !std::isfinite(sm[i])) return fail(MF_ERR_INVALID_ARG, "non-finite source");
     ext_h_ = hext;
     n_ext_ = ns;
+    ext_fmm_dirty_ = true;
     if (ns > 0) {
       MF_TRY(ext_pos4_.reserve(size_t(ns) * sizeof(R4)));
       MF_TRY(ext_mom4_.reserve(size_t(ns) * sizeof(R4)));
@@ -308,6 +309,9 @@ class Engine final : public EngineBase {
       MF_CUDA_TRY(cudaGetLastError());
       ++ctr_.kernel_launches;
       rext_zero_ = true;
+    } else if (use_fmm_ext()) {
+      MF_TRY(eval_hext_fmm());
+      rext_zero_ = false;
     } else {
       LaunchIO<Real> io;
       io.tpos = pos4();
@@ -472,17 +476,17 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_ORDER:
         if (v < 4 || v > 8 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..8");
         fmm_cfg_.order = int(v);
-        fmm_dirty_ = true;
+        fmm_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_FMM_THETA:
         if (!(v > 0.0 && v <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm theta must be in (0, 1]");
         fmm_cfg_.theta = v;
-        fmm_dirty_ = true;
+        fmm_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_FMM_LEAF:
         if (v < 1 || v > 4096) return fail(MF_ERR_INVALID_ARG, "fmm leaf size must be 1..4096");
         fmm_cfg_.leaf_min = int(v);
-        fmm_dirty_ = true;
+        fmm_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_AUTOTUNE:
         if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "autotune mode must be 0, 1 or 2");
@@ -537,6 +541,12 @@ class Engine final : public EngineBase {
   Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_, plan_apply_;
   // FMM state (FP32 handles): the octree of the current positions.
   Fmm fmm_;
+  // External dipoles through the FMM: their octree (particles as targets),
+  // their cell list and the near-field correction records.
+  Fmm ext_fmm_;
+  CellList ext_cells_;
+  DevBuf ext_corr_;
+  bool ext_fmm_dirty_ = true;
   FmmConfig fmm_cfg_;
   bool fmm_dirty_ = true;
   int fmm_mode_ = 0;
@@ -843,12 +853,61 @@ class Engine final : public EngineBase {
       ++ctr_.kernel_launches;
       cells_dirty_ = true;
       fmm_dirty_ = true;
+      ext_fmm_dirty_ = true;
     }
   }
 
   bool use_fmm() const {
     if constexpr (!kF32) return false;
     return fmm_mode_ == 1 || (fmm_mode_ == 0 && np_ > kFmmAutoMin);
+  }
+  // Many external dipoles go through the FMM as well (the reference's
+  // fmm_hext_evaluator, magnetic_force.cu:688-697): an octree over the
+  // external sources with the particles as separate targets, smoothing
+  // length ext_mag_h.  The naive path keeps its all-pairs kernels.
+  bool use_fmm_ext() const {
+    if constexpr (!kF32) return false;
+    return !naive_ && fmm_mode_ != 2 && n_ext_ > kFmmAutoMin;
+  }
+  mf_status eval_hext_fmm() {
+    if constexpr (kF32) {
+      const float4* sp = ext_pos4_.template as<float4>();
+      const float4* sm = ext_mom4_.template as<float4>();
+      if (ext_fmm_dirty_) {
+        MF_TRY(ext_cells_.build(sp, {CellSceneSpec{0, n_ext_, double(ext_h_)}}, st_));
+        MF_TRY(ensure_cells());
+        double bbox[6];
+        for (int k = 0; k < 3; ++k) {
+          bbox[k] = std::min(ext_cells_.bbox(0)[k], cells_.bbox(0)[k]);
+          bbox[3 + k] = std::max(ext_cells_.bbox(0)[3 + k], cells_.bbox(0)[3 + k]);
+        }
+        MF_TRY(ext_fmm_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, fmm_cfg_, st_));
+        ctr_.kernel_launches += 17;
+        ext_fmm_dirty_ = false;
+      }
+      MF_TRY(scr_.ensure(0, 0));
+      MF_TRY(ext_corr_.reserve(size_t(2 * np_ + 2) * sizeof(float4), false, true));
+      float4* corr = ext_corr_.template as<float4>();
+      // H_ext = H0 + the sources' field (plan_ext_field_ carries H0 and ext_mag_h)
+      MF_TRY(ext_cells_.field_correction_at(pos4(), np_, sp, sm, corr, st_));
+      AllPairsArgs<float> a{};
+      a.tpos = pos4();
+      a.corr4 = corr;
+      a.out4 = hext4();
+      for (int k = 0; k < 3; ++k) a.out[k] = pubr(MF_Q_HEXT, k);
+      a.err = scr_.err.template as<int32_t>();
+      MF_TRY(ext_fmm_.product(0, sp, sm, a, plan_ext_field_.host[0], st_, nullptr));
+      // its gradient tensor, the 9 SoA arrays of dHextd{x,y,z}
+      MF_TRY(ext_cells_.tensor_correction_at(pos4(), np_, sp, sm, corr, st_));
+      AllPairsArgs<float> t{};
+      t.tpos = pos4();
+      t.corr4 = corr;
+      for (int k = 0; k < 9; ++k) t.out[k] = rext(k);
+      t.err = scr_.err.template as<int32_t>();
+      MF_TRY(ext_fmm_.product(2, sp, sm, t, plan_ext_tensor_.host[0], st_, nullptr));
+      ctr_.kernel_launches += 2 * (ext_fmm_.launches_per_product() + 1);
+    }
+    return MF_OK;
   }
   mf_status ensure_fmm() {
     if constexpr (kF32) {

@@ -230,3 +230,33 @@ def test_fmm_matrix_hessian(mf, oracle, sphere40k):
     g3 = got.reshape(-1, 3, 3)
     assert np.allclose(g3, np.transpose(g3, (0, 2, 1)), rtol=0, atol=1e-6 * np.abs(g3).max())
     A.close()
+
+
+def test_many_external_dipoles_through_fmm(mf):
+    # More than 65,536 external dipoles: H_ext and its gradient tensor come
+    # from an octree over the external sources (the particles as separate
+    # targets, smoothing length ext_mag_h), and equal the all-pairs
+    # evaluation of the same handle to the FMM's truncation error.
+    import scenes
+    sc = scenes.jittered_lattice(8000, "sphere", radius=0.3, chi=1.5, seed=21)
+    rng = np.random.default_rng(22)
+    ne = 70000
+    src = rng.uniform(-0.7, 0.7, (ne, 3)).astype(np.float32)
+    mom = ((np.array([0.0, 0.2, 1.0]) + 0.3 * rng.standard_normal((ne, 3))) * sc.volume).astype(np.float32)
+    hext = 2.0 * sc.h
+    out = {}
+    for mode in (mf.FMM_ON, mf.FMM_OFF):
+        s = mf.Solver(sc.n, sc.h, hext, sc.volume, sc.chi, sc.H0, src, mom, sc.pos, precision="fp32")
+        s.set_option("solver", mf.SOLVER_CG)
+        s.set_option("fmm", mode)
+        s.set_option("fmm_order", 8)
+        s.solve(300)
+        out[mode] = (s.Hext, np.stack([s.dHextdx, s.dHextdy, s.dHextdz]), s.total_B_over_mu0)
+    h1, g1, b1 = out[mf.FMM_ON]
+    h2, g2, b2 = out[mf.FMM_OFF]
+    e = rel(h1 - np.asarray(sc.H0, np.float32), h2 - np.asarray(sc.H0, np.float32))
+    # the two paths differ (the all-pairs one is deterministic, so equality
+    # would mean the FMM did not run) by no more than the truncation error
+    assert 0.0 < e < 1e-5
+    assert rel(g1, g2) < 3e-4
+    assert rel(b1, b2) < 1e-5
