@@ -370,7 +370,7 @@ class Engine final : public EngineBase {
       for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
     io.naive_quirks = naive_ ? 1 : 0;
     if (plan_force_.body == Body::ForceF2) MF_TRY(prepare_packed(mom4(), true, io));
-    MF_TRY(run(plan_force_, io));
+    MF_TRY(run(plan_force_sym_.n_scenes ? plan_force_sym_ : plan_force_, io));
     ctr_.force_passes += 1;
     ctr_.force_pairs += plan_force_.pairs;
     if (!kF32) publish_f(MF_Q_FORCE);
@@ -539,6 +539,7 @@ class Engine final : public EngineBase {
   CellList cells_;
   bool cells_dirty_ = true;
   Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_, plan_apply_;
+  Plan<Real> plan_force_sym_;  // packed force once per unordered pair (FP32; n_scenes 0 when unused)
   // FMM state (FP32 handles): the octree of the current positions.
   Fmm fmm_;
   // External dipoles through the FMM: their octree (particles as targets),
@@ -672,6 +673,12 @@ class Engine final : public EngineBase {
     MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_, fshape));
     s = base;
     MF_TRY(build_plan<Real>(gb, {s}, plan_force_, gshape));
+    // The packed force once per unordered pair (the all-pairs FMM handles
+    // take their own path and never use it).
+    plan_force_sym_.n_scenes = 0;
+    plan_force_sym_.host.clear();
+    if constexpr (kF32)
+      if (gb == Body::ForceF2) MF_TRY(build_force_sym_plan({s}, plan_force_sym_));
     MF_TRY(build_plan<Real>(fb, {base}, plan_apply_, fshape));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
@@ -700,11 +707,15 @@ class Engine final : public EngineBase {
 
   mf_status run(const Plan<Real>& plan, const LaunchIO<Real>& io) {
     if (!timing_) {
-      MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+      MF_TRY(launch(plan, io));
     } else {
       // Grow the scratch before the first event so the bracket holds the kernel only.
       size_t pd = 0, nc = 0;
-      plan_scratch_needs(plan, &pd, &nc);
+      if (&plan == &plan_force_sym_) {
+        if constexpr (kF32) force_sym_needs(plan, &pd);
+      } else {
+        plan_scratch_needs(plan, &pd, &nc);
+      }
       MF_TRY(scr_.ensure(pd, nc));
       TimedLaunch t;
       // statistics per kernel kind: field (0), force (1), tensor (2)
@@ -715,12 +726,20 @@ class Engine final : public EngineBase {
       MF_CUDA_TRY(cudaEventCreate(&t.start));
       MF_CUDA_TRY(cudaEventCreate(&t.stop));
       MF_CUDA_TRY(cudaEventRecord(t.start, st_));
-      MF_TRY(run_plan<Real>(plan, io, scr_, st_));
+      MF_TRY(launch(plan, io));
       MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
       timed_.push_back(t);
     }
     ++ctr_.kernel_launches;
+    if (&plan == &plan_force_sym_) ++ctr_.kernel_launches;  // the per-particle finish
     return MF_OK;
+  }
+  // The force product once per unordered pair (plan_force_sym_), or a plan of
+  // the all-pairs kernel.
+  mf_status launch(const Plan<Real>& plan, const LaunchIO<Real>& io) {
+    if constexpr (kF32)
+      if (&plan == &plan_force_sym_) return run_force_sym(plan, io, scr_, st_);
+    return run_plan<Real>(plan, io, scr_, st_);
   }
 
  public:

@@ -215,6 +215,15 @@ struct LaunchIO {
   int32_t done_total = 0;
 };
 
+// The packed Kelvin-force product evaluated once per unordered pair
+// (mf_symforce.cu): a plan over scenes whose targets are their sources, and
+// its launch (the pair kernel plus the per-particle finish with the force
+// epilogue).  The scratch holds FP32 block sums, 3 x 512 floats per block
+// pair of 512-particle blocks.
+mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan);
+void force_sym_needs(const Plan<float>& plan, size_t* partial_doubles);
+mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scratch& scr, cudaStream_t st);
+
 // Scratch sizes a plan needs.
 template <class Real>
 void plan_scratch_needs(const Plan<Real>& plan, size_t* partial_doubles, size_t* n_counters);

@@ -1,0 +1,365 @@
+// mf_symforce.cu -- the packed Kelvin-force product evaluated once per
+// unordered pair of particles.
+//
+// The clamped far-form pair force is antisymmetric, f_ji = -f_ij: with d the
+// same separation, the source and target dipoles swap places in
+//   f_ij = P (d (s.m) + s (d.m) + m (d.s)) + Q (d.s)(d.m) d,
+// and d changes sign.  So one evaluation serves both particles.
+//
+// Work layout.  A scene's particles are cut into blocks of TB = TPB * TPT
+// (targets strided by TPB, as in the all-pairs kernel); a source tile is one
+// block.  The steps are the (I, J) block pairs with I <= J, row by row, split
+// evenly over persistent CTAs.
+//   * I < J: each thread holds TPT targets of block I in registers and sweeps
+//     tile J (bulk-copied to shared memory on an mbarrier pipeline, 2 sources
+//     per packed f32x2 instruction).  Each f_ij is added to the target's sum
+//     and to the tile's source sums; those are reduced over the warp by a
+//     fixed shuffle tree and over the warps in a fixed order.
+//   * I == J: the block against itself, every ordered pair, target side only.
+// Every step writes its FP32 block sums (scaled by K) into part[K][X] -- the
+// sums for block K from partner block X, SoA per block pair -- so each entry
+// is written exactly once.  k_force_sym_finish then adds, per particle, the
+// nb entries of its block's row in FP64 in a fixed order and applies the
+// force epilogue (correction, external gradient, scale).  Results do not
+// depend on scheduling.
+#include "mf_internal.h"
+
+namespace mfgb {
+namespace {
+
+constexpr int kSymTPB = 128, kSymTPT = 4, kSymStages = 3;
+constexpr int kSymTB = kSymTPB * kSymTPT;  // particles per block = sources per tile
+constexpr int kSymWarps = kSymTPB / 32;
+constexpr size_t kSymSmem = size_t(kSymStages) * 2 * kSymTB * sizeof(float4);
+
+// Step l of a scene with nb blocks -> (I, J), row I holding nb - I steps.
+__device__ __forceinline__ void sym_block_pair(int64_t l, int nb, int& I, int& J) {
+  // start(I) = I nb - I (I - 1) / 2; solve for the largest I with start(I) <= l.
+  const double b = 2.0 * nb + 1.0;
+  int i = int((b - sqrt(b * b - 8.0 * double(l))) * 0.5);
+  if (i < 0) i = 0;
+  if (i > nb - 1) i = nb - 1;
+  auto start = [&](int r) { return int64_t(r) * nb - int64_t(r) * (r - 1) / 2; };
+  while (i > 0 && start(i) > l) --i;
+  while (i < nb - 1 && start(i + 1) <= l) ++i;
+  I = i;
+  J = i + int(l - start(i));
+}
+
+// f_ij for two sources (packed) and one target: the clamped far form of the
+// Kelvin force, in units of K.
+__device__ __forceinline__ void force_pair2_full(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy,
+                                                 float2 tmz, const PairItems::Item& it, float near2, float2* f) {
+  const float2 dx = f2_sub(tx, it.x), dy = f2_sub(ty, it.y), dz = f2_sub(tz, it.z);
+  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+  const float2 ri = clamp_rsqrt2(r2, near2);
+  const float2 ri2 = f2_mul(ri, ri);
+  const float2 ri5 = f2_mul(f2_mul(ri2, ri2), ri);
+  const float2 ds = f2_fma(dz, it.mz, f2_fma(dy, it.my, f2_mul(dx, it.mx)));
+  const float2 dm = f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx)));
+  const float2 sm = f2_fma(it.mz, tmz, f2_fma(it.my, tmy, f2_mul(it.mx, tmx)));
+  const float2 u = f2_mul(ds, ri5);
+  const float2 v = f2_mul(dm, ri5);
+  const float2 e = f2_mul(f2_mul(ri2, ds), f2_dup(-5.f));
+  const float2 w = f2_fma(e, v, f2_mul(sm, ri5));
+  f[0] = f2_fma(dx, w, f2_fma(tmx, u, f2_mul(it.mx, v)));
+  f[1] = f2_fma(dy, w, f2_fma(tmy, u, f2_mul(it.my, v)));
+  f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_mul(it.mz, v)));
+}
+
+__global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float> a, float* __restrict__ part) {
+  constexpr int TPB = kSymTPB, TPT = kSymTPT, TB = kSymTB, STAGES = kSymStages, NI = TB / 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  // per warp: the source sums of each pair item, [component * 2 + source of the pair][item]
+  __shared__ float s_srcf[kSymWarps][6][NI];
+
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t T = a.total_steps, G = gridDim.x, b = blockIdx.x;
+  const int64_t k_begin = step_start(T, G, b), k_end = step_start(T, G, b + 1);
+  if (k_begin >= k_end) return;
+  auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + size_t(s) * 2 * TB; };
+  auto stage_mom = [&](int s) { return stage_pos(s) + TB; };
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) mbar_init(&full_bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // Producer (thread 0): stage source block J of step k into stage s.
+  auto issue = [&](int64_t k, int s) {
+    const int si = find_scene(a.scenes, a.n_scenes, k);
+    const SceneDesc<float>& sc = a.scenes[si];
+    int I, J;
+    sym_block_pair(k - sc.step_off, sc.n_tb, I, J);
+    const int64_t first = sc.s_off + int64_t(J) * TB;
+    const int64_t rem = sc.ns - int64_t(J) * TB;
+    const int cnt = int(rem < TB ? rem : TB);
+    const uint32_t bytes = PairItems::tile_bytes(cnt);
+    mbar_arrive_expect_tx(&full_bar[s], 2 * bytes);
+    bulk_g2s(stage_pos(s), a.spos + first, bytes, &full_bar[s]);
+    bulk_g2s(stage_mom(s), a.smom + first, bytes, &full_bar[s]);
+  };
+  if (tid == 0)
+    for (int s = 0; s < STAGES && k_begin + s < k_end; ++s) issue(k_begin + s, s);
+
+  float2 tx[TPT], ty[TPT], tz[TPT], tmx[TPT], tmy[TPT], tmz[TPT];
+  int cur_si = -1, cur_I = -1;
+  int64_t k_fail = -1;
+  for (int64_t k = k_begin; k < k_end; ++k) {
+    const int64_t u = k - k_begin;
+    const int s = int(u % STAGES);
+    const int si = find_scene(a.scenes, a.n_scenes, k);
+    const SceneDesc<float>& sc = a.scenes[si];
+    const int nb = sc.n_tb;
+    int I, J;
+    sym_block_pair(k - sc.step_off, nb, I, J);
+    if (si != cur_si || I != cur_I) {  // the targets of block I
+      // Slots past the scene's end hold a zero dipole: their forces vanish
+      // on both sides of every pair.
+#pragma unroll
+      for (int t = 0; t < TPT; ++t) {
+        const int64_t li = int64_t(I) * TB + t * TPB + tid;
+        const bool live = li < sc.nt;
+        const float4 p = a.tpos[sc.t_off + (live ? li : 0)];
+        const float4 m = live ? a.tmom[sc.t_off + li] : make_float4(0.f, 0.f, 0.f, 0.f);
+        tx[t] = f2_dup(p.x);
+        ty[t] = f2_dup(p.y);
+        tz[t] = f2_dup(p.z);
+        tmx[t] = f2_dup(m.x);
+        tmy[t] = f2_dup(m.y);
+        tmz[t] = f2_dup(m.z);
+      }
+      cur_si = si;
+      cur_I = I;
+    }
+    const bool ok = mbar_wait_bounded(&full_bar[s], uint32_t((u / STAGES) & 1));
+    if (__syncthreads_or(!ok)) {
+      k_fail = k;
+      break;
+    }
+    const bool sym = I != J;
+    const int64_t rem = sc.ns - int64_t(J) * TB;
+    const int cnt = int(rem < TB ? rem : TB);
+    const int n_items = PairItems::items(cnt);
+    const float4* __restrict__ sp = stage_pos(s);
+    const float4* __restrict__ smv = stage_mom(s);
+    const float near2 = sc.pc.near2_force;
+    float2 acc[TPT][3];
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
+#pragma unroll 2
+    for (int j = 0; j < n_items; ++j) {
+      const PairItems::Item it = PairItems::load_item(sp, smv, j);
+      float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+      for (int t = 0; t < TPT; ++t) {
+        float2 f[3];
+        force_pair2_full(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, f);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          acc[t][c] = f2_add(acc[t][c], f[c]);
+          src[c] = f2_add(src[c], f[c]);
+        }
+      }
+      if (sym) {  // warp-uniform
+        // Reduce-scatter of the 6 sums (3 components x 2 sources, padded to
+        // 8) over the warp: halve the values held per lane at each of the
+        // first three levels, then finish the last one over the remaining
+        // lanes.  Value k = 4 b2 + 2 b1 + b0 ends in the lanes whose bits
+        // 4, 3, 2 are b2, b1, b0.
+        float v[8] = {src[0].x, src[0].y, src[1].x, src[1].y, src[2].x, src[2].y, 0.f, 0.f};
+        const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+        float w4[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float send = h16 ? v[q] : v[q + 4];
+          const float keep = h16 ? v[q + 4] : v[q];
+          w4[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
+        float w2[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float send = h8 ? w4[q] : w4[q + 2];
+          const float keep = h8 ? w4[q + 2] : w4[q];
+          w2[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+        }
+        float w1;
+        {
+          const float send = h4 ? w2[0] : w2[1];
+          const float keep = h4 ? w2[1] : w2[0];
+          w1 = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+        }
+        w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
+        w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
+        const int kv = (h16 ? 4 : 0) + (h8 ? 2 : 0) + (h4 ? 1 : 0);
+        if ((lane & 3) == 0 && kv < 6) s_srcf[wid][kv][j] = w1;
+      }
+    }
+    const float kk = float(kForceK);
+    float* pr = part + (sc.tb_off + int64_t(I) * nb + J) * 3 * TB;  // sums for block I from block J
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+      const int r = t * TPB + tid;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pr[c * TB + r] = (acc[t][c].x + acc[t][c].y) * kk;
+    }
+    __syncthreads();  // s_srcf complete; every thread is done with stage s
+    if (sym) {
+      float* ps = part + (sc.tb_off + int64_t(J) * nb + I) * 3 * TB;  // sums for block J from block I
+      for (int r = tid; r < TB; r += TPB) {
+        const int j = r >> 1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float v = 0.f;
+#pragma unroll
+          for (int w = 0; w < kSymWarps; ++w) v += s_srcf[w][2 * c + (r & 1)][j];
+          ps[c * TB + r] = -v * kk;  // f_ji = -f_ij
+        }
+      }
+      __syncthreads();  // s_srcf is read before the next step overwrites it
+    }
+    if (tid == 0 && k + STAGES < k_end) {
+      fence_proxy_async_smem();
+      issue(k + STAGES, s);
+    }
+  }
+
+  if (k_fail >= 0) {
+    if (tid == 0) {
+      atomicExch(a.err, MF_DEVERR_STAGE_TIMEOUT);
+      // Copies in flight: steps k_fail .. min(k_end, k_fail + STAGES) - 1, one
+      // per stage.  Wait for each (bounded) before the CTA leaves.
+      const int64_t k_stop = (k_fail + STAGES < k_end) ? k_fail + STAGES : k_end;
+      bool drained = true;
+      for (int64_t kk = k_fail; kk < k_stop; ++kk) {
+        const int64_t uu = kk - k_begin;
+        if (!mbar_wait_bounded(&full_bar[uu % STAGES], uint32_t((uu / STAGES) & 1))) drained = false;
+      }
+      if (!drained) atomicExch(a.err, MF_DEVERR_DRAIN_TIMEOUT);
+    }
+    __syncthreads();
+  }
+}
+
+// Per particle: the nb partner-block sums of its block, FP64 in block order,
+// then the force epilogue.  g runs over [g0, g0 + n_span), the particle
+// indices from the first scene's start to the last one's end (scenes are in
+// increasing t_off order; indices between scenes are skipped).
+__global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __restrict__ part, int64_t g0,
+                                   int64_t n_span) {
+  for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < n_span;
+       g += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t gi = g0 + g;
+    int lo = 0, hi = a.n_scenes - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.scenes[mid].t_off <= gi) lo = mid;
+      else hi = mid - 1;
+    }
+    const SceneDesc<float>& sc = a.scenes[lo];
+    const int64_t i = gi - sc.t_off;
+    if (i >= sc.nt) continue;  // the padding slot after an odd scene
+    const int K = int(i / kSymTB), r = int(i % kSymTB);
+    const int nb = sc.n_tb;
+    const float* row = part + (sc.tb_off + int64_t(K) * nb) * 3 * kSymTB;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int X = 0; X < nb; ++X) {
+      const float* p = row + int64_t(X) * 3 * kSymTB;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[c] += double(__ldcg(p + c * kSymTB + r));
+    }
+    const float4 m = a.tmom[gi];
+    force_epilogue<float>(a, sc, gi, double(m.x), double(m.y), double(m.z), v);
+  }
+}
+
+}  // namespace
+
+mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan) {
+  plan.body = Body::ForceF2;
+  plan.shape = 0;
+  plan.host.clear();
+  int64_t step = 0, blocks = 0;
+  double pairs = 0;
+  for (const SceneSpec& s : specs) {
+    if (s.nt <= 0 || s.nt != s.ns || s.t_off != s.s_off)
+      return fail(MF_ERR_INVALID_ARG, "symmetric force plan: targets must be the sources");
+    if (s.t_off % 2) return fail(MF_ERR_INVALID_ARG, "symmetric force plan: scene must start at an even index");
+    SceneDesc<float> d;
+    memset(&d, 0, sizeof(d));
+    d.t_off = s.t_off;
+    d.nt = s.nt;
+    d.s_off = s.s_off;
+    d.ns = s.ns;
+    const int64_t nb = (s.nt + kSymTB - 1) / kSymTB;
+    d.n_tb = int32_t(nb);
+    d.n_tiles = int32_t(nb);
+    d.step_off = step;
+    d.tb_off = blocks;  // first block pair of this scene in the partial array
+    d.flag_index = s.flag_index >= 0 ? s.flag_index : int32_t(plan.host.size());
+    d.pc = make_pair_consts<float>(s.h);
+    d.scale = float(s.scale);
+    step += nb * (nb + 1) / 2;
+    blocks += nb * nb;
+    pairs += double(s.nt) * double(s.ns);
+    plan.host.push_back(d);
+  }
+  plan.total_steps = step;
+  plan.total_tb = blocks;
+  plan.n_scenes = int32_t(plan.host.size());
+  plan.pairs = pairs;
+  const size_t bytes = plan.host.size() * sizeof(SceneDesc<float>);
+  MF_TRY(plan.d_scenes.reserve_grow(bytes));
+  if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
+  return MF_OK;
+}
+
+void force_sym_needs(const Plan<float>& plan, size_t* partial_doubles) {
+  // FP32 block sums: 3 x TB per block pair, in doubles
+  *partial_doubles = (size_t(plan.total_tb) * 3 * kSymTB + 1) / 2;
+}
+
+mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scratch& scr, cudaStream_t st) {
+  if (plan.total_steps <= 0) return MF_OK;
+  size_t pd = 0;
+  force_sym_needs(plan, &pd);
+  MF_TRY(scr.ensure(pd, 0));
+  static int grid_cache[64] = {};
+  const int dev = current_device();
+  int& gmax = grid_cache[dev >= 0 && dev < 64 ? dev : 0];
+  if (!gmax) {
+    MF_CUDA_TRY(cudaFuncSetAttribute(k_force_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSymSmem)));
+    int per_sm = 0;
+    MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_sym, kSymTPB, kSymSmem));
+    gmax = std::max(per_sm, 1) * device_sms(dev);
+  }
+  AllPairsArgs<float> a;
+  memset(&a, 0, sizeof(a));
+  a.scenes = plan.d_scenes.as<SceneDesc<float>>();
+  a.n_scenes = plan.n_scenes;
+  a.total_steps = plan.total_steps;
+  a.tpos = io.tpos;
+  a.tmom = io.tmom;
+  a.spos = io.spos;
+  a.smom = io.smom;
+  for (int k = 0; k < 9; ++k) {
+    a.out[k] = io.out[k];
+    a.rext[k] = io.rext[k];
+  }
+  a.naive_quirks = io.naive_quirks;
+  a.corr4 = io.corr4;
+  a.err = scr.err.as<int32_t>();
+  float* part = reinterpret_cast<float*>(scr.partials.as<double>());
+  const int64_t g = std::min<int64_t>(plan.total_steps, gmax);
+  k_force_sym<<<unsigned(g), kSymTPB, kSymSmem, st>>>(a, part);
+  MF_CUDA_TRY(cudaGetLastError());
+  const int64_t g0 = plan.host.front().t_off;
+  const int64_t n_span = plan.host.back().t_off + plan.host.back().nt - g0;
+  const int64_t fb = std::min<int64_t>((n_span + 255) / 256, 8192);
+  k_force_sym_finish<<<unsigned(fb), 256, 0, st>>>(a, part, g0, n_span);
+  MF_CUDA_TRY(cudaGetLastError());
+  return MF_OK;
+}
+
+}  // namespace mfgb
