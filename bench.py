@@ -45,6 +45,18 @@ import numpy as np  # noqa: E402
 
 FLOP_FIELD_PAIR = 32.0  # minimal far-field form, FMA = 2, rsqrt = 1
 FLOP_FORCE_PAIR = 53.0
+# one evaluation of the far-form force serving both particles of an unordered
+# pair: 49 FLOP for f_ij, plus 3 adds into the target and 3 into the source
+FLOP_FORCE_UPAIR = 55.0
+
+
+def product_flop(name, st):
+    """Algorithmic FLOP of the timed launches of one product kind: the
+    ordered pairs at the per-pair count, or, where one evaluation served both
+    particles (evals < pairs), the unordered pairs at the per-evaluation count."""
+    if name == "force" and st.get("evals", st["pairs"]) < st["pairs"]:
+        return FLOP_FORCE_UPAIR * st["evals"], "k_force_sym"
+    return (FLOP_FIELD_PAIR if name == "field" else FLOP_FORCE_PAIR) * st["pairs"], f"allpairs_kernel<{name}>"
 METRIC = "pair interactions/s; p50/p99 step latency, served vs plain at 1e-5 rel err"
 UNIT = "pairs/s"
 
@@ -52,7 +64,7 @@ UNIT = "pairs/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--dt", type=float, default=1e-4)
@@ -118,7 +130,9 @@ def allreduce_sum(x: float, world: int) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    """nvidia-smi sampled every 50 ms while the timed region runs.  start()
+    returns once the sampler has written its first line; the lines written
+    before that point are dropped, so the record covers the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -128,6 +142,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.skip = 0
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -135,9 +150,17 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except FileNotFoundError:
             self.proc = None
+            return
+        t_end = time.time() + 5.0
+        while time.time() < t_end and self.proc.poll() is None:
+            with open(self.path) as f:
+                self.skip = sum(1 for _ in f)
+            if self.skip:
+                break
+            time.sleep(0.01)
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -153,6 +176,7 @@ class ClockSampler:
             if len(parts) >= 9:
                 rows.append(parts)
         os.unlink(self.path)
+        rows = rows[self.skip:] if len(rows) > self.skip else rows[-1:]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -257,25 +281,33 @@ def run_ours(args, rank, world, local):
     # dominant all-pairs kernel and its FP32 roofline
     peak = mfgb.probe_fp32_peak()
     kern = {}
-    for name, st, fpp in (("field", kf, FLOP_FIELD_PAIR), ("force", kg, FLOP_FORCE_PAIR)):
+    names = {}
+    for name, st in (("field", kf), ("force", kg)):
         if st["launches"]:
-            kern[name] = {"launches": st["launches"], "total_ms": round(st["total_ms"], 4),
+            flop, names[name] = product_flop(name, st)
+            kern[name] = {"kernel": names[name], "launches": st["launches"], "total_ms": round(st["total_ms"], 4),
                           "avg_ms": round(st["total_ms"] / st["launches"], 4),
                           "pairs_per_launch": st["pairs"] / st["launches"],
-                          "tflops": fpp * st["pairs"] / (st["total_ms"] * 1e-3) / 1e12,
+                          "evals_per_launch": st["evals"] / st["launches"],
+                          "flop_per_launch": flop / st["launches"],
+                          "tflops": flop / (st["total_ms"] * 1e-3) / 1e12,
                           "pairs_per_s": st["pairs"] / (st["total_ms"] * 1e-3)}
     dom = max(kern, key=lambda k: kern[k]["total_ms"])
     ach = kern[dom]["tflops"]
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(f"allpairs_{dom}_fp32_65536")
+        key = "force_sym_fp32_65536" if names[dom] == "k_force_sym" else f"allpairs_{dom}_fp32_65536"
+        traffic = json.load(open(tpath)).get(key) if n == 65536 else None
     roofline = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
-                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": f"allpairs_kernel<{dom}>",
+                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": names[dom],
                 "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
                 "kernels": kern,
-                "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores; "
-                        "DRAM traffic per launch: the 2 MB of pair-layout records, read about twice (L2 absorbs the rest)"}
+                "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores. "
+                        "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair, or 55 per "
+                        "unordered pair for the force evaluated once per pair (k_force_sym; its timed bracket "
+                        "includes the per-particle finish). DRAM traffic per launch: the 2 MB of pair-layout "
+                        "records, read a few times (L2 absorbs the rest)"}
 
     # accuracy on a sample: fixed-point residual and force, FP64 oracle
     errors = None

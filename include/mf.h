@@ -217,7 +217,11 @@ typedef enum mf_kernel_kind {
 typedef struct mf_kernel_stats {
   int64_t launches;
   double total_ms;
-  double pairs;
+  double pairs;  /* ordered target-source pairs the launches covered */
+  double evals;  /* pair evaluations the algorithm needs for them: equal to
+                    pairs, except for the force product of one scene, where
+                    one evaluation serves both particles of an unordered pair
+                    (n (n - 1) / 2 per scene) */
 } mf_kernel_stats;
 mf_status mf_get_kernel_stats(mf_solver* s, int32_t kind, mf_kernel_stats* out);
 

@@ -301,6 +301,7 @@ mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>&
   plan.total_tb = tbo;
   plan.n_scenes = int32_t(plan.host.size());
   plan.pairs = pairs;
+  plan.evals = pairs;
   const size_t bytes = plan.host.size() * sizeof(SceneDesc<Real>);
   MF_TRY(plan.d_scenes.reserve_grow(bytes));
   if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
@@ -391,10 +392,14 @@ mf_status run_plan(const Plan<Real>& plan, const LaunchIO<Real>& io, Scratch& sc
 // Autotuner
 // ---------------------------------------------------------------------------
 namespace {
+// shape kShapes: the force once per unordered pair (k_force_sym), a
+// candidate only where the caller offered it (its entries are keyed apart).
 struct TuneEntry {
   int shape = 0;
-  float ms[kShapes] = {};
+  int n = kShapes;  // candidates timed
+  float ms[kShapes + 1] = {};
 };
+constexpr int kSymKey = 16;  // added to the body in the cache key when the symmetric launch was offered
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, uint32_t>, TuneEntry> g_tune;
 
@@ -424,9 +429,9 @@ uint32_t tune_class(const std::vector<SceneSpec>& specs) {
   return (uint32_t(ilog2(pairs)) << 8) | uint32_t(std::min(ilog2(double(specs.size())), 255));
 }
 
-int tuned_shape(Body body, uint32_t cls) {
+int tuned_shape(Body body, uint32_t cls, bool sym_offered) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  auto it = g_tune.find(std::make_tuple(current_device(), int(body), cls));
+  auto it = g_tune.find(std::make_tuple(current_device(), int(body) + (sym_offered ? kSymKey : 0), cls));
   return it == g_tune.end() ? -1 : it->second.shape;
 }
 
@@ -439,26 +444,35 @@ Tune default_tune_mode() {
 }
 
 mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
-                     Scratch& scratch, cudaStream_t st, Tune mode) {
+                     Scratch& scratch, cudaStream_t st, Tune mode, bool* sym) {
+  // Without a measurement the symmetric launch is taken where offered.
+  const bool offer = sym && body == Body::ForceF2;
+  if (sym) *sym = offer;
   if (mode == Tune::Off || !shaped(body)) return build_plan<float>(body, specs, plan, 0);
   const uint32_t cls = tune_class(specs);
-  const int known = tuned_shape(body, cls);
-  if (known >= 0) return build_plan<float>(body, specs, plan, known);
+  const int known = tuned_shape(body, cls, offer);
+  if (known >= 0) {
+    if (offer) *sym = known == kShapes;
+    return build_plan<float>(body, specs, plan, known == kShapes ? 0 : known);
+  }
   if (mode == Tune::CachedOnly) return build_plan<float>(body, specs, plan, 0);
   TuneEntry te;
+  te.n = kShapes + (offer ? 1 : 0);
   float best = 1e30f;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   MF_CUDA_TRY(cudaEventCreate(&e0));
   MF_CUDA_TRY(cudaEventCreate(&e1));
   mf_status status = MF_OK;
-  for (int s = 0; s < kShapes && status == MF_OK; ++s) {
+  for (int s = 0; s < te.n && status == MF_OK; ++s) {
     Plan<float> p;
-    status = build_plan<float>(body, specs, p, s);
+    const bool is_sym = s == kShapes;
+    status = is_sym ? build_force_sym_plan(specs, p) : build_plan<float>(body, specs, p, s);
     if (status != MF_OK) break;
-    status = run_plan<float>(p, io, scratch, st);  // warm-up (grows the scratch outside the timing)
+    auto launch = [&] { return is_sym ? run_force_sym(p, io, scratch, st) : run_plan<float>(p, io, scratch, st); };
+    status = launch();  // warm-up (grows the scratch outside the timing)
     if (status != MF_OK) break;
     cudaEventRecord(e0, st);
-    for (int r = 0; r < 2 && status == MF_OK; ++r) status = run_plan<float>(p, io, scratch, st);
+    for (int r = 0; r < 2 && status == MF_OK; ++r) status = launch();
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) status = cuda_fail(cudaGetLastError(), "autotune timing");
     float ms = 0.f;
@@ -475,9 +489,10 @@ mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>
   MF_TRY(scratch.check(st));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[std::make_tuple(current_device(), int(body), cls)] = te;
+    g_tune[std::make_tuple(current_device(), int(body) + (offer ? kSymKey : 0), cls)] = te;
   }
-  return build_plan<float>(body, specs, plan, te.shape);
+  if (offer) *sym = te.shape == kShapes;
+  return build_plan<float>(body, specs, plan, te.shape == kShapes ? 0 : te.shape);
 }
 
 std::string autotune_report() {
@@ -486,11 +501,19 @@ std::string autotune_report() {
   char line[256];
   for (const auto& kv : g_tune) {
     const TuneEntry& e = kv.second;
-    snprintf(line, sizeof(line), "device %d %s pairs~2^%u scenes~2^%u: shape %d (%dx%d/%d) ms", std::get<0>(kv.first),
-             body_name(Body(std::get<1>(kv.first))), std::get<2>(kv.first) >> 8, std::get<2>(kv.first) & 255u,
-             e.shape, kShapeTable[e.shape].tpb, kShapeTable[e.shape].tpt, kShapeTable[e.shape].tile);
+    const int kb = std::get<1>(kv.first);
+    const char* extra = kb >= kSymKey ? "+sym" : "";
+    if (e.shape == kShapes)
+      snprintf(line, sizeof(line), "device %d %s%s pairs~2^%u scenes~2^%u: shape %d (once per unordered pair) ms",
+               std::get<0>(kv.first), body_name(Body(kb % kSymKey)), extra, std::get<2>(kv.first) >> 8,
+               std::get<2>(kv.first) & 255u, e.shape);
+    else
+      snprintf(line, sizeof(line), "device %d %s%s pairs~2^%u scenes~2^%u: shape %d (%dx%d/%d) ms",
+               std::get<0>(kv.first), body_name(Body(kb % kSymKey)), extra, std::get<2>(kv.first) >> 8,
+               std::get<2>(kv.first) & 255u, e.shape, kShapeTable[e.shape].tpb, kShapeTable[e.shape].tpt,
+               kShapeTable[e.shape].tile);
     out += line;
-    for (int s = 0; s < kShapes; ++s) {
+    for (int s = 0; s < e.n; ++s) {
       snprintf(line, sizeof(line), " %.4f", double(e.ms[s]));
       out += line;
     }

@@ -634,6 +634,9 @@ class Engine final : public EngineBase {
     // FP32: block shapes from the autotuner, timed on this scene's own
     // positions (the tuning launches write scratch vectors only).
     int fshape = 0, gshape = 0;
+    // The packed force once per unordered pair unless the tuner measured
+    // an all-pairs shape faster.
+    bool use_sym = gb == Body::ForceF2;
     if constexpr (kF32) {
       // A handle on the FMM path launches no all-pairs product: its plans
       // only carry the epilogue coefficients, so they are not timed.
@@ -654,7 +657,7 @@ class Engine final : public EngineBase {
         ig.smom = gb == Body::ForceF2 ? mom2_.template as<float4>() : mom4();
         ig.corr4 = gb == Body::ForceF2 ? corr_.template as<float4>() : nullptr;
         for (int k = 0; k < 3; ++k) ig.out[k] = pubr(MF_Q_FORCE, k);
-        MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_));
+        MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_, &use_sym));
         gshape = tp.shape;
       }
     }
@@ -673,12 +676,12 @@ class Engine final : public EngineBase {
     MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_, fshape));
     s = base;
     MF_TRY(build_plan<Real>(gb, {s}, plan_force_, gshape));
-    // The packed force once per unordered pair (the all-pairs FMM handles
-    // take their own path and never use it).
+    // The packed force once per unordered pair (the FMM handles take their
+    // own path and never use it).
     plan_force_sym_.n_scenes = 0;
     plan_force_sym_.host.clear();
     if constexpr (kF32)
-      if (gb == Body::ForceF2) MF_TRY(build_force_sym_plan({s}, plan_force_sym_));
+      if (use_sym) MF_TRY(build_force_sym_plan({s}, plan_force_sym_));
     MF_TRY(build_plan<Real>(fb, {base}, plan_apply_, fshape));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
@@ -723,6 +726,7 @@ class Engine final : public EngineBase {
                : (plan.body == Body::Force || plan.body == Body::ForceF2) ? 1
                                                                           : 2;
       t.pairs = plan.pairs;
+      t.evals = plan.evals;
       MF_CUDA_TRY(cudaEventCreate(&t.start));
       MF_CUDA_TRY(cudaEventCreate(&t.stop));
       MF_CUDA_TRY(cudaEventRecord(t.start, st_));
@@ -752,6 +756,7 @@ class Engine final : public EngineBase {
       agg_[t.body].launches += t.skipped ? 0 : 1;
       agg_[t.body].total_ms += ms;
       agg_[t.body].pairs += t.skipped ? 0.0 : t.pairs;
+      agg_[t.body].evals += t.skipped ? 0.0 : t.evals;
       cudaEventDestroy(t.start);
       cudaEventDestroy(t.stop);
     }
@@ -830,7 +835,7 @@ class Engine final : public EngineBase {
  private:
   struct TimedLaunch {
     int body = 0;
-    double pairs = 0;
+    double pairs = 0, evals = 0;
     bool skipped = false;
     cudaEvent_t start = nullptr, stop = nullptr;
   };
@@ -970,11 +975,11 @@ class Engine final : public EngineBase {
       cudaEvent_t marks[4] = {nullptr, nullptr, nullptr, nullptr};
       if (timing_) {
         t.body = force ? MF_K_FORCE : MF_K_FIELD;
-        t.pairs = plan.pairs;
+        t.pairs = t.evals = plan.pairs;
         tf.body = MF_K_FMM_FAR;
-        tf.pairs = fmm_.stats().m2l_per_product;
+        tf.pairs = tf.evals = fmm_.stats().m2l_per_product;
         tn.body = force ? MF_K_FMM_NEAR_FORCE : MF_K_FMM_NEAR_FIELD;
-        tn.pairs = fmm_.stats().p2p_pairs;
+        tn.pairs = tn.evals = fmm_.stats().p2p_pairs;
         for (TimedLaunch* x : {&t, &tf, &tn}) {
           MF_CUDA_TRY(cudaEventCreate(&x->start));
           MF_CUDA_TRY(cudaEventCreate(&x->stop));

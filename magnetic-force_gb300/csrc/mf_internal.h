@@ -172,6 +172,7 @@ struct Plan {
   int64_t total_tb = 0;
   int32_t n_scenes = 0;
   double pairs = 0.0;  // sum over scenes of nt * ns
+  double evals = 0.0;  // pair evaluations needed: pairs, or n (n - 1) / 2 per scene when one serves both particles
   DevBuf d_scenes;
   std::vector<SceneDesc<Real>> host;  // the table as uploaded
 };
@@ -244,8 +245,13 @@ mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double*
 // each, CUDA events on `st`; the fastest is cached.  Off, or a body without
 // shapes, builds shape 0; CachedOnly uses a cached choice and never times.
 enum class Tune { Off = 0, OnMiss = 1, CachedOnly = 2 };
+//
+// `sym` (packed force of one scene whose targets are its sources): the force
+// once per unordered pair is one more candidate, and *sym says whether it
+// won (true without a measurement); `plan` then holds the best all-pairs
+// shape all the same.
 mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
-                     Scratch& scratch, cudaStream_t st, Tune mode);
+                     Scratch& scratch, cudaStream_t st, Tune mode, bool* sym = nullptr);
 // Default tuning mode of new handles and batches: OnMiss unless the
 // environment sets MF_AUTOTUNE=0.
 Tune default_tune_mode();
@@ -259,7 +265,7 @@ int current_device();
 // Size class of a launch: log2 of its pairs and of its scene count.
 uint32_t tune_class(const std::vector<SceneSpec>& specs);
 // Shape for (device, body, class): the cached choice, or -1 when not tuned yet.
-int tuned_shape(Body body, uint32_t cls);
+int tuned_shape(Body body, uint32_t cls, bool sym_offered);
 // Text table of the tuned choices (device, body, class, ms per shape).
 std::string autotune_report();
 

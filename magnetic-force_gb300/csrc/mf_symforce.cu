@@ -27,10 +27,44 @@
 namespace mfgb {
 namespace {
 
-constexpr int kSymTPB = 128, kSymTPT = 4, kSymStages = 3;
+constexpr int kSymTPB = 128, kSymTPT = 4, kSymStages = 2;
 constexpr int kSymTB = kSymTPB * kSymTPT;  // particles per block = sources per tile
 constexpr int kSymWarps = kSymTPB / 32;
 constexpr size_t kSymSmem = size_t(kSymStages) * 2 * kSymTB * sizeof(float4);
+// A tile's source sums are reduced over the warps in kSymSplit phases (the
+// per-warp buffer holds one phase: less shared memory per CTA), and over the
+// lanes kSymPair items at a time (one shuffle tree for 6 * kSymPair values).
+constexpr int kSymSplit = 2, kSymPair = 4;
+constexpr int kSymPhaseItems = kSymTB / 2 / kSymSplit;
+static_assert(kSymPhaseItems % kSymPair == 0, "phase items");
+
+// Reduce-scatter of NV values per lane over the warp (NV a power of two,
+// 8 .. 32): the value index halves at each level, lanes with bit b set keep
+// the upper half; after log2(NV) levels each lane holds one value summed over
+// the lanes that differ in the bits used, and the remaining levels finish the
+// sum.  Value k ends in the lanes lane / (32 / NV) == k.  Fixed order: the
+// result does not depend on scheduling.
+template <int NV>
+__device__ __forceinline__ float warp_reduce_scatter(const float (&v)[NV], int lane) {
+  static_assert(NV >= 2 && NV <= 32 && (NV & (NV - 1)) == 0, "NV");
+  float w[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) w[q] = v[q];
+  int b = 16;
+#pragma unroll
+  for (int n = NV; n > 1; n >>= 1, b >>= 1) {
+    const bool hi = lane & b;
+#pragma unroll
+    for (int q = 0; q < n / 2; ++q) {
+      const float send = hi ? w[q] : w[q + n / 2];
+      const float keep = hi ? w[q + n / 2] : w[q];
+      w[q] = keep + __shfl_xor_sync(0xffffffffu, send, b);
+    }
+  }
+#pragma unroll
+  for (; b >= 1; b >>= 1) w[0] += __shfl_xor_sync(0xffffffffu, w[0], b);
+  return w[0];
+}
 
 // Step l of a scene with nb blocks -> (I, J), row I holding nb - I steps.
 __device__ __forceinline__ void sym_block_pair(int64_t l, int nb, int& I, int& J) {
@@ -68,11 +102,14 @@ __device__ __forceinline__ void force_pair2_full(float2 tx, float2 ty, float2 tz
 }
 
 __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float> a, float* __restrict__ part) {
-  constexpr int TPB = kSymTPB, TPT = kSymTPT, TB = kSymTB, STAGES = kSymStages, NI = TB / 2;
+  constexpr int TPB = kSymTPB, TPT = kSymTPT, TB = kSymTB, STAGES = kSymStages;
+  constexpr int NH = kSymPhaseItems, P = kSymPair, NV = P * 6 <= 8 ? 8 : (P * 6 <= 16 ? 16 : 32);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
-  // per warp: the source sums of each pair item, [component * 2 + source of the pair][item]
-  __shared__ float s_srcf[kSymWarps][6][NI];
+  // per warp: the source sums of the phase's pair items, [item][component * 2 + source of the pair]
+  // (row stride 6: the lanes' writes of one item, and 32 threads' reads of
+  // consecutive sources, fall in distinct banks)
+  __shared__ float s_srcf[kSymWarps][NH * 6];
 
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int64_t T = a.total_steps, G = gridDim.x, b = blockIdx.x;
@@ -145,58 +182,65 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
     const float4* __restrict__ sp = stage_pos(s);
     const float4* __restrict__ smv = stage_mom(s);
     const float near2 = sc.pc.near2_force;
+    const float kk = float(kForceK);
     float2 acc[TPT][3];
 #pragma unroll
     for (int t = 0; t < TPT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
+    for (int h = 0; h < kSymSplit; ++h) {
+      const int j_end = min(n_items, (h + 1) * NH);
 #pragma unroll 2
-    for (int j = 0; j < n_items; ++j) {
-      const PairItems::Item it = PairItems::load_item(sp, smv, j);
-      float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      for (int j0 = h * NH; j0 < j_end; j0 += P) {
+        float v[NV];
 #pragma unroll
-      for (int t = 0; t < TPT; ++t) {
-        float2 f[3];
-        force_pair2_full(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, f);
+        for (int q = 0; q < NV; ++q) v[q] = 0.f;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          acc[t][c] = f2_add(acc[t][c], f[c]);
-          src[c] = f2_add(src[c], f[c]);
+        for (int p = 0; p < P; ++p) {
+          // An item past the tile's end is a zero dipole at the origin: its
+          // force is exactly zero on both sides (finite distances, clamped).
+          const bool in = p == 0 || j0 + p < j_end;
+          const PairItems::Item it =
+              in ? PairItems::load_item(sp, smv, j0 + p) : PairItems::Item{{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f},
+                                                                          {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+          float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+          for (int t = 0; t < TPT; ++t) {
+            float2 f[3];
+            force_pair2_full(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, f);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              acc[t][c] = f2_add(acc[t][c], f[c]);
+              src[c] = f2_add(src[c], f[c]);
+            }
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            v[p * 6 + 2 * c] = src[c].x;
+            v[p * 6 + 2 * c + 1] = src[c].y;
+          }
+        }
+        if (sym) {  // warp-uniform
+          const float w = warp_reduce_scatter<NV>(v, lane);
+          const int kv = lane / (32 / NV);
+          if (lane % (32 / NV) == 0 && kv < 6 * P) s_srcf[wid][(j0 - h * NH) * 6 + kv] = w;
         }
       }
-      if (sym) {  // warp-uniform
-        // Reduce-scatter of the 6 sums (3 components x 2 sources, padded to
-        // 8) over the warp: halve the values held per lane at each of the
-        // first three levels, then finish the last one over the remaining
-        // lanes.  Value k = 4 b2 + 2 b1 + b0 ends in the lanes whose bits
-        // 4, 3, 2 are b2, b1, b0.
-        float v[8] = {src[0].x, src[0].y, src[1].x, src[1].y, src[2].x, src[2].y, 0.f, 0.f};
-        const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
-        float w4[4];
+      if (sym) {
+        __syncthreads();  // the phase's s_srcf is complete
+        // sums for block J from block I: sources 2 h NH .. 2 (h + 1) NH - 1
+        float* ps = part + (sc.tb_off + int64_t(J) * nb + I) * 3 * TB;
+        for (int r = tid; r < 2 * NH; r += TPB) {
+          const int j = r >> 1, rr = h * 2 * NH + r;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float send = h16 ? v[q] : v[q + 4];
-          const float keep = h16 ? v[q + 4] : v[q];
-          w4[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-        float w2[2];
+          for (int c = 0; c < 3; ++c) {
+            float x = 0.f;
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          const float send = h8 ? w4[q] : w4[q + 2];
-          const float keep = h8 ? w4[q + 2] : w4[q];
-          w2[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+            for (int w = 0; w < kSymWarps; ++w) x += s_srcf[w][j * 6 + 2 * c + (r & 1)];
+            ps[c * TB + rr] = -x * kk;  // f_ji = -f_ij
+          }
         }
-        float w1;
-        {
-          const float send = h4 ? w2[0] : w2[1];
-          const float keep = h4 ? w2[1] : w2[0];
-          w1 = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-        }
-        w1 += __shfl_xor_sync(0xffffffffu, w1, 2);
-        w1 += __shfl_xor_sync(0xffffffffu, w1, 1);
-        const int kv = (h16 ? 4 : 0) + (h8 ? 2 : 0) + (h4 ? 1 : 0);
-        if ((lane & 3) == 0 && kv < 6) s_srcf[wid][kv][j] = w1;
+        if (h + 1 < kSymSplit) __syncthreads();  // read before the next phase overwrites it
       }
     }
-    const float kk = float(kForceK);
     float* pr = part + (sc.tb_off + int64_t(I) * nb + J) * 3 * TB;  // sums for block I from block J
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
@@ -204,21 +248,7 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
 #pragma unroll
       for (int c = 0; c < 3; ++c) pr[c * TB + r] = (acc[t][c].x + acc[t][c].y) * kk;
     }
-    __syncthreads();  // s_srcf complete; every thread is done with stage s
-    if (sym) {
-      float* ps = part + (sc.tb_off + int64_t(J) * nb + I) * 3 * TB;  // sums for block J from block I
-      for (int r = tid; r < TB; r += TPB) {
-        const int j = r >> 1;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          float v = 0.f;
-#pragma unroll
-          for (int w = 0; w < kSymWarps; ++w) v += s_srcf[w][2 * c + (r & 1)][j];
-          ps[c * TB + r] = -v * kk;  // f_ji = -f_ij
-        }
-      }
-      __syncthreads();  // s_srcf is read before the next step overwrites it
-    }
+    __syncthreads();  // every thread is done with stage s and with s_srcf
     if (tid == 0 && k + STAGES < k_end) {
       fence_proxy_async_smem();
       issue(k + STAGES, s);
@@ -281,7 +311,7 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
   plan.shape = 0;
   plan.host.clear();
   int64_t step = 0, blocks = 0;
-  double pairs = 0;
+  double pairs = 0, evals = 0;
   for (const SceneSpec& s : specs) {
     if (s.nt <= 0 || s.nt != s.ns || s.t_off != s.s_off)
       return fail(MF_ERR_INVALID_ARG, "symmetric force plan: targets must be the sources");
@@ -303,12 +333,14 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
     step += nb * (nb + 1) / 2;
     blocks += nb * nb;
     pairs += double(s.nt) * double(s.ns);
+    evals += double(s.nt) * double(s.nt - 1) * 0.5;
     plan.host.push_back(d);
   }
   plan.total_steps = step;
   plan.total_tb = blocks;
   plan.n_scenes = int32_t(plan.host.size());
   plan.pairs = pairs;
+  plan.evals = evals;
   const size_t bytes = plan.host.size() * sizeof(SceneDesc<float>);
   MF_TRY(plan.d_scenes.reserve_grow(bytes));
   if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));

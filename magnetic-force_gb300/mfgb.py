@@ -67,7 +67,8 @@ class mf_counters(ctypes.Structure):
 
 
 class mf_kernel_stats(ctypes.Structure):
-    _fields_ = [("launches", ctypes.c_int64), ("total_ms", ctypes.c_double), ("pairs", ctypes.c_double)]
+    _fields_ = [("launches", ctypes.c_int64), ("total_ms", ctypes.c_double), ("pairs", ctypes.c_double),
+                ("evals", ctypes.c_double)]
 
 
 class mf_fmm_stats(ctypes.Structure):
@@ -292,7 +293,7 @@ class Solver:
     def kernel_stats(self, kind: str) -> dict:
         st = mf_kernel_stats()
         check(load().mf_get_kernel_stats(self._h, KERNEL[kind], ctypes.byref(st)))
-        return {"launches": st.launches, "total_ms": st.total_ms, "pairs": st.pairs}
+        return {"launches": st.launches, "total_ms": st.total_ms, "pairs": st.pairs, "evals": st.evals}
 
     def fmm_stats(self) -> dict:
         st = mf_fmm_stats()

@@ -205,8 +205,11 @@ def engine(args, np, torch, mfgb, scenes):
     r = max(st["launches"], 1)
     ms = st["total_ms"] / r
     pairs = float(sc.n) * sc.n
+    # the force evaluated once per unordered pair: 55 FLOP per evaluation
+    sym = st["evals"] < st["pairs"]
+    flop = 55.0 * st["evals"] / r if sym else FLOP[kind] * pairs
     print(json.dumps({"kernel": args.kernel, "n": sc.n, "kernel_ms": ms, "pairs_per_s": pairs / (ms * 1e-3),
-                      "tflops": FLOP[kind] * pairs / (ms * 1e-3) / 1e12,
+                      "symmetric": sym, "tflops": flop / (ms * 1e-3) / 1e12,
                       "autotune": mfgb.autotune_report()}), flush=True)
 
 

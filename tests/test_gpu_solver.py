@@ -234,3 +234,29 @@ def test_autotuned_shapes_match_default(mf):
     assert rel(out[1][1], out[0][1]) < 1e-6
     rep = mf.autotune_report()
     assert any("field_packed" in ln for ln in rep) and any("force_packed" in ln for ln in rep)
+
+
+@pytest.mark.parametrize("n", [14337, 32769])
+def test_force_once_per_pair_matches_oracle(mf, oracle, n):
+    # The packed force of one scene evaluated once per unordered pair
+    # (f_ji = -f_ij), taken without tuning: the kernel statistics show one
+    # evaluation per unordered pair.  n is one past a multiple of the
+    # 512-particle block, so the last block holds a single particle.
+    import scenes
+    sc = scenes.jittered_lattice(n, "sphere", radius=0.5, chi=2.0, seed=n)
+    s = make(mf, sc)
+    s.set_option("autotune", 0)
+    s.set_option("solver", mf.SOLVER_CG)
+    s.solve(200)
+    s.set_option("kernel_timing", 1)
+    s.reset_counters()
+    s.evaluate_fitted_near_foece()
+    st = s.kernel_stats("force")
+    assert st["launches"] == 1 and st["pairs"] == float(n) * n
+    assert st["evals"] == float(n) * (n - 1) / 2
+    M = np.asarray(s.M, np.float64)
+    F = oracle.force(np.asarray(sc.pos, np.float64), M, sc.h, None)
+    got = np.asarray(s.magnetic_bodyforce, np.float64)
+    assert rel(got, F) < 1e-5
+    # internal forces only (uniform applied field): they sum to zero
+    assert np.linalg.norm(got.sum(axis=0)) < 1e-5 * np.abs(got).sum()
