@@ -244,12 +244,25 @@ class Batch {
         MF_TRY(tuned_plan(fb, cgq[p], plan_cgq_[p], io, scr_, st_, tune_));
         MF_TRY(build_plan<float>(fb, resid[p], plan_resid_[p], plan_cgq_[p].shape));
       }
-      if (!force[p].empty()) MF_TRY(tuned_plan(gb, force[p], plan_force_[p], ig, scr_, st_, tune_));
+      // Packed force: once per unordered pair unless the tuner measured an
+      // all-pairs shape faster on these scenes.
+      bool sym = false;
+      if (!force[p].empty()) MF_TRY(tuned_plan(gb, force[p], plan_force_[p], ig, scr_, st_, tune_, p ? &sym : nullptr));
       for (const Plan<float>* pl : {&plan_resid_[p], &plan_cgq_[p], &plan_force_[p]}) {
         if (pl->n_scenes == 0) continue;
         size_t pd = 0, nc = 0;
         plan_scratch_needs(*pl, &pd, &nc);
         MF_TRY(scr_.ensure(pd, nc));
+      }
+      if (p) {
+        plan_force_sym_.n_scenes = 0;
+        plan_force_sym_.host.clear();
+        if (sym) {
+          MF_TRY(build_force_sym_plan(force[p], plan_force_sym_));
+          size_t pd = 0;
+          force_sym_needs(plan_force_sym_, &pd);
+          MF_TRY(scr_.ensure(pd, 0));
+        }
       }
     }
 
@@ -300,6 +313,9 @@ class Batch {
         pr.first->host.clear();
       }
     }
+    plan_force_sym_ = std::move(o.plan_force_sym_);
+    plan_force_sym_.n_scenes = 0;
+    plan_force_sym_.host.clear();
   }
   int scenes() const { return int(sc_.size()); }
 
@@ -349,8 +365,13 @@ class Batch {
       io.spos = pos2_.as<float4>();
       io.smom = mom2_.as<float4>();
       io.corr4 = corr_.as<float4>();
-      MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
-      ctr_.kernel_launches += 3;
+      if (plan_force_sym_.n_scenes) {
+        MF_TRY(run_force_sym(plan_force_sym_, io, scr_, st_));
+        ctr_.kernel_launches += 4;
+      } else {
+        MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
+        ctr_.kernel_launches += 3;
+      }
     }
     ctr_.force_passes += 1;
     ctr_.force_pairs += pairs_;
@@ -572,6 +593,7 @@ class Batch {
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
   Plan<float> plan_resid_[2], plan_cgq_[2], plan_force_[2];  // [0] exact branches, [1] packed
+  Plan<float> plan_force_sym_;  // the packed scenes' force once per unordered pair (n_scenes 0 when unused)
   Tune tune_ = Tune::OnMiss;
   Scratch scr_;
   CellList cells_;

@@ -22,6 +22,8 @@
 // nb entries of its block's row in FP64 in a fixed order and applies the
 // force epilogue (correction, external gradient, scale).  Results do not
 // depend on scheduling.
+#include <mutex>
+
 #include "mf_internal.h"
 
 namespace mfgb {
@@ -304,6 +306,25 @@ __global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __r
   }
 }
 
+// Resident CTAs of k_force_sym on the current device (its shared-memory
+// attribute set on the first call).  Plans call it when they are built, so
+// a launch inside a stream capture makes no attribute or occupancy calls.
+mf_status sym_grid_max(int* out) {
+  static std::mutex mu;
+  static int cache[64] = {};
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lk(mu);
+  int& g = cache[dev >= 0 && dev < 64 ? dev : 0];
+  if (!g) {
+    MF_CUDA_TRY(cudaFuncSetAttribute(k_force_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSymSmem)));
+    int per_sm = 0;
+    MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_sym, kSymTPB, kSymSmem));
+    g = std::max(per_sm, 1) * device_sms(dev);
+  }
+  *out = g;
+  return MF_OK;
+}
+
 }  // namespace
 
 mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan) {
@@ -336,6 +357,8 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
     evals += double(s.nt) * double(s.nt - 1) * 0.5;
     plan.host.push_back(d);
   }
+  int gmax = 0;
+  MF_TRY(sym_grid_max(&gmax));
   plan.total_steps = step;
   plan.total_tb = blocks;
   plan.n_scenes = int32_t(plan.host.size());
@@ -357,15 +380,8 @@ mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scra
   size_t pd = 0;
   force_sym_needs(plan, &pd);
   MF_TRY(scr.ensure(pd, 0));
-  static int grid_cache[64] = {};
-  const int dev = current_device();
-  int& gmax = grid_cache[dev >= 0 && dev < 64 ? dev : 0];
-  if (!gmax) {
-    MF_CUDA_TRY(cudaFuncSetAttribute(k_force_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSymSmem)));
-    int per_sm = 0;
-    MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_sym, kSymTPB, kSymSmem));
-    gmax = std::max(per_sm, 1) * device_sms(dev);
-  }
+  int gmax = 0;
+  MF_TRY(sym_grid_max(&gmax));
   AllPairsArgs<float> a;
   memset(&a, 0, sizeof(a));
   a.scenes = plan.d_scenes.as<SceneDesc<float>>();

@@ -84,3 +84,57 @@ def test_counters_count_executed_pairs(mf):
     c = b.counters()
     want = sum(sc.n ** 2 * (1 + i) for sc, i in zip(scs, it))
     assert c["field_pairs"] == pytest.approx(want)
+
+
+CHILD = r"""
+import sys
+import numpy as np
+sys.path[:0] = sys.argv[2:]
+import mfgb
+from test_gpu_batch import mixed_scenes
+mfgb.load()
+scs = mixed_scenes(seed=41, sizes=(4097, 6000, 9001))
+b = mfgb.Batch(scs)
+b.solve(300, 1e-7)
+b.reset_counters()
+b.eval_force()
+out = {"launches": b.counters()["kernel_launches"]}
+for k in range(len(scs)):
+    out["F%d" % k] = b.get(k, "magnetic_bodyforce")
+a, g = mfgb.Batch(scs), mfgb.Batch(scs)
+for x in (a, g):
+    x.solve(300, 1e-7)
+a.advance(1e-4, 3, iters_per_step=6, rel_tol=1e-7, graph=False)
+g.advance(1e-4, 3, iters_per_step=6, rel_tol=1e-7, graph=True)
+out["graph_equal"] = all(np.array_equal(a.get(k, q), g.get(k, q)) for k in range(len(scs))
+                         for q in ("positions", "velocity", "magnetic_bodyforce"))
+np.savez(sys.argv[1], **out)
+"""
+
+
+def test_packed_force_once_per_pair_in_batch(mf, tmp_path):
+    # Scenes of the packed force path, tuning off (a child process with
+    # MF_AUTOTUNE=0, read once per process): the batch evaluates their force
+    # once per unordered pair -- 4 launches: pair records, near-field
+    # correction, pair kernel, per-particle finish.  Each scene matches the
+    # same scene solved alone, and graph-captured steps match plain steps
+    # bit for bit.
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    pkg = os.path.join(os.path.dirname(here), "magnetic-force_gb300")
+    path = str(tmp_path / "batch.npz")
+    env = dict(os.environ, MF_AUTOTUNE="0")
+    subprocess.run([sys.executable, "-c", CHILD, path, here, pkg], env=env, check=True, timeout=600)
+    got = np.load(path)
+    assert int(got["launches"]) == 4
+    assert bool(got["graph_equal"])
+    for k, sc in enumerate(mixed_scenes(seed=41, sizes=(4097, 6000, 9001))):
+        s = mf.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
+        s.set_option("solver", mf.SOLVER_CG)
+        s.set_option("rel_tol", 1e-7)
+        s.solve(300)
+        s.evaluate_fitted_near_foece()
+        assert rel(got["F%d" % k], s.magnetic_bodyforce) < 1e-5
+        s.close()
