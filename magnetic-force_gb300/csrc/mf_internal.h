@@ -219,8 +219,8 @@ struct LaunchIO {
 // The packed Kelvin-force product evaluated once per unordered pair
 // (mf_symforce.cu): a plan over scenes whose targets are their sources, and
 // its launch (the pair kernel plus the per-particle finish with the force
-// epilogue).  The scratch holds FP32 block sums, 3 x 512 floats per block
-// pair of 512-particle blocks.
+// epilogue).  The scratch holds FP32 block sums: 3 floats per particle of a
+// block, per ordered block pair.
 mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan);
 void force_sym_needs(const Plan<float>& plan, size_t* partial_doubles);
 mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scratch& scr, cudaStream_t st);

@@ -19,9 +19,9 @@
 // Every step writes its FP32 block sums (scaled by K) into part[K][X] -- the
 // sums for block K from partner block X, SoA per block pair -- so each entry
 // is written exactly once.  k_force_sym_finish then adds, per particle, the
-// nb entries of its block's row in FP64 in a fixed order and applies the
-// force epilogue (correction, external gradient, scale).  Results do not
-// depend on scheduling.
+// nb entries of its block's row (compensated FP32, in a fixed order) and
+// applies the force epilogue (correction, external gradient, scale).
+// Results do not depend on scheduling.
 #include <mutex>
 
 #include "mf_internal.h"
@@ -29,14 +29,19 @@
 namespace mfgb {
 namespace {
 
-constexpr int kSymTPB = 128, kSymTPT = 4, kSymStages = 2;
+constexpr int kSymTPB = 128, kSymTPT = 8, kSymStages = 2;
 constexpr int kSymTB = kSymTPB * kSymTPT;  // particles per block = sources per tile
 constexpr int kSymWarps = kSymTPB / 32;
 constexpr size_t kSymSmem = size_t(kSymStages) * 2 * kSymTB * sizeof(float4);
 // A tile's source sums are reduced over the warps in kSymSplit phases (the
 // per-warp buffer holds one phase: less shared memory per CTA), and over the
 // lanes kSymPair items at a time (one shuffle tree for 6 * kSymPair values).
-constexpr int kSymSplit = 2, kSymPair = 4;
+// Measured at N = 65,536 / 131,072 (ms per product; TPB x TPT, stages,
+// split, pair): 128x4 3,1,1 3.41 / 13.02; 128x4 2,2,2 3.23 / 12.66;
+// 128x4 2,2,4 3.14 / 12.31; 128x8 2,2,1 3.01 / 12.00; 128x8 2,4,2 2.94 /
+// 11.68; 64x8 2,2,2 2.95 / 11.56; 128x8 2,2,2 2.88 / 11.47 (254 registers,
+// 2 CTAs per SM).
+constexpr int kSymSplit = 2, kSymPair = 2;
 constexpr int kSymPhaseItems = kSymTB / 2 / kSymSplit;
 static_assert(kSymPhaseItems % kSymPair == 0, "phase items");
 
@@ -274,8 +279,21 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
   }
 }
 
-// Per particle: the nb partner-block sums of its block, FP64 in block order,
-// then the force epilogue.  g runs over [g0, g0 + n_span), the particle
+// s + x with the rounding error of the add carried in e: Knuth's TwoSum
+// (The Art of Computer Programming, vol. 2, 4.2.2), exact in round-to-
+// nearest without any ordering of |s| and |x|.
+__device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
+  const float t = __fadd_rn(s, x);
+  const float xp = __fsub_rn(t, s);
+  const float sp = __fsub_rn(t, xp);
+  e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, sp), __fsub_rn(x, xp)));
+  s = t;
+}
+
+// Per particle: the nb partner-block sums of its block, compensated FP32
+// (sum and carried rounding error) in four chains over the blocks X = q
+// (mod 4) -- a fixed order, with four independent chains in flight -- the
+// chains combined in FP64 as (c0 + c1) + (c2 + c3); then the force epilogue.  g runs over [g0, g0 + n_span), the particle
 // indices from the first scene's start to the last one's end (scenes are in
 // increasing t_off order; indices between scenes are skipped).
 __global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __restrict__ part, int64_t g0,
@@ -295,11 +313,31 @@ __global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __r
     const int K = int(i / kSymTB), r = int(i % kSymTB);
     const int nb = sc.n_tb;
     const float* row = part + (sc.tb_off + int64_t(K) * nb) * 3 * kSymTB;
-    double v[3] = {0.0, 0.0, 0.0};
-    for (int X = 0; X < nb; ++X) {
-      const float* p = row + int64_t(X) * 3 * kSymTB;
+    float s4[4][3] = {}, e4[4][3] = {};
+    int X = 0;
+    for (; X + 4 <= nb; X += 4) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) v[c] += double(__ldcg(p + c * kSymTB + r));
+      for (int q = 0; q < 4; ++q) {
+        const float* p = row + int64_t(X + q) * 3 * kSymTB;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) two_sum_acc(s4[q][c], e4[q][c], __ldcg(p + c * kSymTB + r));
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (X + q < nb) {
+        const float* p = row + int64_t(X + q) * 3 * kSymTB;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) two_sum_acc(s4[q][c], e4[q][c], __ldcg(p + c * kSymTB + r));
+      }
+    }
+    double v[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) w[q] = double(s4[q][c]) + double(e4[q][c]);
+      v[c] = (w[0] + w[1]) + (w[2] + w[3]);
     }
     const float4 m = a.tmom[gi];
     force_epilogue<float>(a, sc, gi, double(m.x), double(m.y), double(m.z), v);

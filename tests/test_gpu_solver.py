@@ -241,7 +241,8 @@ def test_force_once_per_pair_matches_oracle(mf, oracle, n):
     # The packed force of one scene evaluated once per unordered pair
     # (f_ji = -f_ij), taken without tuning: the kernel statistics show one
     # evaluation per unordered pair.  n is one past a multiple of the
-    # 512-particle block, so the last block holds a single particle.
+    # kernel's block (1,024 particles), so the last block holds a single
+    # particle.
     import scenes
     sc = scenes.jittered_lattice(n, "sphere", radius=0.5, chi=2.0, seed=n)
     s = make(mf, sc)
