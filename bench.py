@@ -45,17 +45,20 @@ import numpy as np  # noqa: E402
 
 FLOP_FIELD_PAIR = 32.0  # minimal far-field form, FMA = 2, rsqrt = 1
 FLOP_FORCE_PAIR = 53.0
-# one evaluation of the far-form force serving both particles of an unordered
-# pair: 49 FLOP for f_ij, plus 3 adds into the target and 3 into the source
+# one evaluation serving both particles of an unordered pair:
+#   force: 49 FLOP for f_ij, plus 3 adds into the target and 3 into the source
+#   field: 13 for d, r^2, rsqrt, r^-3, -3 r^-5; 10 for d.m_s and d.m_t; 2 for
+#          their products with -3 r^-5; 2 x 3 x 2 FMA into each side's sum
 FLOP_FORCE_UPAIR = 55.0
+FLOP_FIELD_UPAIR = 49.0
 
 
 def product_flop(name, st):
     """Algorithmic FLOP of the timed launches of one product kind: the
     ordered pairs at the per-pair count, or, where one evaluation served both
     particles (evals < pairs), the unordered pairs at the per-evaluation count."""
-    if name == "force" and st.get("evals", st["pairs"]) < st["pairs"]:
-        return FLOP_FORCE_UPAIR * st["evals"], "k_force_sym"
+    if st.get("evals", st["pairs"]) < st["pairs"]:
+        return (FLOP_FORCE_UPAIR if name == "force" else FLOP_FIELD_UPAIR) * st["evals"], f"k_sym<{name}>"
     return (FLOP_FIELD_PAIR if name == "field" else FLOP_FORCE_PAIR) * st["pairs"], f"allpairs_kernel<{name}>"
 METRIC = "pair interactions/s; p50/p99 step latency, served vs plain at 1e-5 rel err"
 UNIT = "pairs/s"
@@ -297,17 +300,17 @@ def run_ours(args, rank, world, local):
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        key = "force_sym_fp32_65536" if names[dom] == "k_force_sym" else f"allpairs_{dom}_fp32_65536"
+        key = f"sym_{dom}_fp32_65536" if names[dom].startswith("k_sym") else f"allpairs_{dom}_fp32_65536"
         traffic = json.load(open(tpath)).get(key) if n == 65536 else None
     roofline = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "kernel": names[dom],
                 "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
                 "kernels": kern,
                 "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores. "
-                        "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair, or 55 per "
-                        "unordered pair for the force evaluated once per pair (k_force_sym; its timed bracket "
-                        "includes the per-particle finish). DRAM traffic per launch: the 2 MB of pair-layout "
-                        "records, read a few times (L2 absorbs the rest)"}
+                        "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair; for a product "
+                        "evaluated once per unordered pair (k_sym; its timed bracket includes the per-particle "
+                        "finish) 49 (field) or 55 (force) per unordered pair. DRAM traffic per launch: the 2 MB "
+                        "of pair-layout records, read a few times (L2 absorbs the rest)"}
 
     # accuracy on a sample: fixed-point residual and force, FP64 oracle
     errors = None

@@ -100,11 +100,17 @@ typedef enum mf_option {
   MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture, default 0.5 (FMMOptions.hpp:118) */
   MF_OPT_FMM_LEAF = 12,     /* FMM leaf level: the deepest whose boxes hold at least this many
                                particles on average (default 64) */
-  MF_OPT_AUTOTUNE = 13      /* block shapes of the FP32 all-pairs launches: 0 fixed default,
+  MF_OPT_AUTOTUNE = 13,     /* block shapes of the FP32 all-pairs launches: 0 fixed default,
                                1 tuned (default; each new body and size class is timed once
                                per process on the scene's own data), 2 tuned choices only when
                                already cached.  MF_AUTOTUNE=0 in the environment makes 0 the
                                default for handles and batches. */
+  MF_OPT_PAIR_SYMMETRIC = 14 /* FP32 packed field and force products of the handle's scene,
+                               each unordered pair evaluated once for both particles (a pair
+                               kernel and a per-particle finish) instead of every ordered
+                               pair: 0 never, 1 where tuning measured it faster (default;
+                               without tuning, the force only), 2 always.  Not in the
+                               reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */

@@ -257,7 +257,7 @@ static void cfg_of(Body b, int* tile, int* tbt, int shape) {
 }
 
 template <class Real>
-static void fill_coefs(const SceneSpec& s, SceneDesc<Real>& d) {
+void fill_scene_coefs(const SceneSpec& s, SceneDesc<Real>& d) {
   d.pc = make_pair_consts<Real>(s.h);
   d.scale = Real(s.scale);
   d.coef_add = Real(s.coef_add);
@@ -267,6 +267,8 @@ static void fill_coefs(const SceneSpec& s, SceneDesc<Real>& d) {
 
 template <class Real>
 mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>& plan, int shape) {
+  if constexpr (std::is_same<Real, float>::value)
+    if (shape == kShapeSym) return build_sym_plan(body, specs, plan);
   if (shape < 0 || shape >= kShapes || (shape != 0 && !(std::is_same<Real, float>::value && shaped(body))))
     return fail(MF_ERR_INVALID_ARG, "build_plan: bad block shape");
   int tile = 0, tbt = 0;
@@ -291,7 +293,7 @@ mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>&
     d.step_off = step;
     d.tb_off = tbo;
     d.flag_index = s.flag_index >= 0 ? s.flag_index : int32_t(plan.host.size());
-    fill_coefs(s, d);
+    fill_scene_coefs(s, d);
     step += int64_t(d.n_tiles) * d.n_tb;
     tbo += d.n_tb;
     pairs += double(s.nt) * double(s.ns);
@@ -311,7 +313,7 @@ mf_status build_plan(Body body, const std::vector<SceneSpec>& specs, Plan<Real>&
 template <class Real>
 mf_status refresh_plan_coefs(const std::vector<SceneSpec>& specs, Plan<Real>& plan) {
   if (specs.size() != plan.host.size()) return fail(MF_ERR_INVALID_ARG, "refresh_plan_coefs: size");
-  for (size_t i = 0; i < specs.size(); ++i) fill_coefs(specs[i], plan.host[i]);
+  for (size_t i = 0; i < specs.size(); ++i) fill_scene_coefs(specs[i], plan.host[i]);
   const size_t bytes = plan.host.size() * sizeof(SceneDesc<Real>);
   if (bytes) MF_CUDA_TRY(cudaMemcpy(plan.d_scenes.ptr, plan.host.data(), bytes, cudaMemcpyHostToDevice));
   return MF_OK;
@@ -349,6 +351,12 @@ struct Shaped {
 
 template <class Real>
 void plan_scratch_needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
+  if constexpr (std::is_same<Real, float>::value)
+    if (plan.shape == kShapeSym) {
+      sym_needs(plan, pd);
+      *nc = 0;
+      return;
+    }
   switch (plan.body) {
     case Body::Field: Shaped<Real, Body::Field>::needs(plan, pd, nc); break;
     case Body::Force: Shaped<Real, Body::Force>::needs(plan, pd, nc); break;
@@ -365,6 +373,8 @@ void plan_scratch_needs(const Plan<Real>& plan, size_t* pd, size_t* nc) {
 template <class Real>
 mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double* partials, int32_t* counters,
                        int32_t* err, cudaStream_t st) {
+  if constexpr (std::is_same<Real, float>::value)
+    if (plan.shape == kShapeSym) return run_sym(plan, io, partials, err, st);
   switch (plan.body) {
     case Body::Field: return Shaped<Real, Body::Field>::launch(plan, io, partials, counters, err, st);
     case Body::Force: return Shaped<Real, Body::Force>::launch(plan, io, partials, counters, err, st);
@@ -392,8 +402,8 @@ mf_status run_plan(const Plan<Real>& plan, const LaunchIO<Real>& io, Scratch& sc
 // Autotuner
 // ---------------------------------------------------------------------------
 namespace {
-// shape kShapes: the force once per unordered pair (k_force_sym), a
-// candidate only where the caller offered it (its entries are keyed apart).
+// shape kShapeSym: the launch once per unordered pair, a candidate only
+// where the caller offered it (its entries are keyed apart).
 struct TuneEntry {
   int shape = 0;
   int n = kShapes;  // candidates timed
@@ -435,6 +445,14 @@ int tuned_shape(Body body, uint32_t cls, bool sym_offered) {
   return it == g_tune.end() ? -1 : it->second.shape;
 }
 
+int default_sym_mode() {
+  static const int mode = [] {
+    const char* e = getenv("MF_PAIR_SYMMETRIC");
+    return (e && (e[0] == '0' || e[0] == '2') && e[1] == 0) ? e[0] - '0' : 1;
+  }();
+  return mode;
+}
+
 Tune default_tune_mode() {
   static const Tune mode = [] {
     const char* e = getenv("MF_AUTOTUNE");
@@ -443,19 +461,18 @@ Tune default_tune_mode() {
   return mode;
 }
 
+int default_shape(Body body, const std::vector<SceneSpec>& specs, bool allow_sym) {
+  return allow_sym && body == Body::ForceF2 && sym_eligible(body, specs) ? kShapeSym : 0;
+}
+
 mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
-                     Scratch& scratch, cudaStream_t st, Tune mode, bool* sym) {
-  // Without a measurement the symmetric launch is taken where offered.
-  const bool offer = sym && body == Body::ForceF2;
-  if (sym) *sym = offer;
-  if (mode == Tune::Off || !shaped(body)) return build_plan<float>(body, specs, plan, 0);
+                     Scratch& scratch, cudaStream_t st, Tune mode, bool allow_sym) {
+  const bool offer = allow_sym && sym_eligible(body, specs);
+  if (mode == Tune::Off || !shaped(body)) return build_plan<float>(body, specs, plan, default_shape(body, specs, offer));
   const uint32_t cls = tune_class(specs);
   const int known = tuned_shape(body, cls, offer);
-  if (known >= 0) {
-    if (offer) *sym = known == kShapes;
-    return build_plan<float>(body, specs, plan, known == kShapes ? 0 : known);
-  }
-  if (mode == Tune::CachedOnly) return build_plan<float>(body, specs, plan, 0);
+  if (known >= 0) return build_plan<float>(body, specs, plan, known);
+  if (mode == Tune::CachedOnly) return build_plan<float>(body, specs, plan, default_shape(body, specs, offer));
   TuneEntry te;
   te.n = kShapes + (offer ? 1 : 0);
   float best = 1e30f;
@@ -465,14 +482,12 @@ mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>
   mf_status status = MF_OK;
   for (int s = 0; s < te.n && status == MF_OK; ++s) {
     Plan<float> p;
-    const bool is_sym = s == kShapes;
-    status = is_sym ? build_force_sym_plan(specs, p) : build_plan<float>(body, specs, p, s);
+    status = build_plan<float>(body, specs, p, s);
     if (status != MF_OK) break;
-    auto launch = [&] { return is_sym ? run_force_sym(p, io, scratch, st) : run_plan<float>(p, io, scratch, st); };
-    status = launch();  // warm-up (grows the scratch outside the timing)
+    status = run_plan<float>(p, io, scratch, st);  // warm-up (grows the scratch outside the timing)
     if (status != MF_OK) break;
     cudaEventRecord(e0, st);
-    for (int r = 0; r < 2 && status == MF_OK; ++r) status = launch();
+    for (int r = 0; r < 2 && status == MF_OK; ++r) status = run_plan<float>(p, io, scratch, st);
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) status = cuda_fail(cudaGetLastError(), "autotune timing");
     float ms = 0.f;
@@ -491,8 +506,7 @@ mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[std::make_tuple(current_device(), int(body) + (offer ? kSymKey : 0), cls)] = te;
   }
-  if (offer) *sym = te.shape == kShapes;
-  return build_plan<float>(body, specs, plan, te.shape == kShapes ? 0 : te.shape);
+  return build_plan<float>(body, specs, plan, te.shape);
 }
 
 std::string autotune_report() {
@@ -503,7 +517,7 @@ std::string autotune_report() {
     const TuneEntry& e = kv.second;
     const int kb = std::get<1>(kv.first);
     const char* extra = kb >= kSymKey ? "+sym" : "";
-    if (e.shape == kShapes)
+    if (e.shape == kShapeSym)
       snprintf(line, sizeof(line), "device %d %s%s pairs~2^%u scenes~2^%u: shape %d (once per unordered pair) ms",
                std::get<0>(kv.first), body_name(Body(kb % kSymKey)), extra, std::get<2>(kv.first) >> 8,
                std::get<2>(kv.first) & 255u, e.shape);
@@ -524,6 +538,7 @@ std::string autotune_report() {
 
 #define MF_INSTANTIATE(R)                                                                                  \
   template mf_status build_plan<R>(Body, const std::vector<SceneSpec>&, Plan<R>&, int);                   \
+  template void fill_scene_coefs<R>(const SceneSpec&, SceneDesc<R>&);                                     \
   template mf_status refresh_plan_coefs<R>(const std::vector<SceneSpec>&, Plan<R>&);                      \
   template void plan_scratch_needs<R>(const Plan<R>&, size_t*, size_t*);                                  \
   template mf_status run_plan<R>(const Plan<R>&, const LaunchIO<R>&, Scratch&, cudaStream_t);             \

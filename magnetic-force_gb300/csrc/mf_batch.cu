@@ -240,29 +240,24 @@ class Batch {
       ig.out4 = nullptr;
       ig.tmom = mom4_.as<float4>();
       for (int k = 0; k < 3; ++k) ig.out[k] = fs_.as<float>() + int64_t(k) * n_alloc_;
+      // The packed products may run once per unordered pair (kShapeSym):
+      // the tuner's candidate, and without tuning the force's default.
+      // (MF_PAIR_SYMMETRIC=0 never, 2 always).
+      auto pick = [&](Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan,
+                      const LaunchIO<float>& lio) -> mf_status {
+        if (sym_mode_ == 2 && sym_eligible(body, specs)) return build_plan<float>(body, specs, plan, kShapeSym);
+        return tuned_plan(body, specs, plan, lio, scr_, st_, tune_, sym_mode_ == 1);
+      };
       if (!resid[p].empty()) {
-        MF_TRY(tuned_plan(fb, cgq[p], plan_cgq_[p], io, scr_, st_, tune_));
+        MF_TRY(pick(fb, cgq[p], plan_cgq_[p], io));
         MF_TRY(build_plan<float>(fb, resid[p], plan_resid_[p], plan_cgq_[p].shape));
       }
-      // Packed force: once per unordered pair unless the tuner measured an
-      // all-pairs shape faster on these scenes.
-      bool sym = false;
-      if (!force[p].empty()) MF_TRY(tuned_plan(gb, force[p], plan_force_[p], ig, scr_, st_, tune_, p ? &sym : nullptr));
+      if (!force[p].empty()) MF_TRY(pick(gb, force[p], plan_force_[p], ig));
       for (const Plan<float>* pl : {&plan_resid_[p], &plan_cgq_[p], &plan_force_[p]}) {
         if (pl->n_scenes == 0) continue;
         size_t pd = 0, nc = 0;
         plan_scratch_needs(*pl, &pd, &nc);
         MF_TRY(scr_.ensure(pd, nc));
-      }
-      if (p) {
-        plan_force_sym_.n_scenes = 0;
-        plan_force_sym_.host.clear();
-        if (sym) {
-          MF_TRY(build_force_sym_plan(force[p], plan_force_sym_));
-          size_t pd = 0;
-          force_sym_needs(plan_force_sym_, &pd);
-          MF_TRY(scr_.ensure(pd, 0));
-        }
       }
     }
 
@@ -313,9 +308,7 @@ class Batch {
         pr.first->host.clear();
       }
     }
-    plan_force_sym_ = std::move(o.plan_force_sym_);
-    plan_force_sym_.n_scenes = 0;
-    plan_force_sym_.host.clear();
+
   }
   int scenes() const { return int(sc_.size()); }
 
@@ -365,13 +358,8 @@ class Batch {
       io.spos = pos2_.as<float4>();
       io.smom = mom2_.as<float4>();
       io.corr4 = corr_.as<float4>();
-      if (plan_force_sym_.n_scenes) {
-        MF_TRY(run_force_sym(plan_force_sym_, io, scr_, st_));
-        ctr_.kernel_launches += 4;
-      } else {
-        MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
-        ctr_.kernel_launches += 3;
-      }
+      MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
+      ctr_.kernel_launches += plan_force_[1].shape == kShapeSym ? 4 : 3;
     }
     ctr_.force_passes += 1;
     ctr_.force_pairs += pairs_;
@@ -562,7 +550,7 @@ class Batch {
       io.smom = mom2_.as<float4>();
       io.corr4 = corr_.as<float4>();
       MF_TRY(run_plan<float>(plans[1], io, scr_, st_));
-      ctr_.kernel_launches += 3;
+      ctr_.kernel_launches += plans[1].shape == kShapeSym ? 4 : 3;
     }
     return MF_OK;
   }
@@ -593,8 +581,8 @@ class Batch {
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
   Plan<float> plan_resid_[2], plan_cgq_[2], plan_force_[2];  // [0] exact branches, [1] packed
-  Plan<float> plan_force_sym_;  // the packed scenes' force once per unordered pair (n_scenes 0 when unused)
   Tune tune_ = Tune::OnMiss;
+  int sym_mode_ = default_sym_mode();  // pair-symmetric products: 0 never, 1 tuned, 2 always
   Scratch scr_;
   CellList cells_;
   mf_counters ctr_ = {};

@@ -370,7 +370,7 @@ class Engine final : public EngineBase {
       for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
     io.naive_quirks = naive_ ? 1 : 0;
     if (plan_force_.body == Body::ForceF2) MF_TRY(prepare_packed(mom4(), true, io));
-    MF_TRY(run(plan_force_sym_.n_scenes ? plan_force_sym_ : plan_force_, io));
+    MF_TRY(run(plan_force_, io));
     ctr_.force_passes += 1;
     ctr_.force_pairs += plan_force_.pairs;
     if (!kF32) publish_f(MF_Q_FORCE);
@@ -495,6 +495,13 @@ class Engine final : public EngineBase {
           MF_TRY(build_plans());
         }
         return MF_OK;
+      case MF_OPT_PAIR_SYMMETRIC:
+        if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "pair_symmetric must be 0, 1 or 2");
+        if (int(v) != sym_mode_) {
+          sym_mode_ = int(v);
+          MF_TRY(build_plans());
+        }
+        return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -516,6 +523,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_THETA: *v = fmm_cfg_.theta; return MF_OK;
       case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
       case MF_OPT_AUTOTUNE: *v = double(int(tune_)); return MF_OK;
+      case MF_OPT_PAIR_SYMMETRIC: *v = double(sym_mode_); return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -539,7 +547,6 @@ class Engine final : public EngineBase {
   CellList cells_;
   bool cells_dirty_ = true;
   Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_, plan_apply_;
-  Plan<Real> plan_force_sym_;  // packed force once per unordered pair (FP32; n_scenes 0 when unused)
   // FMM state (FP32 handles): the octree of the current positions.
   Fmm fmm_;
   // External dipoles through the FMM: their octree (particles as targets),
@@ -552,6 +559,7 @@ class Engine final : public EngineBase {
   bool fmm_dirty_ = true;
   int fmm_mode_ = 0;
   Tune tune_ = default_tune_mode();
+  int sym_mode_ = default_sym_mode();  // MF_OPT_PAIR_SYMMETRIC
   int64_t fmm_field_products_ = 0, fmm_force_products_ = 0;
   bool plans_ready_ = false;
   bool rext_zero_ = true;
@@ -633,13 +641,18 @@ class Engine final : public EngineBase {
     const Body gb = (kF32 && np_ >= kPackedForceMin) ? Body::ForceF2 : Body::Force;
     // FP32: block shapes from the autotuner, timed on this scene's own
     // positions (the tuning launches write scratch vectors only).
+    // The packed products may run once per unordered pair (kShapeSym): the
+    // tuner's candidate, and without tuning the force's default
+    // (MF_OPT_PAIR_SYMMETRIC 1); never (0); always (2).
     int fshape = 0, gshape = 0;
-    // The packed force once per unordered pair unless the tuner measured
-    // an all-pairs shape faster.
-    bool use_sym = gb == Body::ForceF2;
+    const bool offer = sym_mode_ == 1;
     if constexpr (kF32) {
       // A handle on the FMM path launches no all-pairs product: its plans
       // only carry the epilogue coefficients, so they are not timed.
+      if (!use_fmm()) {
+        fshape = default_shape(fb, {base}, offer);
+        gshape = default_shape(gb, {base}, offer);
+      }
       if (tune_ != Tune::Off && !use_fmm()) {
         LaunchIO<Real> io;
         io.tpos = pos4();
@@ -648,7 +661,7 @@ class Engine final : public EngineBase {
         io.corr4 = fb == Body::FieldF2 ? corr_.template as<float4>() : nullptr;
         io.out4 = v4(V_DD);
         Plan<Real> tp;
-        MF_TRY(tuned_plan(fb, {base}, tp, io, scr_, st_, tune_));
+        MF_TRY(tuned_plan(fb, {base}, tp, io, scr_, st_, tune_, offer));
         fshape = tp.shape;
         LaunchIO<Real> ig;
         ig.tpos = pos4();
@@ -657,8 +670,12 @@ class Engine final : public EngineBase {
         ig.smom = gb == Body::ForceF2 ? mom2_.template as<float4>() : mom4();
         ig.corr4 = gb == Body::ForceF2 ? corr_.template as<float4>() : nullptr;
         for (int k = 0; k < 3; ++k) ig.out[k] = pubr(MF_Q_FORCE, k);
-        MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_, &use_sym));
+        MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_, offer));
         gshape = tp.shape;
+      }
+      if (sym_mode_ == 2 && !use_fmm()) {
+        if (sym_eligible(fb, {base})) fshape = kShapeSym;
+        if (sym_eligible(gb, {base})) gshape = kShapeSym;
       }
     }
     MF_TRY(build_plan<Real>(fb, {s}, plan_resid_, fshape));
@@ -676,12 +693,6 @@ class Engine final : public EngineBase {
     MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_, fshape));
     s = base;
     MF_TRY(build_plan<Real>(gb, {s}, plan_force_, gshape));
-    // The packed force once per unordered pair (the FMM handles take their
-    // own path and never use it).
-    plan_force_sym_.n_scenes = 0;
-    plan_force_sym_.host.clear();
-    if constexpr (kF32)
-      if (use_sym) MF_TRY(build_force_sym_plan({s}, plan_force_sym_));
     MF_TRY(build_plan<Real>(fb, {base}, plan_apply_, fshape));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
@@ -714,11 +725,7 @@ class Engine final : public EngineBase {
     } else {
       // Grow the scratch before the first event so the bracket holds the kernel only.
       size_t pd = 0, nc = 0;
-      if (&plan == &plan_force_sym_) {
-        if constexpr (kF32) force_sym_needs(plan, &pd);
-      } else {
-        plan_scratch_needs(plan, &pd, &nc);
-      }
+      plan_scratch_needs(plan, &pd, &nc);
       MF_TRY(scr_.ensure(pd, nc));
       TimedLaunch t;
       // statistics per kernel kind: field (0), force (1), tensor (2)
@@ -734,17 +741,10 @@ class Engine final : public EngineBase {
       MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
       timed_.push_back(t);
     }
-    ++ctr_.kernel_launches;
-    if (&plan == &plan_force_sym_) ++ctr_.kernel_launches;  // the per-particle finish
+    ctr_.kernel_launches += plan.shape == kShapeSym ? 2 : 1;  // pair-symmetric: pair kernel + finish
     return MF_OK;
   }
-  // The force product once per unordered pair (plan_force_sym_), or a plan of
-  // the all-pairs kernel.
-  mf_status launch(const Plan<Real>& plan, const LaunchIO<Real>& io) {
-    if constexpr (kF32)
-      if (&plan == &plan_force_sym_) return run_force_sym(plan, io, scr_, st_);
-    return run_plan<Real>(plan, io, scr_, st_);
-  }
+  mf_status launch(const Plan<Real>& plan, const LaunchIO<Real>& io) { return run_plan<Real>(plan, io, scr_, st_); }
 
  public:
   mf_status kernel_stats(int kind, mf_kernel_stats* out) override {

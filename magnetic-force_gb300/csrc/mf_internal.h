@@ -151,6 +151,9 @@ struct Shape {
 constexpr int kShapes = 5;
 constexpr Shape kShapeTable[kShapes] = {{256, 2, 256}, {128, 2, 256}, {256, 1, 256}, {128, 4, 128}, {128, 4, 256}};
 inline bool shaped(Body b) { return b != Body::Tensor; }
+// Shape index of the packed field / force evaluated once per unordered pair
+// (mf_sympair.cu), for scenes whose targets are their sources.
+constexpr int kShapeSym = kShapes;
 
 // One scene of a launch before it is laid out in step space.  nt > 0, ns > 0.
 struct SceneSpec {
@@ -167,7 +170,7 @@ struct SceneSpec {
 template <class Real>
 struct Plan {
   Body body = Body::Field;
-  int shape = 0;  // FP32 shaped bodies: index into kShapeTable
+  int shape = 0;  // FP32 shaped bodies: index into kShapeTable, or kShapeSym
   int64_t total_steps = 0;
   int64_t total_tb = 0;
   int32_t n_scenes = 0;
@@ -216,14 +219,21 @@ struct LaunchIO {
   int32_t done_total = 0;
 };
 
-// The packed Kelvin-force product evaluated once per unordered pair
-// (mf_symforce.cu): a plan over scenes whose targets are their sources, and
-// its launch (the pair kernel plus the per-particle finish with the force
-// epilogue).  The scratch holds FP32 block sums: 3 floats per particle of a
-// block, per ordered block pair.
-mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan);
-void force_sym_needs(const Plan<float>& plan, size_t* partial_doubles);
-mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scratch& scr, cudaStream_t st);
+// A scene's epilogue coefficients in its launch table.
+template <class Real>
+void fill_scene_coefs(const SceneSpec& s, SceneDesc<Real>& d);
+
+// The packed field / force products evaluated once per unordered pair
+// (mf_sympair.cu; plans of shape kShapeSym, built and run through build_plan
+// and run_plan): packed FP32 bodies on scenes whose targets are their
+// sources, each starting at an even index.  A launch is the pair kernel plus
+// the per-particle finish with the body's epilogue; the scratch holds FP32
+// block sums, 3 floats per particle of a block per ordered block pair.
+bool sym_eligible(Body body, const std::vector<SceneSpec>& specs);
+mf_status build_sym_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan);
+void sym_needs(const Plan<float>& plan, size_t* partial_doubles);
+mf_status run_sym(const Plan<float>& plan, const LaunchIO<float>& io, double* partials, int32_t* err,
+                  cudaStream_t st);
 
 // Scratch sizes a plan needs.
 template <class Real>
@@ -246,15 +256,19 @@ mf_status run_plan_raw(const Plan<Real>& plan, const LaunchIO<Real>& io, double*
 // shapes, builds shape 0; CachedOnly uses a cached choice and never times.
 enum class Tune { Off = 0, OnMiss = 1, CachedOnly = 2 };
 //
-// `sym` (packed force of one scene whose targets are its sources): the force
-// once per unordered pair is one more candidate, and *sym says whether it
-// won (true without a measurement); `plan` then holds the best all-pairs
-// shape all the same.
+// allow_sym: where the scenes are eligible (sym_eligible), the launch once per
+// unordered pair (kShapeSym) is one more candidate; without tuning it is the
+// default for the packed force.
 mf_status tuned_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan, const LaunchIO<float>& io,
-                     Scratch& scratch, cudaStream_t st, Tune mode, bool* sym = nullptr);
+                     Scratch& scratch, cudaStream_t st, Tune mode, bool allow_sym = false);
+// The shape a plan gets without tuning.
+int default_shape(Body body, const std::vector<SceneSpec>& specs, bool allow_sym);
 // Default tuning mode of new handles and batches: OnMiss unless the
 // environment sets MF_AUTOTUNE=0.
 Tune default_tune_mode();
+// Default pair-symmetric mode of new handles and batches (MF_OPT_PAIR_SYMMETRIC:
+// 0 never, 1 tuned, 2 always): 1 unless the environment sets MF_PAIR_SYMMETRIC.
+int default_sym_mode();
 
 int device_sms(int device);
 int current_device();
@@ -265,7 +279,7 @@ int current_device();
 // Size class of a launch: log2 of its pairs and of its scene count.
 uint32_t tune_class(const std::vector<SceneSpec>& specs);
 // Shape for (device, body, class): the cached choice, or -1 when not tuned yet.
-int tuned_shape(Body body, uint32_t cls, bool sym_offered);
+int tuned_shape(Body body, uint32_t cls, bool sym_offered);  // kShapeSym when the pair-symmetric launch won
 // Text table of the tuned choices (device, body, class, ms per shape).
 std::string autotune_report();
 

@@ -1,10 +1,12 @@
-// mf_symforce.cu -- the packed Kelvin-force product evaluated once per
+// mf_sympair.cu -- the packed field and force products evaluated once per
 // unordered pair of particles.
 //
-// The clamped far-form pair force is antisymmetric, f_ji = -f_ij: with d the
-// same separation, the source and target dipoles swap places in
-//   f_ij = P (d (s.m) + s (d.m) + m (d.s)) + Q (d.s)(d.m) d,
-// and d changes sign.  So one evaluation serves both particles.
+// Both clamped far-form pair terms are symmetric in the pair:
+//   * the dipole field tensor T(d) = 3 d d^T r^-5 - I r^-3 is even in d, so
+//     the field at i from j is T m_j and the field at j from i is T m_i;
+//   * the Kelvin force f_ij = P (d (s.m) + s (d.m) + m (d.s)) + Q (d.s)(d.m) d
+//     is antisymmetric, f_ji = -f_ij (the dipoles swap places, d changes sign).
+// So one evaluation of the pair's scalars serves both particles.
 //
 // Work layout.  A scene's particles are cut into blocks of TB = TPB * TPT
 // (targets strided by TPB, as in the all-pairs kernel); a source tile is one
@@ -12,16 +14,19 @@
 // evenly over persistent CTAs.
 //   * I < J: each thread holds TPT targets of block I in registers and sweeps
 //     tile J (bulk-copied to shared memory on an mbarrier pipeline, 2 sources
-//     per packed f32x2 instruction).  Each f_ij is added to the target's sum
-//     and to the tile's source sums; those are reduced over the warp by a
+//     per packed f32x2 instruction).  Each pair adds into the target's sum
+//     and into the tile's source sums; those are reduced over the warp by a
 //     fixed shuffle tree and over the warps in a fixed order.
 //   * I == J: the block against itself, every ordered pair, target side only.
-// Every step writes its FP32 block sums (scaled by K) into part[K][X] -- the
-// sums for block K from partner block X, SoA per block pair -- so each entry
-// is written exactly once.  k_force_sym_finish then adds, per particle, the
-// nb entries of its block's row (compensated FP32, in a fixed order) and
-// applies the force epilogue (correction, external gradient, scale).
-// Results do not depend on scheduling.
+// Every step writes its FP32 block sums (scaled to the all-pairs kernels'
+// output units) into part[K][X] -- the sums for block K from partner block
+// X, SoA per block pair -- so each entry is written exactly once.
+// k_sym_finish then adds, per particle, the nb entries of its block's row
+// (compensated FP32, in a fixed order) and applies the body's epilogue
+// (correction, scale and addends for the field; correction, external
+// gradient and scale for the force).  Results do not depend on scheduling.
+// Force targets are read from the AoS records, field targets from the same
+// pair-layout records as the sources.
 #include <mutex>
 
 #include "mf_internal.h"
@@ -41,9 +46,8 @@ constexpr size_t kSymSmem = size_t(kSymStages) * 2 * kSymTB * sizeof(float4);
 // 128x4 2,2,4 3.14 / 12.31; 128x8 2,2,1 3.01 / 12.00; 128x8 2,4,2 2.94 /
 // 11.68; 64x8 2,2,2 2.95 / 11.56; 128x8 2,2,2 2.88 / 11.47 (254 registers,
 // 2 CTAs per SM).
+// (The field body sets its own split and pair counts below.)
 constexpr int kSymSplit = 2, kSymPair = 2;
-constexpr int kSymPhaseItems = kSymTB / 2 / kSymSplit;
-static_assert(kSymPhaseItems % kSymPair == 0, "phase items");
 
 // Reduce-scatter of NV values per lane over the warp (NV a power of two,
 // 8 .. 32): the value index halves at each level, lanes with bit b set keep
@@ -108,9 +112,81 @@ __device__ __forceinline__ void force_pair2_full(float2 tx, float2 ty, float2 tz
   f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_mul(it.mz, v)));
 }
 
-__global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float> a, float* __restrict__ part) {
+// What one pair item adds on both sides, and the scaling of the sums.
+template <bool kForce>
+struct SymBody;
+
+// Kelvin force: f_ij into the target, -f_ij into the source.
+template <>
+struct SymBody<true> {
+  static constexpr float kSrcSign = -1.f;
+  // Targets from the AoS records (a force product always has them; reading
+  // them from the pair records cost 3 % in the force kernel at N = 65,536).
+  static constexpr bool kAosTargets = true;
+  static constexpr int kSplit = kSymSplit, kPair = kSymPair;
+  __device__ static float near2(const PairConsts<float>& pc) { return pc.near2_force; }
+  __device__ static float scale() { return float(kForceK); }
+  __device__ static void pair(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
+                              const PairItems::Item& it, float near2, float2* acc, float2* src) {
+    float2 f[3];
+    force_pair2_full(tx, ty, tz, tmx, tmy, tmz, it, near2, f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      acc[c] = f2_add(acc[c], f[c]);
+      src[c] = f2_add(src[c], f[c]);
+    }
+  }
+};
+
+// Dipole field: the target gets T m_s, the source T m_t, each accumulated as
+// -(3 d (d.m) r^-5 - m r^-3) = d (d.m) (-3 r^-5) + m r^-3 with FMAs straight
+// into the sums (30 packed operations per target and item); the scale
+// -1/(4 pi) gives the all-pairs field kernels' output units.
+template <>
+struct SymBody<false> {
+  static constexpr float kSrcSign = 1.f;
+  static constexpr bool kAosTargets = false;  // a field product carries the pair records only
+  static constexpr int kSplit = 2, kPair = 2;
+  __device__ static float near2(const PairConsts<float>& pc) { return pc.near2_field; }
+  __device__ static float scale() { return -float(kInv4Pi); }
+  __device__ static void pair(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
+                              const PairItems::Item& it, float near2, float2* acc, float2* src) {
+    const float2 dx = f2_sub(tx, it.x), dy = f2_sub(ty, it.y), dz = f2_sub(tz, it.z);
+    const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+    const float2 ri = clamp_rsqrt2(r2, near2);
+    const float2 ri2 = f2_mul(ri, ri);
+    const float2 beta = f2_mul(ri2, ri);
+    const float2 a3 = f2_mul(beta, f2_mul(ri2, f2_dup(-3.f)));
+    const float2 ts = f2_mul(f2_fma(dz, it.mz, f2_fma(dy, it.my, f2_mul(dx, it.mx))), a3);
+    const float2 tt = f2_mul(f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx))), a3);
+    acc[0] = f2_fma(it.mx, beta, f2_fma(dx, ts, acc[0]));
+    acc[1] = f2_fma(it.my, beta, f2_fma(dy, ts, acc[1]));
+    acc[2] = f2_fma(it.mz, beta, f2_fma(dz, ts, acc[2]));
+    src[0] = f2_fma(tmx, beta, f2_fma(dx, tt, src[0]));
+    src[1] = f2_fma(tmy, beta, f2_fma(dy, tt, src[1]));
+    src[2] = f2_fma(tmz, beta, f2_fma(dz, tt, src[2]));
+  }
+};
+
+// Particle g of the pair-layout records (two particles per 32-byte item):
+// component k of lane g & 1.
+__device__ __forceinline__ float3 pair_rec(const float4* __restrict__ p4, int64_t g) {
+  const int64_t b = g & ~int64_t(1);
+  const float4 p0 = p4[b], p1 = p4[b + 1];
+  return (g & 1) ? make_float3(p0.y, p0.w, p1.y) : make_float3(p0.x, p0.z, p1.x);
+}
+
+__device__ __forceinline__ bool scene_done(const AllPairsArgs<float>& a, const SceneDesc<float>& sc) {
+  return a.done_flags && a.done_flags[int64_t(sc.flag_index) * a.done_stride] != 0.0;
+}
+
+template <bool kForce>
+__global__ void __launch_bounds__(kSymTPB) k_sym(const AllPairsArgs<float> a, float* __restrict__ part) {
+  using BodyT = SymBody<kForce>;
   constexpr int TPB = kSymTPB, TPT = kSymTPT, TB = kSymTB, STAGES = kSymStages;
-  constexpr int NH = kSymPhaseItems, P = kSymPair, NV = P * 6 <= 8 ? 8 : (P * 6 <= 16 ? 16 : 32);
+  constexpr int SPLIT = BodyT::kSplit, NH = TB / 2 / SPLIT, P = BodyT::kPair;
+  constexpr int NV = P * 6 <= 8 ? 8 : (P * 6 <= 16 ? 16 : 32);
+  static_assert(NH % P == 0, "phase items");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   // per warp: the source sums of the phase's pair items, [item][component * 2 + source of the pair]
@@ -122,6 +198,9 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
   const int64_t T = a.total_steps, G = gridDim.x, b = blockIdx.x;
   const int64_t k_begin = step_start(T, G, b), k_end = step_start(T, G, b + 1);
   if (k_begin >= k_end) return;
+  // A launch whose solves have all stopped does nothing.
+  if (a.n_scenes == 1 && scene_done(a, a.scenes[0])) return;
+  if (a.done_count && *a.done_count >= a.done_total) return;
   auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + size_t(s) * 2 * TB; };
   auto stage_mom = [&](int s) { return stage_pos(s) + TB; };
   if (tid == 0) {
@@ -159,14 +238,22 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
     int I, J;
     sym_block_pair(k - sc.step_off, nb, I, J);
     if (si != cur_si || I != cur_I) {  // the targets of block I
-      // Slots past the scene's end hold a zero dipole: their forces vanish
-      // on both sides of every pair.
+      // Slots past the scene's end hold a zero dipole: their terms vanish
+      // on the source side of every pair, and their own sums are not read.
 #pragma unroll
       for (int t = 0; t < TPT; ++t) {
         const int64_t li = int64_t(I) * TB + t * TPB + tid;
         const bool live = li < sc.nt;
-        const float4 p = a.tpos[sc.t_off + (live ? li : 0)];
-        const float4 m = live ? a.tmom[sc.t_off + li] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 p, m;
+        if constexpr (BodyT::kAosTargets) {
+          const float4 q = a.tpos[sc.t_off + (live ? li : 0)];
+          const float4 w = live ? a.tmom[sc.t_off + li] : make_float4(0.f, 0.f, 0.f, 0.f);
+          p = make_float3(q.x, q.y, q.z);
+          m = make_float3(w.x, w.y, w.z);
+        } else {
+          p = pair_rec(a.spos, sc.t_off + (live ? li : 0));
+          m = live ? pair_rec(a.smom, sc.t_off + li) : make_float3(0.f, 0.f, 0.f);
+        }
         tx[t] = f2_dup(p.x);
         ty[t] = f2_dup(p.y);
         tz[t] = f2_dup(p.z);
@@ -182,78 +269,76 @@ __global__ void __launch_bounds__(kSymTPB) k_force_sym(const AllPairsArgs<float>
       k_fail = k;
       break;
     }
-    const bool sym = I != J;
-    const int64_t rem = sc.ns - int64_t(J) * TB;
-    const int cnt = int(rem < TB ? rem : TB);
-    const int n_items = PairItems::items(cnt);
-    const float4* __restrict__ sp = stage_pos(s);
-    const float4* __restrict__ smv = stage_mom(s);
-    const float near2 = sc.pc.near2_force;
-    const float kk = float(kForceK);
-    float2 acc[TPT][3];
+    // A stopped scene's sums are not written (block-uniform).  Force products
+    // carry no stop flags; the check is compiled out of that kernel.
+    if (kForce || !scene_done(a, sc)) {
+      const bool sym = I != J;
+      const int64_t rem = sc.ns - int64_t(J) * TB;
+      const int cnt = int(rem < TB ? rem : TB);
+      const int n_items = PairItems::items(cnt);
+      const float4* __restrict__ sp = stage_pos(s);
+      const float4* __restrict__ smv = stage_mom(s);
+      const float near2 = BodyT::near2(sc.pc);
+      const float kk = BodyT::scale();
+      float2 acc[TPT][3];
 #pragma unroll
-    for (int t = 0; t < TPT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
-    for (int h = 0; h < kSymSplit; ++h) {
-      const int j_end = min(n_items, (h + 1) * NH);
+      for (int t = 0; t < TPT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
+      for (int h = 0; h < SPLIT; ++h) {
+        const int j_end = min(n_items, (h + 1) * NH);
 #pragma unroll 2
-      for (int j0 = h * NH; j0 < j_end; j0 += P) {
-        float v[NV];
+        for (int j0 = h * NH; j0 < j_end; j0 += P) {
+          float v[NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) v[q] = 0.f;
+          for (int q = 0; q < NV; ++q) v[q] = 0.f;
 #pragma unroll
-        for (int p = 0; p < P; ++p) {
-          // An item past the tile's end is a zero dipole at the origin: its
-          // force is exactly zero on both sides (finite distances, clamped).
-          const bool in = p == 0 || j0 + p < j_end;
-          const PairItems::Item it =
-              in ? PairItems::load_item(sp, smv, j0 + p) : PairItems::Item{{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f},
-                                                                          {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-          float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+          for (int p = 0; p < P; ++p) {
+            // An item past the tile's end is a zero dipole at the origin:
+            // nothing on the target side; its source-side sums belong to
+            // slots past the scene's end, which are never read.
+            const bool in = p == 0 || j0 + p < j_end;
+            const PairItems::Item it =
+                in ? PairItems::load_item(sp, smv, j0 + p) : PairItems::Item{{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f},
+                                                                            {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
-          for (int t = 0; t < TPT; ++t) {
-            float2 f[3];
-            force_pair2_full(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, f);
+            for (int t = 0; t < TPT; ++t) BodyT::pair(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              acc[t][c] = f2_add(acc[t][c], f[c]);
-              src[c] = f2_add(src[c], f[c]);
+              v[p * 6 + 2 * c] = src[c].x;
+              v[p * 6 + 2 * c + 1] = src[c].y;
             }
           }
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            v[p * 6 + 2 * c] = src[c].x;
-            v[p * 6 + 2 * c + 1] = src[c].y;
+          if (sym) {  // warp-uniform
+            const float w = warp_reduce_scatter<NV>(v, lane);
+            const int kv = lane / (32 / NV);
+            if (lane % (32 / NV) == 0 && kv < 6 * P) s_srcf[wid][(j0 - h * NH) * 6 + kv] = w;
           }
         }
-        if (sym) {  // warp-uniform
-          const float w = warp_reduce_scatter<NV>(v, lane);
-          const int kv = lane / (32 / NV);
-          if (lane % (32 / NV) == 0 && kv < 6 * P) s_srcf[wid][(j0 - h * NH) * 6 + kv] = w;
-        }
-      }
-      if (sym) {
-        __syncthreads();  // the phase's s_srcf is complete
-        // sums for block J from block I: sources 2 h NH .. 2 (h + 1) NH - 1
-        float* ps = part + (sc.tb_off + int64_t(J) * nb + I) * 3 * TB;
-        for (int r = tid; r < 2 * NH; r += TPB) {
-          const int j = r >> 1, rr = h * 2 * NH + r;
+        if (sym) {
+          __syncthreads();  // the phase's s_srcf is complete
+          // sums for block J from block I: sources 2 h NH .. 2 (h + 1) NH - 1
+          float* ps = part + (sc.tb_off + int64_t(J) * nb + I) * 3 * TB;
+          const float ks = kk * BodyT::kSrcSign;
+          for (int r = tid; r < 2 * NH; r += TPB) {
+            const int j = r >> 1, rr = h * 2 * NH + r;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float x = 0.f;
+            for (int c = 0; c < 3; ++c) {
+              float x = 0.f;
 #pragma unroll
-            for (int w = 0; w < kSymWarps; ++w) x += s_srcf[w][j * 6 + 2 * c + (r & 1)];
-            ps[c * TB + rr] = -x * kk;  // f_ji = -f_ij
+              for (int w = 0; w < kSymWarps; ++w) x += s_srcf[w][j * 6 + 2 * c + (r & 1)];
+              ps[c * TB + rr] = x * ks;
+            }
           }
+          if (h + 1 < SPLIT) __syncthreads();  // read before the next phase overwrites it
         }
-        if (h + 1 < kSymSplit) __syncthreads();  // read before the next phase overwrites it
       }
-    }
-    float* pr = part + (sc.tb_off + int64_t(I) * nb + J) * 3 * TB;  // sums for block I from block J
+      float* pr = part + (sc.tb_off + int64_t(I) * nb + J) * 3 * TB;  // sums for block I from block J
 #pragma unroll
-    for (int t = 0; t < TPT; ++t) {
-      const int r = t * TPB + tid;
+      for (int t = 0; t < TPT; ++t) {
+        const int r = t * TPB + tid;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) pr[c * TB + r] = (acc[t][c].x + acc[t][c].y) * kk;
+        for (int c = 0; c < 3; ++c) pr[c * TB + r] = (acc[t][c].x + acc[t][c].y) * kk;
+      }
     }
     __syncthreads();  // every thread is done with stage s and with s_srcf
     if (tid == 0 && k + STAGES < k_end) {
@@ -293,11 +378,14 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
 // Per particle: the nb partner-block sums of its block, compensated FP32
 // (sum and carried rounding error) in four chains over the blocks X = q
 // (mod 4) -- a fixed order, with four independent chains in flight -- the
-// chains combined in FP64 as (c0 + c1) + (c2 + c3); then the force epilogue.  g runs over [g0, g0 + n_span), the particle
-// indices from the first scene's start to the last one's end (scenes are in
-// increasing t_off order; indices between scenes are skipped).
-__global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __restrict__ part, int64_t g0,
-                                   int64_t n_span) {
+// chains combined in FP64 as (c0 + c1) + (c2 + c3); then the body's
+// epilogue.  g runs over [g0, g0 + n_span), the particle indices from the
+// first scene's start to the last one's end (scenes are in increasing t_off
+// order; indices between scenes are skipped, and so are stopped scenes).
+template <bool kForce>
+__global__ void k_sym_finish(const AllPairsArgs<float> a, const float* __restrict__ part, int64_t g0,
+                             int64_t n_span) {
+  if (a.done_count && *a.done_count >= a.done_total) return;
   for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < n_span;
        g += int64_t(gridDim.x) * blockDim.x) {
     const int64_t gi = g0 + g;
@@ -309,7 +397,8 @@ __global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __r
     }
     const SceneDesc<float>& sc = a.scenes[lo];
     const int64_t i = gi - sc.t_off;
-    if (i >= sc.nt) continue;  // the padding slot after an odd scene
+    if (i >= sc.nt) continue;  // the padding slot after an odd scene, or a scene not in the plan
+    if (scene_done(a, sc)) continue;
     const int K = int(i / kSymTB), r = int(i % kSymTB);
     const int nb = sc.n_tb;
     const float* row = part + (sc.tb_off + int64_t(K) * nb) * 3 * kSymTB;
@@ -339,14 +428,19 @@ __global__ void k_force_sym_finish(const AllPairsArgs<float> a, const float* __r
       for (int q = 0; q < 4; ++q) w[q] = double(s4[q][c]) + double(e4[q][c]);
       v[c] = (w[0] + w[1]) + (w[2] + w[3]);
     }
-    const float4 m = a.tmom[gi];
-    force_epilogue<float>(a, sc, gi, double(m.x), double(m.y), double(m.z), v);
+    if constexpr (kForce) {
+      const float4 m = a.tmom[gi];
+      force_epilogue<float>(a, sc, gi, double(m.x), double(m.y), double(m.z), v);
+    } else {
+      FieldBody<float>::epilogue(a, sc, gi, FieldBody<float>::TData{}, v);
+    }
   }
 }
 
-// Resident CTAs of k_force_sym on the current device (its shared-memory
+// Resident CTAs of k_sym<kForce> on the current device (its shared-memory
 // attribute set on the first call).  Plans call it when they are built, so
 // a launch inside a stream capture makes no attribute or occupancy calls.
+template <bool kForce>
 mf_status sym_grid_max(int* out) {
   static std::mutex mu;
   static int cache[64] = {};
@@ -354,27 +448,39 @@ mf_status sym_grid_max(int* out) {
   std::lock_guard<std::mutex> lk(mu);
   int& g = cache[dev >= 0 && dev < 64 ? dev : 0];
   if (!g) {
-    MF_CUDA_TRY(cudaFuncSetAttribute(k_force_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSymSmem)));
+    MF_CUDA_TRY(cudaFuncSetAttribute(k_sym<kForce>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSymSmem)));
     int per_sm = 0;
-    MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_sym, kSymTPB, kSymSmem));
+    MF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sym<kForce>, kSymTPB, kSymSmem));
     g = std::max(per_sm, 1) * device_sms(dev);
   }
   *out = g;
   return MF_OK;
 }
 
+mf_status sym_grid(Body body, int* out) {
+  return body == Body::ForceF2 ? sym_grid_max<true>(out) : sym_grid_max<false>(out);
+}
+
 }  // namespace
 
-mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan) {
-  plan.body = Body::ForceF2;
-  plan.shape = 0;
+bool sym_eligible(Body body, const std::vector<SceneSpec>& specs) {
+  if (body != Body::FieldF2 && body != Body::ForceF2) return false;
+  for (const SceneSpec& s : specs)
+    if (s.nt <= 0 || s.nt != s.ns || s.t_off != s.s_off || s.t_off % 2) return false;
+  return !specs.empty();
+}
+
+mf_status build_sym_plan(Body body, const std::vector<SceneSpec>& specs, Plan<float>& plan) {
+  if (!sym_eligible(body, specs))
+    return fail(MF_ERR_INVALID_ARG,
+                "pair-symmetric plan: packed field or force, targets equal to the sources, scenes at even indices");
+  plan.body = body;
+  plan.shape = kShapeSym;
   plan.host.clear();
   int64_t step = 0, blocks = 0;
   double pairs = 0, evals = 0;
   for (const SceneSpec& s : specs) {
-    if (s.nt <= 0 || s.nt != s.ns || s.t_off != s.s_off)
-      return fail(MF_ERR_INVALID_ARG, "symmetric force plan: targets must be the sources");
-    if (s.t_off % 2) return fail(MF_ERR_INVALID_ARG, "symmetric force plan: scene must start at an even index");
+    if (!(s.h > 0.0)) return fail(MF_ERR_INVALID_ARG, "build_plan: smoothing length must be > 0");
     SceneDesc<float> d;
     memset(&d, 0, sizeof(d));
     d.t_off = s.t_off;
@@ -387,8 +493,7 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
     d.step_off = step;
     d.tb_off = blocks;  // first block pair of this scene in the partial array
     d.flag_index = s.flag_index >= 0 ? s.flag_index : int32_t(plan.host.size());
-    d.pc = make_pair_consts<float>(s.h);
-    d.scale = float(s.scale);
+    fill_scene_coefs<float>(s, d);
     step += nb * (nb + 1) / 2;
     blocks += nb * nb;
     pairs += double(s.nt) * double(s.ns);
@@ -396,7 +501,7 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
     plan.host.push_back(d);
   }
   int gmax = 0;
-  MF_TRY(sym_grid_max(&gmax));
+  MF_TRY(sym_grid(body, &gmax));
   plan.total_steps = step;
   plan.total_tb = blocks;
   plan.n_scenes = int32_t(plan.host.size());
@@ -408,18 +513,17 @@ mf_status build_force_sym_plan(const std::vector<SceneSpec>& specs, Plan<float>&
   return MF_OK;
 }
 
-void force_sym_needs(const Plan<float>& plan, size_t* partial_doubles) {
-  // FP32 block sums: 3 x TB per block pair, in doubles
+void sym_needs(const Plan<float>& plan, size_t* partial_doubles) {
+  // FP32 block sums: 3 x TB per ordered block pair, in doubles
   *partial_doubles = (size_t(plan.total_tb) * 3 * kSymTB + 1) / 2;
 }
 
-mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scratch& scr, cudaStream_t st) {
+mf_status run_sym(const Plan<float>& plan, const LaunchIO<float>& io, double* partials, int32_t* err,
+                  cudaStream_t st) {
   if (plan.total_steps <= 0) return MF_OK;
-  size_t pd = 0;
-  force_sym_needs(plan, &pd);
-  MF_TRY(scr.ensure(pd, 0));
+  const bool force = plan.body == Body::ForceF2;
   int gmax = 0;
-  MF_TRY(sym_grid_max(&gmax));
+  MF_TRY(sym_grid(plan.body, &gmax));
   AllPairsArgs<float> a;
   memset(&a, 0, sizeof(a));
   a.scenes = plan.d_scenes.as<SceneDesc<float>>();
@@ -433,17 +537,30 @@ mf_status run_force_sym(const Plan<float>& plan, const LaunchIO<float>& io, Scra
     a.out[k] = io.out[k];
     a.rext[k] = io.rext[k];
   }
+  a.out4 = io.out4;
+  a.add4 = io.add4;
+  a.add4b = io.add4b;
   a.naive_quirks = io.naive_quirks;
+  a.done_flags = io.done_flags;
+  a.done_stride = io.done_stride;
   a.corr4 = io.corr4;
-  a.err = scr.err.as<int32_t>();
-  float* part = reinterpret_cast<float*>(scr.partials.as<double>());
+  a.done_count = io.done_count;
+  a.done_total = io.done_total;
+  a.err = err;
+  float* part = reinterpret_cast<float*>(partials);
   const int64_t g = std::min<int64_t>(plan.total_steps, gmax);
-  k_force_sym<<<unsigned(g), kSymTPB, kSymSmem, st>>>(a, part);
-  MF_CUDA_TRY(cudaGetLastError());
   const int64_t g0 = plan.host.front().t_off;
   const int64_t n_span = plan.host.back().t_off + plan.host.back().nt - g0;
   const int64_t fb = std::min<int64_t>((n_span + 255) / 256, 8192);
-  k_force_sym_finish<<<unsigned(fb), 256, 0, st>>>(a, part, g0, n_span);
+  if (force) {
+    k_sym<true><<<unsigned(g), kSymTPB, kSymSmem, st>>>(a, part);
+    MF_CUDA_TRY(cudaGetLastError());
+    k_sym_finish<true><<<unsigned(fb), 256, 0, st>>>(a, part, g0, n_span);
+  } else {
+    k_sym<false><<<unsigned(g), kSymTPB, kSymSmem, st>>>(a, part);
+    MF_CUDA_TRY(cudaGetLastError());
+    k_sym_finish<false><<<unsigned(fb), 256, 0, st>>>(a, part, g0, n_span);
+  }
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

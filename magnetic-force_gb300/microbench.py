@@ -205,9 +205,9 @@ def engine(args, np, torch, mfgb, scenes):
     r = max(st["launches"], 1)
     ms = st["total_ms"] / r
     pairs = float(sc.n) * sc.n
-    # the force evaluated once per unordered pair: 55 FLOP per evaluation
+    # once per unordered pair: 49 (field) / 55 (force) FLOP per evaluation
     sym = st["evals"] < st["pairs"]
-    flop = 55.0 * st["evals"] / r if sym else FLOP[kind] * pairs
+    flop = (55.0 if kind == "force" else 49.0) * st["evals"] / r if sym else FLOP[kind] * pairs
     print(json.dumps({"kernel": args.kernel, "n": sc.n, "kernel_ms": ms, "pairs_per_s": pairs / (ms * 1e-3),
                       "symmetric": sym, "tflops": flop / (ms * 1e-3) / 1e12,
                       "autotune": mfgb.autotune_report()}), flush=True)

@@ -101,6 +101,7 @@ b.eval_force()
 out = {"launches": b.counters()["kernel_launches"]}
 for k in range(len(scs)):
     out["F%d" % k] = b.get(k, "magnetic_bodyforce")
+    out["B%d" % k] = b.get(k, "total_B_over_mu0")
 a, g = mfgb.Batch(scs), mfgb.Batch(scs)
 for x in (a, g):
     x.solve(300, 1e-7)
@@ -112,20 +113,21 @@ np.savez(sys.argv[1], **out)
 """
 
 
-def test_packed_force_once_per_pair_in_batch(mf, tmp_path):
-    # Scenes of the packed force path, tuning off (a child process with
-    # MF_AUTOTUNE=0, read once per process): the batch evaluates their force
-    # once per unordered pair -- 4 launches: pair records, near-field
-    # correction, pair kernel, per-particle finish.  Each scene matches the
-    # same scene solved alone, and graph-captured steps match plain steps
-    # bit for bit.
+def test_packed_products_once_per_pair_in_batch(mf, tmp_path):
+    # Scenes of the packed field and force paths in a child process with
+    # MF_PAIR_SYMMETRIC=2 and MF_AUTOTUNE=0 (both read once per process): the
+    # batch evaluates every field and force product once per unordered pair,
+    # the CG's per-scene stop flags included -- a force product is 4
+    # launches: pair records, near-field correction, pair kernel,
+    # per-particle finish.  Each scene matches the same scene solved alone,
+    # and graph-captured steps match plain steps bit for bit.
     import os
     import subprocess
     import sys
     here = os.path.dirname(os.path.abspath(__file__))
     pkg = os.path.join(os.path.dirname(here), "magnetic-force_gb300")
     path = str(tmp_path / "batch.npz")
-    env = dict(os.environ, MF_AUTOTUNE="0")
+    env = dict(os.environ, MF_AUTOTUNE="0", MF_PAIR_SYMMETRIC="2")
     subprocess.run([sys.executable, "-c", CHILD, path, here, pkg], env=env, check=True, timeout=600)
     got = np.load(path)
     assert int(got["launches"]) == 4
@@ -136,5 +138,6 @@ def test_packed_force_once_per_pair_in_batch(mf, tmp_path):
         s.set_option("rel_tol", 1e-7)
         s.solve(300)
         s.evaluate_fitted_near_foece()
+        assert rel(got["B%d" % k], s.total_B_over_mu0) < 1e-5
         assert rel(got["F%d" % k], s.magnetic_bodyforce) < 1e-5
         s.close()

@@ -238,18 +238,22 @@ def test_autotuned_shapes_match_default(mf):
 
 @pytest.mark.parametrize("n", [14337, 32769])
 def test_force_once_per_pair_matches_oracle(mf, oracle, n):
-    # The packed force of one scene evaluated once per unordered pair
-    # (f_ji = -f_ij), taken without tuning: the kernel statistics show one
-    # evaluation per unordered pair.  n is one past a multiple of the
-    # kernel's block (1,024 particles), so the last block holds a single
-    # particle.
+    # The packed field and force of one scene evaluated once per unordered
+    # pair (T even in d, f_ji = -f_ij; MF_OPT_PAIR_SYMMETRIC 2): the kernel
+    # statistics show one evaluation per unordered pair.  n is one past a
+    # multiple of the kernel's block (1,024 particles), so the last block
+    # holds a single particle.
     import scenes
     sc = scenes.jittered_lattice(n, "sphere", radius=0.5, chi=2.0, seed=n)
     s = make(mf, sc)
-    s.set_option("autotune", 0)
+    s.set_option("pair_symmetric", 2)
+    assert s.get_option("pair_symmetric") == 2
     s.set_option("solver", mf.SOLVER_CG)
-    s.solve(200)
     s.set_option("kernel_timing", 1)
+    it, relres = s.solve(200)
+    assert relres < 1e-6
+    fs = s.kernel_stats("field")
+    assert fs["launches"] >= 1 and fs["evals"] == fs["launches"] * float(n) * (n - 1) / 2
     s.reset_counters()
     s.evaluate_fitted_near_foece()
     st = s.kernel_stats("force")
@@ -261,3 +265,33 @@ def test_force_once_per_pair_matches_oracle(mf, oracle, n):
     assert rel(got, F) < 1e-5
     # internal forces only (uniform applied field): they sum to zero
     assert np.linalg.norm(got.sum(axis=0)) < 1e-5 * np.abs(got).sum()
+
+
+@pytest.mark.parametrize("n", [2049, 5001])
+def test_field_once_per_pair_matches_oracle(mf, oracle, n):
+    # Packed field products once per unordered pair through a whole CG
+    # solve (the launches after convergence skipped by the done flag), against
+    # the FP64 oracle; and the same handle with every ordered pair evaluated
+    # (MF_OPT_PAIR_SYMMETRIC 0) agrees to FP32 summation order.
+    import scenes
+    sc = scenes.jittered_lattice(n, "sphere", radius=0.5, chi=2.0, seed=n + 7)
+    want = oracle_step(oracle, sc.pos, sc.h, sc.volume, sc.chi, sc.H0)
+    out = {}
+    for mode in (2, 0):
+        s = make(mf, sc)
+        s.set_option("pair_symmetric", mode)
+        s.set_option("solver", mf.SOLVER_CG)
+        s.set_option("kernel_timing", 1)
+        it, relres = s.solve(200)
+        assert relres < 1e-6
+        st = s.kernel_stats("field")
+        per = float(n) * (n - 1) / 2 if mode == 2 else float(n) * n
+        assert st["evals"] == st["launches"] * per
+        s.evaluate_fitted_near_foece()
+        out[mode] = (np.asarray(s.total_B_over_mu0), np.asarray(s.M), np.asarray(s.magnetic_bodyforce))
+        s.close()
+    assert rel(out[2][0], want["b"]) < 1e-5
+    assert rel(out[2][1], want["M"]) < 1e-5
+    assert rel(out[2][2], want["F"]) < 1e-5
+    assert rel(out[2][0], out[0][0]) < 1e-6
+    assert rel(out[2][2], out[0][2]) < 1e-5
