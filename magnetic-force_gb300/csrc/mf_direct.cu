@@ -64,9 +64,9 @@ struct DirectCtx {
 
 DirectCtx g_ctx[64];
 
-mf_status get_plan(DirectCtx& c, Body body, int64_t nt, int64_t ns, double h, const Plan<float>** out) {
+mf_status get_plan(DirectCtx& c, Body body, int64_t nt, int64_t ns, double h, int shape, const Plan<float>** out) {
   const int b = int(body);
-  if (!c.plan_ok[b] || c.plan_nt[b] != nt || c.plan_ns[b] != ns || c.plan_h[b] != h) {
+  if (!c.plan_ok[b] || c.plan_nt[b] != nt || c.plan_ns[b] != ns || c.plan_h[b] != h || c.plan[b].shape != shape) {
     SceneSpec s;
     s.t_off = 0;
     s.nt = nt;
@@ -74,7 +74,7 @@ mf_status get_plan(DirectCtx& c, Body body, int64_t nt, int64_t ns, double h, co
     s.ns = ns;
     s.h = h;
     s.scale = 1.0;
-    MF_TRY(build_plan<float>(body, {s}, c.plan[b]));
+    MF_TRY(build_plan<float>(body, {s}, c.plan[b], shape));
     c.plan_ok[b] = true;
     c.plan_nt[b] = nt;
     c.plan_ns[b] = ns;
@@ -144,8 +144,19 @@ mf_status direct_impl(Body body, const float* targets, int64_t nt, const float* 
     io.smom = c.m2.as<float4>();
     io.corr4 = c.corr.as<float4>();
   }
+  // One particle set (the force always; the field when the caller passes
+  // the sources as the targets): each unordered pair once for both
+  // particles from kSymDirectMin particles on (no tuning on this path: a
+  // call can be seconds long), per MF_PAIR_SYMMETRIC.
+  int shape = 0;
+  if ((launch_body == Body::FieldF2 || launch_body == Body::ForceF2) &&
+      (body == Body::Force || (targets == sources && nt == ns))) {
+    const int mode = default_sym_mode();
+    if (mode == 2 || (mode == 1 && nt >= kSymDirectMin)) shape = kShapeSym;
+  }
+  if (shape == kShapeSym) io.tpos = c.s4.as<float4>();  // the same records as the sources
   const Plan<float>* plan = nullptr;
-  MF_TRY(get_plan(c, launch_body, nt, ns, h, &plan));
+  MF_TRY(get_plan(c, launch_body, nt, ns, h, shape, &plan));
   float* soa = c.soa.as<float>();
   for (int k = 0; k < kOut; ++k) io.out[k] = soa + int64_t(k) * nt;
   if (body == Body::Force) {

@@ -153,3 +153,21 @@ def test_large_subsample(mf, cuda, oracle):
     idx = rng.choice(sc.n, 512, replace=False)
     want = oracle.field(sc.pos[idx], sc.pos, m, sc.h)
     assert rel(got[idx], want) < TOL
+
+
+def test_force_once_per_pair_direct(mf, cuda, oracle):
+    # mf_direct_force from 32,768 particles on evaluates each unordered pair
+    # once (f_ji = -f_ij); n is one past a multiple of the 1,024-particle
+    # block, with an external gradient tensor in the epilogue.
+    rng = np.random.default_rng(33793)
+    n = 33793
+    x = rng.random((n, 3)).astype(np.float32)
+    m = (rng.normal(size=(n, 3)) * 1e-3).astype(np.float32)
+    h = 0.01
+    ext_s = rng.random((5, 3)).astype(np.float32) * 2 - 0.5
+    ext_m = rng.normal(size=(5, 3)).astype(np.float32)
+    _, rext = oracle.ext(x, ext_s, ext_m, [0, 0, 1], 0.1)
+    rext32 = rext.astype(np.float32)
+    got = mf.direct_force(dev(cuda, x), dev(cuda, m), h, dev(cuda, rext32, 9)).cpu().numpy()
+    want = oracle.force(x, m, h, rext32)
+    assert rel(got, want) < TOL
