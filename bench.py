@@ -535,6 +535,7 @@ def run_batch(args, rank, world, local):
                       "path": "one mf_solver per scene, scenes one after the other"},
             "batched_over_plain": value / plain_value,
             "scene_generation_s": round(gen_s, 1), "clocks": clk,
+            "autotune": mfgb.autotune_report(),
         }
         print(json.dumps(out), flush=True)
     b.close()

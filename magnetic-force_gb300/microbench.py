@@ -178,7 +178,8 @@ def batch(args, torch, mfgb, scenes):
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) * 1e3 / max(args.reps, 1)
     torch.cuda.profiler.stop()
-    print(json.dumps({"kernel": "batch", "scenes": 256, "ms_per_step": ms, "counters": b.counters()}), flush=True)
+    print(json.dumps({"kernel": "batch", "scenes": 256, "ms_per_step": ms, "counters": b.counters(),
+                      "autotune": mfgb.autotune_report()}), flush=True)
 
 
 def engine(args, np, torch, mfgb, scenes):
