@@ -1,4 +1,4 @@
-"""Host-side model of the all-pairs kernel's work split (no GPU).
+"""Host-side models of the pair kernels' work splits (no GPU).
 
 The kernel (mf_allpairs.cuh) walks a flat (target block, source tile) step
 space split evenly over a grid of CTAs; target blocks cut by a CTA boundary
@@ -6,7 +6,9 @@ are finished from FP64 partials by the last CTA to arrive.  This model replays
 that control flow for many shapes and checks that every (target block, tile)
 pair is computed exactly once, that every partial the reducer reads was
 written by the CTA it expects, in the slot it expects, and that the ticket
-count equals the number of writers.
+count equals the number of writers.  A second model covers the pair-symmetric
+launch (mf_sympair.cu): its step-to-block-pair map, that every block-sum slot
+is written once, and that the finish's row sums equal the direct sums.
 """
 import itertools
 import random
@@ -108,3 +110,111 @@ def test_many_scenes():
         scenes = [(n, n) for n in (int(rng.uniform(1, 5000)) for _ in range(rng.randint(1, 40)))]
         for G in (1, 13, 152, 304, 608):
             simulate(scenes, 256, 512, G)
+
+
+# ---------------------------------------------------------------------------
+# The pair-symmetric launch (mf_sympair.cu): steps are the block pairs
+# (I, J), I <= J, row by row; step I < J writes the target-side block sums
+# into part[I][J] and the (negated, for the force) source-side ones into
+# part[J][I]; a diagonal step writes part[I][I] from every ordered pair.  The
+# finish adds, per particle, the nb entries of its block's row.
+# ---------------------------------------------------------------------------
+import math
+
+import numpy as np
+
+
+def sym_block_pair(l, nb):
+    """Step l -> (I, J), as the device computes it (double sqrt, then exact
+    integer corrections)."""
+    b = 2.0 * nb + 1.0
+    i = int((b - math.sqrt(b * b - 8.0 * l)) * 0.5)
+    i = min(max(i, 0), nb - 1)
+
+    def row_start(r):
+        return r * nb - r * (r - 1) // 2
+
+    while i > 0 and row_start(i) > l:
+        i -= 1
+    while i < nb - 1 and row_start(i + 1) <= l:
+        i += 1
+    return i, i + (l - row_start(i))
+
+
+def test_sym_block_pairs_are_a_bijection():
+    for nb in list(range(1, 130)) + [511]:
+        steps = nb * (nb + 1) // 2
+        seen = [sym_block_pair(l, nb) for l in range(steps)]
+        want = [(i, j) for i in range(nb) for j in range(i, nb)]
+        assert seen == want, nb
+    # large scenes: the first and last step of every row
+    for nb in (1024, 4097, 65536):
+        l = 0
+        for i in range(nb):
+            assert sym_block_pair(l, nb) == (i, i)
+            l += nb - i
+            assert sym_block_pair(l - 1, nb) == (i, nb - 1)
+
+
+def sym_plan(sizes, tb):
+    out, step, blocks, off = [], 0, 0, 0
+    for n in sizes:
+        nb = -(-n // tb)
+        out.append(dict(n=n, off=off, nb=nb, step_off=step, tb_off=blocks))
+        step += nb * (nb + 1) // 2
+        blocks += nb * nb
+        off += n + (n & 1)  # scenes start at even indices
+    return out, step, blocks
+
+
+def test_sym_partial_slots_written_once():
+    rng = random.Random(5)
+    for trial in range(40):
+        tb = rng.choice([64, 512, 1024])
+        sizes = [rng.randint(1, 5 * tb) for _ in range(rng.randint(1, 6))]
+        plan, T, blocks = sym_plan(sizes, tb)
+        G = rng.randint(1, 700)
+        G = min(G, T)
+        writes = [0] * blocks
+        done = [0] * T
+        for b in range(G):
+            for k in range(start(T, G, b), start(T, G, b + 1)):
+                done[k] += 1
+                sc = max((s for s in plan if s["step_off"] <= k), key=lambda s: s["step_off"])
+                I, J = sym_block_pair(k - sc["step_off"], sc["nb"])
+                writes[sc["tb_off"] + I * sc["nb"] + J] += 1
+                if I != J:
+                    writes[sc["tb_off"] + J * sc["nb"] + I] += 1
+        assert all(d == 1 for d in done)
+        assert all(w == 1 for w in writes)
+
+
+def test_sym_sums_equal_the_direct_sums():
+    # Antisymmetric pair values (the force) with the source side negated,
+    # and symmetric ones (the field) taken as they are: the finish's row sum
+    # per particle equals the direct sum over all partners.
+    rng = np.random.default_rng(3)
+    tb = 8
+    for sizes in ([1], [7], [8], [17, 2, 31], [40]):
+        plan, T, blocks = sym_plan(sizes, tb)
+        for sign in (-1.0, 1.0):
+            for sc in plan:
+                n, nb = sc["n"], sc["nb"]
+                a, c = rng.normal(size=n), rng.normal(size=n)
+                f = np.outer(a, c) + sign * np.outer(c, a)  # f[i, j] = sign * f[j, i]
+                if sign < 0:
+                    np.fill_diagonal(f, 0.0)
+                part = np.full((nb, nb, tb), np.nan)
+                for l in range(nb * (nb + 1) // 2):
+                    I, J = sym_block_pair(l, nb)
+                    ti = np.arange(I * tb, min((I + 1) * tb, n))
+                    sj = np.arange(J * tb, min((J + 1) * tb, n))
+                    part[I, J, : len(ti)] = f[np.ix_(ti, sj)].sum(axis=1)  # target side
+                    if I != J:
+                        # source side: sum over the targets of f[i, j], times the
+                        # body's source sign (f[j, i] = sign * f[i, j])
+                        part[J, I, : len(sj)] = sign * f[np.ix_(ti, sj)].sum(axis=0)
+                for i in range(n):
+                    K, r = divmod(i, tb)
+                    got = part[K, :, r].sum()
+                    assert abs(got - f[i].sum()) < 1e-9 * (1 + np.abs(f[i]).sum())
