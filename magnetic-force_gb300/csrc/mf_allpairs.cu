@@ -9,6 +9,8 @@
 #include <tuple>
 #include <type_traits>
 
+#include <atomic>
+#include <vector>
 #include "mf_internal.h"
 
 namespace mfgb {
@@ -38,11 +40,62 @@ mf_status cuda_fail(cudaError_t e, const char* what) {
 // ---------------------------------------------------------------------------
 // DevBuf / Scratch
 // ---------------------------------------------------------------------------
+namespace {
+std::mutex g_free_mu;
+std::vector<std::pair<void*, size_t>> g_dev_graveyard;
+std::vector<void*> g_host_graveyard;
+std::atomic<int> g_defer{0};
+std::atomic<size_t> g_deferred_bytes{0};
+}  // namespace
+
+void device_free(void* p, size_t bytes) {
+  if (!p) return;
+  if (g_defer.load() > 0) {
+    std::lock_guard<std::mutex> lk(g_free_mu);
+    g_dev_graveyard.emplace_back(p, bytes);
+    g_deferred_bytes += bytes;
+    return;
+  }
+  cudaFree(p);
+}
+
+void pinned_free(void* p) {
+  if (!p) return;
+  if (g_defer.load() > 0) {
+    std::lock_guard<std::mutex> lk(g_free_mu);
+    g_host_graveyard.push_back(p);
+    return;
+  }
+  cudaFreeHost(p);
+}
+
+void defer_frees(bool on) { g_defer += on ? 1 : -1; }
+size_t deferred_bytes() { return g_deferred_bytes.load(); }
+
+void flush_deferred_frees() {
+  std::vector<std::pair<void*, size_t>> dev;
+  std::vector<void*> host;
+  {
+    std::lock_guard<std::mutex> lk(g_free_mu);
+    dev.swap(g_dev_graveyard);
+    host.swap(g_host_graveyard);
+    g_deferred_bytes = 0;
+  }
+  for (auto& d : dev) cudaFree(d.first);
+  for (void* h : host) cudaFreeHost(h);
+}
+
 mf_status DevBuf::reserve(size_t want, bool keep, bool zero) {
   if (want == 0) want = 16;
   if (want <= bytes) return MF_OK;
   void* p = nullptr;
-  MF_CUDA_TRY(cudaMalloc(&p, want));
+  cudaError_t ea = cudaMalloc(&p, want);
+  if (ea == cudaErrorMemoryAllocation && deferred_bytes() > 0) {
+    cudaGetLastError();  // clear the allocation error, then retry with the parked frees done
+    flush_deferred_frees();
+    ea = cudaMalloc(&p, want);
+  }
+  if (ea != cudaSuccess) return cuda_fail(ea, "cudaMalloc");
   size_t kept = 0;
   if (keep && ptr && bytes) {
     cudaError_t e = cudaMemcpy(p, ptr, bytes, cudaMemcpyDeviceToDevice);

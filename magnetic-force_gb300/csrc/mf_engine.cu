@@ -189,7 +189,7 @@ class Engine final : public EngineBase {
  public:
   ~Engine() override {
     reset_stats();
-    if (pinned_) cudaFreeHost(pinned_);
+    if (pinned_) pinned_free(pinned_);
   }
 
   mf_status init(const mf_params& p) override {

@@ -1094,7 +1094,7 @@ const FmmStats& Fmm::stats() {
 }
 
 Fmm::~Fmm() {
-  if (hstat_) cudaFreeHost(hstat_);
+  if (hstat_) pinned_free(hstat_);
   if (stat_ev_) cudaEventDestroy(stat_ev_);
 }
 

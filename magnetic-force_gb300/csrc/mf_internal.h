@@ -34,6 +34,17 @@ mf_status cuda_fail(cudaError_t e, const char* what);
 // ---------------------------------------------------------------------------
 // Device buffer (owning, growable)
 // ---------------------------------------------------------------------------
+// Device and pinned-host frees.  cudaFree and cudaFreeHost wait for every
+// stream of the device.  While deferral is on (a serving loop whose FMM
+// requests keep other streams busy for tens of milliseconds at a time), frees
+// are parked and done by flush_deferred_frees() at a point where that wait is
+// short; a failed device allocation flushes them and retries.  Nests.
+void device_free(void* p, size_t bytes);
+void pinned_free(void* p);
+void defer_frees(bool on);
+size_t deferred_bytes();
+void flush_deferred_frees();
+
 struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
@@ -56,7 +67,7 @@ struct DevBuf {
   }
   ~DevBuf() { release(); }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) device_free(ptr, bytes);
     ptr = nullptr;
     bytes = 0;
   }
