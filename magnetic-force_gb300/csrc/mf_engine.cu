@@ -973,6 +973,10 @@ class Engine final : public EngineBase {
       // (gather .. L2L) and its near-field kernel, each on its own events.
       TimedLaunch t, tf, tn;
       cudaEvent_t marks[4] = {nullptr, nullptr, nullptr, nullptr};
+      // The force's near field once per unordered box pair only when asked
+      // for (MF_OPT_PAIR_SYMMETRIC 2): at N = 1,048,576 it measured 20.6 ms
+      // against 20.2 ms for every ordered pair.
+      const bool sym_near = force && sym_mode_ == 2;
       if (timing_) {
         t.body = force ? MF_K_FORCE : MF_K_FIELD;
         t.pairs = t.evals = plan.pairs;
@@ -980,6 +984,7 @@ class Engine final : public EngineBase {
         tf.pairs = tf.evals = fmm_.stats().m2l_per_product;
         tn.body = force ? MF_K_FMM_NEAR_FORCE : MF_K_FMM_NEAR_FIELD;
         tn.pairs = tn.evals = fmm_.stats().p2p_pairs;
+        if (sym_near) tn.evals = fmm_.sym_near_evals();
         for (TimedLaunch* x : {&t, &tf, &tn}) {
           MF_CUDA_TRY(cudaEventCreate(&x->start));
           MF_CUDA_TRY(cudaEventCreate(&x->stop));
@@ -990,7 +995,8 @@ class Engine final : public EngineBase {
         marks[2] = tn.start;
         marks[3] = tn.stop;
       }
-      MF_TRY(fmm_.product(force ? 1 : 0, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr));
+      MF_TRY(fmm_.product(force ? 1 : 0, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr,
+                          sym_near));
       if (timing_) {
         MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
         timed_.push_back(t);

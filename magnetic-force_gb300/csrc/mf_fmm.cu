@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "mf_internal.h"
+#include "mf_sym.cuh"
 
 namespace mfgb {
 namespace {
@@ -176,6 +177,7 @@ __global__ void k_fmm_p2p_stats(FmmLevel lv, const int32_t* __restrict__ cnt, co
     atomicAdd(&out[0], s * unsigned(n));
     atomicMax(&out[1], (unsigned long long)n);
     atomicAdd(&out[3], 1ull);
+    atomicAdd(&out[4], (unsigned long long)cnt[c] * unsigned(n));
   }
 }
 
@@ -521,13 +523,29 @@ struct P2PArgs {
   const int4* rows;   // (half-width w, dy, dz, 0)
   int32_t n_rows;
   const double* done;
+  // Near field from partial sums (k_fmm_near_sym): the half-stencil rows,
+  // the planes [1 + offsets][3][n_slots] and their slot count.
+  const int4* hrows;
+  int32_t n_hrows;
+  const float* part;
+  int64_t n_slots;
 };
+
+// Plane of box offset dx in half row hr (1 + offsets before the row + index).
+__device__ __forceinline__ int near_plane(const int4& hr, int dx) {
+  return 1 + hr.w + ((hr.y == 0 && hr.z == 0) ? dx - 1 : dx + hr.x);
+}
 
 // kKind: 0 field (H), 1 Kelvin force (contracted with the target dipole),
 // 2 force tensor (the Hessian kernel's 3x3 at each target).
-template <int Q, int kKind>
+// kParts (force, targets = sources): the near field is not swept here but
+// added from k_fmm_near_sym's partial sums -- the box's own plane, then the
+// plane of every writer box (this box minus a half-stencil offset, inside the
+// grid and not empty), in a fixed order with compensated FP32.
+template <int Q, int kKind, bool kParts = false>
 __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const AllPairsArgs<float> a,
                                                          const SceneDesc<float> sc) {
+  static_assert(!kParts || kKind == 1, "partial sums: the Kelvin force only");
   using Body = std::conditional_t<kKind == 0, FieldF2Body, std::conditional_t<kKind == 1, ForceF2Body, TensorF2Body>>;
   constexpr bool kForce = kKind == 1;
   constexpr int kOut = Body::kOut;
@@ -605,11 +623,31 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
     float run[kOut], cmp[kOut];
 #pragma unroll
     for (int q = 0; q < kOut; ++q) run[q] = cmp[q] = 0.f;
+    if constexpr (kParts) {
+      if (act) {
+        const int64_t slot = int64_t(st0) + t0 + tid;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) two_sum_acc(run[q], cmp[q], __ldcg(p.part + int64_t(q) * p.n_slots + slot));
+        for (int r = 0; r < p.n_hrows; ++r) {
+          const int4 hr = p.hrows[r];
+          const int ay = iy - hr.y, az = iz - hr.z;
+          if (ay < 0 || ay >= lv.ny || az < 0 || az >= lv.nz) continue;
+          for (int dx = (hr.y == 0 && hr.z == 0) ? 1 : -hr.x; dx <= hr.x; ++dx) {
+            const int ax = ix - dx;
+            if (ax < 0 || ax >= lv.nx) continue;
+            if (p.cnt[(int64_t(az) * lv.ny + ay) * lv.nx + ax] == 0) continue;
+            const float* pl = p.part + int64_t(near_plane(hr, dx)) * 3 * p.n_slots + slot;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) two_sum_acc(run[q], cmp[q], __ldcg(pl + int64_t(q) * p.n_slots));
+          }
+        }
+      }
+    }
     if (tid == 0) {
       s_row = 0;
       s_pos = -1;
     }
-    for (;;) {
+    for (; !kParts;) {
       __syncthreads();  // the previous segment's steps are consumed
       if (tid == 0) fill();
       __syncthreads();
@@ -729,6 +767,146 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
       if (!mbar_wait_bounded(&bar[uu % kP2PStages], (uu / kP2PStages) & 1u)) drained = false;
     }
     if (!drained) atomicExch(a.err, MF_DEVERR_DRAIN_TIMEOUT);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Near field of the Kelvin force once per unordered box pair (targets are the
+// sources): one warp per leaf box A, up to 4 targets per lane (rounds of 128
+// for larger boxes).
+//   * A's own pairs: every ordered pair, target side only.
+//   * The boxes B of the half stencil: each pair item's force adds into the
+//     targets' sums and, reduced over the warp by a fixed shuffle tree, into
+//     the sources' sums (f_ji = -f_ij), stored at plane near_plane(B - A) of
+//     the source's slot.  A later target round adds to the entries of the
+//     earlier ones (the same lane, in order).
+//   * The targets' sums go to plane 0.
+// Every (plane, slot) entry has one writer, so results do not depend on
+// scheduling.  Sums are in the all-pairs kernels' units (times K).
+// ---------------------------------------------------------------------------
+struct NearSymArgs {
+  FmmLevel lv;
+  const int32_t* start;  // box slot starts (even-padded), leaf level
+  const int32_t* cnt;
+  const int32_t* perm;   // slot -> particle
+  const float4* pos2s;   // pair-layout records by slot
+  const float4* mom2s;
+  const int4* hrows;
+  int32_t n_hrows;
+  float* part;
+  int64_t n_slots;
+  const double* done;
+};
+constexpr int kNearSymWarps = 4, kNearSymTPT = 4;
+
+__global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
+                                                                     const SceneDesc<float> sc) {
+  constexpr int TPT = kNearSymTPT;
+  if (p.done && *p.done != 0.0) return;
+  const FmmLevel& lv = p.lv;
+  const int lane = threadIdx.x & 31;
+  const int64_t c = int64_t(blockIdx.x) * kNearSymWarps + (threadIdx.x >> 5);
+  if (c >= lv.nbox) return;  // warp-uniform; the kernel has no block barrier
+  const int32_t n = p.cnt[c];
+  if (n == 0) return;
+  const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
+  const int32_t st0 = p.start[c];
+  const float near2 = sc.pc.near2_force;
+  const float kk = float(kForceK);
+  const PairItems::Item zero_item{{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (int t0 = 0; t0 < n; t0 += 32 * TPT) {
+    float2 tx[TPT], ty[TPT], tz[TPT], tmx[TPT], tmy[TPT], tmz[TPT];
+    float2 acc[TPT][3];
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+      const int li = t0 + t * 32 + lane;
+      const bool live = li < n;
+      const int32_t i = p.perm[st0 + (live ? li : 0)];
+      const float4 q = a.tpos[i];
+      const float4 w = live ? a.tmom[i] : make_float4(0.f, 0.f, 0.f, 0.f);  // a dead slot adds nothing to sources
+      tx[t] = f2_dup(q.x);
+      ty[t] = f2_dup(q.y);
+      tz[t] = f2_dup(q.z);
+      tmx[t] = f2_dup(w.x);
+      tmy[t] = f2_dup(w.y);
+      tmz[t] = f2_dup(w.z);
+      acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
+    }
+    {  // the box's own pairs, target side only
+      const float4* sp = p.pos2s + st0;
+      const float4* sm = p.mom2s + st0;
+      const int ni = (n + 1) >> 1;
+      for (int j = 0; j < ni; ++j) {
+        const PairItems::Item it = PairItems::load_item(sp, sm, j);
+        float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
+      }
+    }
+    for (int r = 0; r < p.n_hrows; ++r) {
+      const int4 hr = p.hrows[r];
+      const int cy = iy + hr.y, cz = iz + hr.z;
+      if (cy < 0 || cy >= lv.ny || cz < 0 || cz >= lv.nz) continue;
+      for (int dx = (hr.y == 0 && hr.z == 0) ? 1 : -hr.x; dx <= hr.x; ++dx) {
+        const int cx = ix + dx;
+        if (cx < 0 || cx >= lv.nx) continue;
+        const int64_t b = (int64_t(cz) * lv.ny + cy) * lv.nx + cx;
+        const int32_t nb = p.cnt[b];
+        if (nb == 0) continue;
+        const int32_t sb = p.start[b];
+        const float4* sp = p.pos2s + sb;
+        const float4* sm = p.mom2s + sb;
+        float* plane = p.part + int64_t(near_plane(hr, dx)) * 3 * p.n_slots;
+        const int ni = (nb + 1) >> 1;
+        // The next item pair is loaded while the current one is computed
+        // (the records come from L2; two warps per scheduler do not hide that
+        // wait).  Past the box's last item: a zero dipole at the origin,
+        // nothing on either side.
+        PairItems::Item nxt[2];
+        nxt[0] = PairItems::load_item(sp, sm, 0);
+        nxt[1] = 1 < ni ? PairItems::load_item(sp, sm, 1) : zero_item;
+        for (int j0 = 0; j0 < ni; j0 += 2) {
+          const PairItems::Item cur[2] = {nxt[0], nxt[1]};
+          nxt[0] = j0 + 2 < ni ? PairItems::load_item(sp, sm, j0 + 2) : zero_item;
+          nxt[1] = j0 + 3 < ni ? PairItems::load_item(sp, sm, j0 + 3) : zero_item;
+          float v[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) v[q] = 0.f;
+#pragma unroll
+          for (int q2 = 0; q2 < 2; ++q2) {
+            const PairItems::Item& it = cur[q2];
+            float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+            for (int t = 0; t < TPT; ++t)
+              sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              v[q2 * 6 + 2 * k] = src[k].x;
+              v[q2 * 6 + 2 * k + 1] = src[k].y;
+            }
+          }
+          const float w = warp_reduce_scatter<16>(v, lane);
+          const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
+          if ((lane & 1) == 0 && kv < 12) {
+            const int j = j0 + kv / 6, rem = kv % 6;
+            if (j < ni) {
+              float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(sb) + 2 * j + (rem & 1));
+              const float val = -w * kk;  // f_ji = -f_ij
+              if (t0 == 0) *dst = val;
+              else *dst += val;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+      const int li = t0 + t * 32 + lane;
+      if (li < n) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) p.part[int64_t(k) * p.n_slots + st0 + li] = (acc[t][k].x + acc[t][k].y) * kk;
+      }
+    }
   }
 }
 
@@ -990,6 +1168,22 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
       }
   }
   n_rows_ = int(rows.size());
+  // Half stencil for the near field once per unordered box pair: rows with
+  // dz > 0, or dz = 0 and dy > 0 (x offsets -w..w), and the centre row (x
+  // offsets 1..w).  w of a half row holds the box offsets before it; its
+  // offsets dx take planes 1 + w_before + (dx + w) (centre: dx - 1).
+  std::vector<int4> hrows;
+  n_off_ = 0;
+  for (const int4& r : rows) {
+    if (r.z > 0 || (r.z == 0 && r.y > 0)) {
+      hrows.push_back(make_int4(r.x, r.y, r.z, n_off_));
+      n_off_ += 2 * r.x + 1;
+    } else if (r.y == 0 && r.z == 0 && r.x > 0) {
+      hrows.push_back(make_int4(r.x, 0, 0, n_off_));
+      n_off_ += r.x;
+    }
+  }
+  n_hrows_ = int(hrows.size());
   // Interaction lists, rows and the derivative table are uploaded only when
   // they changed (positions that move a little keep the same grid shape).
   // Uploads go through pinned staging that stays alive until the next build.
@@ -1024,16 +1218,21 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
     MF_CUDA_TRY(cudaStreamSynchronize(st));
     host_list_ = std::move(list);
     host_rows_ = std::move(rows);
+    host_hrows_ = std::move(hrows);
     host_lofs_ = list_off_;
     host_lofs_.insert(host_lofs_.end(), list_cnt_.begin(), list_cnt_.end());
     MF_TRY(lists_.reserve_slack(std::max<size_t>(1, host_list_.size()) * sizeof(int4)));
     MF_TRY(rows_.reserve_slack(std::max<size_t>(1, host_rows_.size()) * sizeof(int4)));
+    MF_TRY(hrows_.reserve_slack(std::max<size_t>(1, host_hrows_.size()) * sizeof(int4)));
     MF_TRY(lofs_.reserve_slack(host_lofs_.size() * sizeof(int64_t)));
     if (!host_list_.empty())
       MF_CUDA_TRY(cudaMemcpyAsync(lists_.ptr, host_list_.data(), host_list_.size() * sizeof(int4),
                                   cudaMemcpyHostToDevice, st));
     if (!host_rows_.empty())
       MF_CUDA_TRY(cudaMemcpyAsync(rows_.ptr, host_rows_.data(), host_rows_.size() * sizeof(int4),
+                                  cudaMemcpyHostToDevice, st));
+    if (!host_hrows_.empty())
+      MF_CUDA_TRY(cudaMemcpyAsync(hrows_.ptr, host_hrows_.data(), host_hrows_.size() * sizeof(int4),
                                   cudaMemcpyHostToDevice, st));
     MF_CUDA_TRY(cudaMemcpyAsync(lofs_.ptr, host_lofs_.data(), host_lofs_.size() * sizeof(int64_t),
                                 cudaMemcpyHostToDevice, st));
@@ -1058,8 +1257,8 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
   MF_TRY(lpart_.reserve_slack(size_t(lpart) * sizeof(float)));
 
   // Statistics, counted on the device and read back lazily (stats()).
-  MF_TRY(stat_.reserve(4 * sizeof(unsigned long long)));
-  MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 4 * sizeof(unsigned long long), st));
+  MF_TRY(stat_.reserve(5 * sizeof(unsigned long long)));
+  MF_CUDA_TRY(cudaMemsetAsync(stat_.ptr, 0, 5 * sizeof(unsigned long long), st));
   const int32_t* tocc_all = separate_ ? tocc_.as<int32_t>() : occ;
   k_fmm_p2p_stats<<<blocks_for(ncell), 256, 0, st>>>(leaf, cnt, tocc_all + leaf.box_off, rows_.as<int4>(), n_rows_,
                                                       stat_.as<unsigned long long>());
@@ -1068,9 +1267,9 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
         lv_[size_t(l)], occ, tocc_all, lists_.as<int4>(), lofs_.as<int64_t>() + 8 * l,
         lofs_.as<int64_t>() + list_off_.size() + 8 * l, stat_.as<unsigned long long>());
   MF_CUDA_TRY(cudaGetLastError());
-  if (!hstat_) MF_CUDA_TRY(cudaMallocHost(&hstat_, 4 * sizeof(unsigned long long)));
+  if (!hstat_) MF_CUDA_TRY(cudaMallocHost(&hstat_, 5 * sizeof(unsigned long long)));
   if (!stat_ev_) MF_CUDA_TRY(cudaEventCreateWithFlags(&stat_ev_, cudaEventDisableTiming));
-  MF_CUDA_TRY(cudaMemcpyAsync(hstat_, stat_.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  MF_CUDA_TRY(cudaMemcpyAsync(hstat_, stat_.ptr, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   MF_CUDA_TRY(cudaEventRecord(stat_ev_, st));
   stat_pending_ = true;
   stats_ = FmmStats{};
@@ -1088,6 +1287,7 @@ const FmmStats& Fmm::stats() {
     stats_.max_leaf = int32_t(hstat_[1]);
     stats_.m2l_per_product = double(hstat_[2]);
     stats_.occupied_leaves = int64_t(hstat_[3]);
+    stats_.p2p_self_pairs = double(hstat_[4]);
     stat_pending_ = false;
   }
   return stats_;
@@ -1099,14 +1299,15 @@ Fmm::~Fmm() {
 }
 
 mf_status Fmm::product(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                       const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
+                       const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks,
+                       bool sym_near) {
   if (kind < 0 || kind > 2) return fail(MF_ERR_INVALID_ARG, "fmm: unknown product kind");
   switch (degree_) {
-    case 3: return product_q<3>(kind, pos4, smom, a, sc, st, done, marks);
-    case 4: return product_q<4>(kind, pos4, smom, a, sc, st, done, marks);
-    case 5: return product_q<5>(kind, pos4, smom, a, sc, st, done, marks);
-    case 6: return product_q<6>(kind, pos4, smom, a, sc, st, done, marks);
-    case 7: return product_q<7>(kind, pos4, smom, a, sc, st, done, marks);
+    case 3: return product_q<3>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 4: return product_q<4>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 5: return product_q<5>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 6: return product_q<6>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 7: return product_q<7>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
   }
 }
@@ -1155,7 +1356,8 @@ struct M2LVariants<7> {
 
 template <int Q>
 mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                         const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks) {
+                         const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks,
+                         bool sym_near) {
   constexpr int NC = ncoef(Q) - 1;
   const int L = int(lv_.size()) - 1;
   const FmmLevel& leaf = lv_[size_t(L)];
@@ -1218,12 +1420,36 @@ mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const
   pp.rows = rows_.as<int4>();
   pp.n_rows = n_rows_;
   pp.done = done;
+  const bool sym = kind == 1 && sym_near && !separate_;
+  if (sym) {
+    MF_TRY(npart_.reserve_grow(size_t(1 + n_off_) * 3 * size_t(n_slots_) * sizeof(float)));
+    pp.hrows = hrows_.as<int4>();
+    pp.n_hrows = n_hrows_;
+    pp.part = npart_.as<float>();
+    pp.n_slots = n_slots_;
+  }
   if (leaf.nbox > int64_t(0x7fffffff)) return fail(MF_ERR_INVALID_ARG, "fmm: too many leaf boxes");
   if (marks) {
     MF_CUDA_TRY(cudaEventRecord(marks[1], st));
     MF_CUDA_TRY(cudaEventRecord(marks[2], st));
   }
-  if (kind == 1)
+  if (sym) {
+    NearSymArgs ns{};
+    ns.lv = leaf;
+    ns.start = pp.start;
+    ns.cnt = cnt;
+    ns.perm = pp.perm;
+    ns.pos2s = pp.pos2s;
+    ns.mom2s = pp.mom2s;
+    ns.hrows = pp.hrows;
+    ns.n_hrows = n_hrows_;
+    ns.part = npart_.as<float>();
+    ns.n_slots = n_slots_;
+    ns.done = done;
+    k_fmm_near_sym<<<unsigned((leaf.nbox + kNearSymWarps - 1) / kNearSymWarps), 32 * kNearSymWarps, 0, st>>>(ns, a, sc);
+    ++nl;
+    k_fmm_p2p<Q, 1, true><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+  } else if (kind == 1)
     k_fmm_p2p<Q, 1><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
   else if (kind == 2)
     k_fmm_p2p<Q, 2><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);

@@ -390,6 +390,7 @@ struct FmmStats {
   int32_t levels = 0, leaf_level = 0, degree = 0, pad = 0;
   int64_t leaf_boxes = 0, occupied_leaves = 0;
   double p2p_pairs = 0;   // executed near-field pairs per product (real sources)
+  double p2p_self_pairs = 0;  // of those, pairs within one leaf box (sum of n^2)
   double m2l_per_product = 0;
   int32_t max_leaf = 0, near_rows = 0;
 };
@@ -413,9 +414,14 @@ class Fmm {
   // stages (gather .. L2L), then before and after the near-field kernel.
   // kind: 0 field, 1 Kelvin force, 2 force tensor (6 entries through the
   // tensor epilogue; a.corr4 then holds two records per target).
+  // sym_near (Kelvin force, targets = sources): the near field once per
+  // unordered box pair (k_fmm_near_sym, partial sums per source and writer
+  // box offset, ~1 KB per particle), read back by the near-field kernel.
   mf_status product(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
                     const SceneDesc<float>& sc, cudaStream_t st, const double* done,
-                    cudaEvent_t* marks = nullptr);
+                    cudaEvent_t* marks = nullptr, bool sym_near = false);
+  // Near-field pair evaluations of one force product with sym_near.
+  double sym_near_evals() { return 0.5 * (stats().p2p_pairs + stats().p2p_self_pairs); }
   // Shape and work of the last build (waits for its device counts).
   const FmmStats& stats();
   int launches_per_product() const { return launches_; }
@@ -427,7 +433,8 @@ class Fmm {
  private:
   template <int Q>
   mf_status product_q(int kind, const float4* pos4, const float4* smom, const AllPairsArgs<float>& a,
-                      const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks);
+                      const SceneDesc<float>& sc, cudaStream_t st, const double* done, cudaEvent_t* marks,
+                      bool sym_near);
   FmmConfig cfg_;
   FmmStats stats_;
   int degree_ = 5;
@@ -436,16 +443,18 @@ class Fmm {
   std::vector<int64_t> list_off_, list_cnt_;  // per (level, class)
   std::vector<int32_t> chunks_;               // M2L splits per level
   int n_rows_ = 0;
+  int n_hrows_ = 0, n_off_ = 0;  // half-stencil rows and their box offsets (sym_near)
   int launches_ = 0;
   DevBuf cell_of_, cnt_, start_, cursor_, perm_tmp_, perm_, pos2s_, mom2s_;
   DevBuf occ_, mcoef_, lcoef_, lpart_, lists_, rows_, dtab_, stat_, lofs_;
+  DevBuf hrows_, npart_;  // half-stencil rows; near-field partial sums (sym_near)
   // Separate targets: occupancy per level and leaf binning.
   DevBuf tocc_, tcell_of_, tstart_, tcursor_, tperm_tmp_, tperm_;
   bool separate_ = false;
   int64_t nt_ = 0;
-  std::vector<int4> host_list_, host_rows_;  // as last uploaded
+  std::vector<int4> host_list_, host_rows_, host_hrows_;  // as last uploaded
   std::vector<int32_t> host_dkey_;           // degree and offsets of the uploaded derivative table
-  unsigned long long* hstat_ = nullptr;      // pinned: near pairs, largest leaf, M2L count, occupied leaves
+  unsigned long long* hstat_ = nullptr;      // pinned: near pairs, largest leaf, M2L count, occupied leaves, in-box pairs
   cudaEvent_t stat_ev_ = nullptr;
   bool stat_pending_ = false;
   std::vector<float> host_dt_;

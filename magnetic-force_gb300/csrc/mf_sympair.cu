@@ -30,6 +30,7 @@
 #include <mutex>
 
 #include "mf_internal.h"
+#include "mf_sym.cuh"
 
 namespace mfgb {
 namespace {
@@ -49,34 +50,6 @@ constexpr size_t kSymSmem = size_t(kSymStages) * 2 * kSymTB * sizeof(float4);
 // (The field body sets its own split and pair counts below.)
 constexpr int kSymSplit = 2, kSymPair = 2;
 
-// Reduce-scatter of NV values per lane over the warp (NV a power of two,
-// 8 .. 32): the value index halves at each level, lanes with bit b set keep
-// the upper half; after log2(NV) levels each lane holds one value summed over
-// the lanes that differ in the bits used, and the remaining levels finish the
-// sum.  Value k ends in the lanes lane / (32 / NV) == k.  Fixed order: the
-// result does not depend on scheduling.
-template <int NV>
-__device__ __forceinline__ float warp_reduce_scatter(const float (&v)[NV], int lane) {
-  static_assert(NV >= 2 && NV <= 32 && (NV & (NV - 1)) == 0, "NV");
-  float w[NV];
-#pragma unroll
-  for (int q = 0; q < NV; ++q) w[q] = v[q];
-  int b = 16;
-#pragma unroll
-  for (int n = NV; n > 1; n >>= 1, b >>= 1) {
-    const bool hi = lane & b;
-#pragma unroll
-    for (int q = 0; q < n / 2; ++q) {
-      const float send = hi ? w[q] : w[q + n / 2];
-      const float keep = hi ? w[q + n / 2] : w[q];
-      w[q] = keep + __shfl_xor_sync(0xffffffffu, send, b);
-    }
-  }
-#pragma unroll
-  for (; b >= 1; b >>= 1) w[0] += __shfl_xor_sync(0xffffffffu, w[0], b);
-  return w[0];
-}
-
 // Step l of a scene with nb blocks -> (I, J), row I holding nb - I steps.
 __device__ __forceinline__ void sym_block_pair(int64_t l, int nb, int& I, int& J) {
   // start(I) = I nb - I (I - 1) / 2; solve for the largest I with start(I) <= l.
@@ -89,27 +62,6 @@ __device__ __forceinline__ void sym_block_pair(int64_t l, int nb, int& I, int& J
   while (i < nb - 1 && start(i + 1) <= l) ++i;
   I = i;
   J = i + int(l - start(i));
-}
-
-// f_ij for two sources (packed) and one target: the clamped far form of the
-// Kelvin force, in units of K.
-__device__ __forceinline__ void force_pair2_full(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy,
-                                                 float2 tmz, const PairItems::Item& it, float near2, float2* f) {
-  const float2 dx = f2_sub(tx, it.x), dy = f2_sub(ty, it.y), dz = f2_sub(tz, it.z);
-  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-  const float2 ri = clamp_rsqrt2(r2, near2);
-  const float2 ri2 = f2_mul(ri, ri);
-  const float2 ri5 = f2_mul(f2_mul(ri2, ri2), ri);
-  const float2 ds = f2_fma(dz, it.mz, f2_fma(dy, it.my, f2_mul(dx, it.mx)));
-  const float2 dm = f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx)));
-  const float2 sm = f2_fma(it.mz, tmz, f2_fma(it.my, tmy, f2_mul(it.mx, tmx)));
-  const float2 u = f2_mul(ds, ri5);
-  const float2 v = f2_mul(dm, ri5);
-  const float2 e = f2_mul(f2_mul(ri2, ds), f2_dup(-5.f));
-  const float2 w = f2_fma(e, v, f2_mul(sm, ri5));
-  f[0] = f2_fma(dx, w, f2_fma(tmx, u, f2_mul(it.mx, v)));
-  f[1] = f2_fma(dy, w, f2_fma(tmy, u, f2_mul(it.my, v)));
-  f[2] = f2_fma(dz, w, f2_fma(tmz, u, f2_mul(it.mz, v)));
 }
 
 // What one pair item adds on both sides, and the scaling of the sums.
@@ -128,13 +80,7 @@ struct SymBody<true> {
   __device__ static float scale() { return float(kForceK); }
   __device__ static void pair(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
                               const PairItems::Item& it, float near2, float2* acc, float2* src) {
-    float2 f[3];
-    force_pair2_full(tx, ty, tz, tmx, tmy, tmz, it, near2, f);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      acc[c] = f2_add(acc[c], f[c]);
-      src[c] = f2_add(src[c], f[c]);
-    }
+    sym_force_pair2(tx, ty, tz, tmx, tmy, tmz, it, near2, acc, src);
   }
 };
 
@@ -151,20 +97,7 @@ struct SymBody<false> {
   __device__ static float scale() { return -float(kInv4Pi); }
   __device__ static void pair(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy, float2 tmz,
                               const PairItems::Item& it, float near2, float2* acc, float2* src) {
-    const float2 dx = f2_sub(tx, it.x), dy = f2_sub(ty, it.y), dz = f2_sub(tz, it.z);
-    const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
-    const float2 ri = clamp_rsqrt2(r2, near2);
-    const float2 ri2 = f2_mul(ri, ri);
-    const float2 beta = f2_mul(ri2, ri);
-    const float2 a3 = f2_mul(beta, f2_mul(ri2, f2_dup(-3.f)));
-    const float2 ts = f2_mul(f2_fma(dz, it.mz, f2_fma(dy, it.my, f2_mul(dx, it.mx))), a3);
-    const float2 tt = f2_mul(f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx))), a3);
-    acc[0] = f2_fma(it.mx, beta, f2_fma(dx, ts, acc[0]));
-    acc[1] = f2_fma(it.my, beta, f2_fma(dy, ts, acc[1]));
-    acc[2] = f2_fma(it.mz, beta, f2_fma(dz, ts, acc[2]));
-    src[0] = f2_fma(tmx, beta, f2_fma(dx, tt, src[0]));
-    src[1] = f2_fma(tmy, beta, f2_fma(dy, tt, src[1]));
-    src[2] = f2_fma(tmz, beta, f2_fma(dz, tt, src[2]));
+    sym_field_pair2(tx, ty, tz, tmx, tmy, tmz, it, near2, acc, src);
   }
 };
 
@@ -362,17 +295,6 @@ __global__ void __launch_bounds__(kSymTPB) k_sym(const AllPairsArgs<float> a, fl
     }
     __syncthreads();
   }
-}
-
-// s + x with the rounding error of the add carried in e: Knuth's TwoSum
-// (The Art of Computer Programming, vol. 2, 4.2.2), exact in round-to-
-// nearest without any ordering of |s| and |x|.
-__device__ __forceinline__ void two_sum_acc(float& s, float& e, float x) {
-  const float t = __fadd_rn(s, x);
-  const float xp = __fsub_rn(t, s);
-  const float sp = __fsub_rn(t, xp);
-  e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, sp), __fsub_rn(x, xp)));
-  s = t;
 }
 
 // Per particle: the nb partner-block sums of its block, compensated FP32

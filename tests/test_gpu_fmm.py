@@ -260,3 +260,31 @@ def test_many_external_dipoles_through_fmm(mf):
     assert 0.0 < e < 1e-5
     assert rel(g1, g2) < 3e-4
     assert rel(b1, b2) < 1e-5
+
+
+@pytest.mark.parametrize("leaf", [8, 200])
+def test_force_near_field_once_per_box_pair(mf, sphere40k, leaf):
+    # The FMM's near field of the force once per unordered box pair
+    # (MF_OPT_PAIR_SYMMETRIC 2) against every ordered pair (0, and 1, the
+    # default, for the FMM): the magnetization and the far field are the
+    # same, the near sums differ in FP32 order only.  leaf 200 makes boxes of
+    # more than 128 particles (more than one target round per warp).
+    sc = sphere40k
+    out = {}
+    for mode in (2, 0):
+        s = solver(mf, sc, fmm=mf.FMM_ON, fmm_order=8, fmm_leaf=leaf, solver=mf.SOLVER_CG)
+        s.set_option("pair_symmetric", mode)
+        it, rr = s.solve(300)
+        assert rr < 1e-6
+        s.set_option("kernel_timing", 1)
+        s.reset_counters()
+        s.evaluate_fitted_near_foece()
+        out[mode] = (np.asarray(s.magnetic_bodyforce, np.float64), s.kernel_stats("fmm_near_force"),
+                     s.fmm_stats()["max_leaf"])
+        s.close()
+    sym, full = out[2][1], out[0][1]
+    assert full["evals"] == full["pairs"]
+    assert sym["pairs"] == full["pairs"] and 0.45 * sym["pairs"] < sym["evals"] < 0.6 * sym["pairs"]
+    if leaf == 200:
+        assert out[2][2] > 128
+    assert rel(out[2][0], out[0][0]) < 2e-6
