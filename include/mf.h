@@ -109,9 +109,9 @@ typedef enum mf_option {
                                each unordered pair evaluated once for both particles (a pair
                                kernel and a per-particle finish) instead of every ordered
                                pair: 0 never, 1 where tuning measured it faster (default;
-                               without tuning, the force only), 2 always (on the FMM path
-                               too: the force's near field once per unordered box pair).
-                               Not in the reference. */
+                               without tuning, the force only), 2 always.  On the FMM path,
+                               1 and 2 evaluate the force's near field once per unordered
+                               box pair.  Not in the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */

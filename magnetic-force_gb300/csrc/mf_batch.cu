@@ -639,7 +639,9 @@ class Server {
   // scratch.  FMM request: a solver handle's vectors, published arrays, cell
   // list and octree.
   static double need_bytes(int64_t n) {
-    if (n > kServeFmmMin) return double(n) * 720.0 + 64.0 * 1024 * 1024;
+    // FMM requests: the handle's state and tree, plus ~1.2 KB per particle of
+    // near-field partial sums (the force's near field once per box pair).
+    if (n > kServeFmmMin) return double(n) * (720.0 + 1200.0) + 64.0 * 1024 * 1024;
     return double(n) * 320.0 + 4.0 * 1024 * 1024;
   }
 

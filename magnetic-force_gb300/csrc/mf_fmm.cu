@@ -797,14 +797,18 @@ struct NearSymArgs {
   int64_t n_slots;
   const double* done;
 };
-constexpr int kNearSymWarps = 4, kNearSymTPT = 4;
+constexpr int kNearSymWarps = 4, kNearSymTPT = 4, kNearSymChunk = 64;
 
 __global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
                                                                      const SceneDesc<float> sc) {
-  constexpr int TPT = kNearSymTPT;
+  constexpr int TPT = kNearSymTPT, CH = kNearSymChunk;
+  // per warp: a chunk of a source box's pair items (positions, then dipoles)
+  __shared__ float4 s_pos[kNearSymWarps][2 * CH], s_mom[kNearSymWarps][2 * CH];
   if (p.done && *p.done != 0.0) return;
   const FmmLevel& lv = p.lv;
   const int lane = threadIdx.x & 31;
+  float4* const wpos = s_pos[threadIdx.x >> 5];
+  float4* const wmom = s_mom[threadIdx.x >> 5];
   const int64_t c = int64_t(blockIdx.x) * kNearSymWarps + (threadIdx.x >> 5);
   if (c >= lv.nbox) return;  // warp-uniform; the kernel has no block barrier
   const int32_t n = p.cnt[c];
@@ -858,42 +862,45 @@ __global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearS
         const float4* sm = p.mom2s + sb;
         float* plane = p.part + int64_t(near_plane(hr, dx)) * 3 * p.n_slots;
         const int ni = (nb + 1) >> 1;
-        // The next item pair is loaded while the current one is computed
-        // (the records come from L2; two warps per scheduler do not hide that
-        // wait).  Past the box's last item: a zero dipole at the origin,
-        // nothing on either side.
-        PairItems::Item nxt[2];
-        nxt[0] = PairItems::load_item(sp, sm, 0);
-        nxt[1] = 1 < ni ? PairItems::load_item(sp, sm, 1) : zero_item;
-        for (int j0 = 0; j0 < ni; j0 += 2) {
-          const PairItems::Item cur[2] = {nxt[0], nxt[1]};
-          nxt[0] = j0 + 2 < ni ? PairItems::load_item(sp, sm, j0 + 2) : zero_item;
-          nxt[1] = j0 + 3 < ni ? PairItems::load_item(sp, sm, j0 + 3) : zero_item;
-          float v[16];
-#pragma unroll
-          for (int q = 0; q < 16; ++q) v[q] = 0.f;
-#pragma unroll
-          for (int q2 = 0; q2 < 2; ++q2) {
-            const PairItems::Item& it = cur[q2];
-            float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-#pragma unroll
-            for (int t = 0; t < TPT; ++t)
-              sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              v[q2 * 6 + 2 * k] = src[k].x;
-              v[q2 * 6 + 2 * k + 1] = src[k].y;
-            }
+        // The box's items in chunks of CH, staged by the warp with coalesced
+        // loads and read back as broadcasts.  Past the box's last item: a zero
+        // dipole at the origin, nothing on either side.
+        for (int cs = 0; cs < ni; cs += CH) {
+          const int cn = min(CH, ni - cs);
+          __syncwarp();
+          for (int k = lane; k < 2 * cn; k += 32) {
+            wpos[k] = sp[2 * cs + k];
+            wmom[k] = sm[2 * cs + k];
           }
-          const float w = warp_reduce_scatter<16>(v, lane);
-          const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
-          if ((lane & 1) == 0 && kv < 12) {
-            const int j = j0 + kv / 6, rem = kv % 6;
-            if (j < ni) {
-              float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(sb) + 2 * j + (rem & 1));
-              const float val = -w * kk;  // f_ji = -f_ij
-              if (t0 == 0) *dst = val;
-              else *dst += val;
+          __syncwarp();
+          for (int j0 = 0; j0 < cn; j0 += 2) {
+            float v[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] = 0.f;
+#pragma unroll
+            for (int q2 = 0; q2 < 2; ++q2) {
+              const PairItems::Item it =
+                  (q2 == 0 || j0 + 1 < cn) ? PairItems::load_item(wpos, wmom, j0 + q2) : zero_item;
+              float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+              for (int t = 0; t < TPT; ++t)
+                sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
+#pragma unroll
+              for (int k = 0; k < 3; ++k) {
+                v[q2 * 6 + 2 * k] = src[k].x;
+                v[q2 * 6 + 2 * k + 1] = src[k].y;
+              }
+            }
+            const float w = warp_reduce_scatter<16>(v, lane);
+            const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
+            if ((lane & 1) == 0 && kv < 12) {
+              const int jl = j0 + kv / 6, rem = kv % 6;
+              if (jl < cn) {
+                float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(sb) + 2 * (cs + jl) + (rem & 1));
+                const float val = -w * kk;  // f_ji = -f_ij
+                if (t0 == 0) *dst = val;
+                else *dst += val;
+              }
             }
           }
         }
