@@ -109,9 +109,10 @@ typedef enum mf_option {
                                each unordered pair evaluated once for both particles (a pair
                                kernel and a per-particle finish) instead of every ordered
                                pair: 0 never, 1 where tuning measured it faster (default;
-                               without tuning, the force only), 2 always.  On the FMM path,
-                               1 and 2 evaluate the force's near field once per unordered
-                               box pair.  Not in the reference. */
+                               without tuning, the force only), 2 always.  On the FMM path
+                               the force's near field is evaluated once per unordered box
+                               pair with 2, and with 1 from 524,288 particles on.  Not in
+                               the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */

@@ -973,10 +973,10 @@ class Engine final : public EngineBase {
       // (gather .. L2L) and its near-field kernel, each on its own events.
       TimedLaunch t, tf, tn;
       cudaEvent_t marks[4] = {nullptr, nullptr, nullptr, nullptr};
-      // The force's near field once per unordered box pair unless pair
-      // symmetry is off (MF_OPT_PAIR_SYMMETRIC 0): at N = 1,048,576 it
-      // measured 18.7 ms against 20.2 ms for every ordered pair.
-      const bool sym_near = force && sym_mode_ != 0;
+      // The force's near field once per unordered box pair: always with
+      // MF_OPT_PAIR_SYMMETRIC 2, never with 0, and by default from
+      // kSymNearMin particles on.
+      const bool sym_near = force && (sym_mode_ == 2 || (sym_mode_ == 1 && np_ >= kSymNearMin));
       if (timing_) {
         t.body = force ? MF_K_FORCE : MF_K_FIELD;
         t.pairs = t.evals = plan.pairs;

@@ -119,6 +119,12 @@ constexpr int64_t kBatchPackedForceMin = 4096;
 // particles: force 0.82 against 1.04 ms; at 16,384 the all-pairs field wins
 // (0.206 against 0.213 ms).
 constexpr int64_t kSymDirectMin = 32768;
+// FMM handles: the force's near field once per unordered box pair from this
+// size on.  At 1,048,576 particles (P = 8) it measured 18.7 ms against 20.2 ms
+// for every ordered pair; with it on for the served stream's FMM requests
+// (75,000-225,000 particles, P = 6) the served capacity fell from 7.1 to 5.0
+// requests/s.
+constexpr int64_t kSymNearMin = 524288;
 
 template <class Real, Body B>
 struct KCfg;

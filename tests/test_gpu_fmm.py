@@ -264,8 +264,9 @@ def test_many_external_dipoles_through_fmm(mf):
 
 @pytest.mark.parametrize("leaf", [8, 200])
 def test_force_near_field_once_per_box_pair(mf, sphere40k, leaf):
-    # The FMM's near field of the force once per unordered box pair (the
-    # default; here MF_OPT_PAIR_SYMMETRIC 2) against every ordered pair (0):
+    # The FMM's near field of the force once per unordered box pair
+    # (MF_OPT_PAIR_SYMMETRIC 2; the default from 524,288 particles) against
+    # every ordered pair (0):
     # the magnetization and the far field are the same, the near sums differ
     # in FP32 order only.  leaf 200 makes boxes of more than 128 particles
     # (more than one target round per warp).
