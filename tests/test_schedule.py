@@ -8,7 +8,10 @@ pair is computed exactly once, that every partial the reducer reads was
 written by the CTA it expects, in the slot it expects, and that the ticket
 count equals the number of writers.  A second model covers the pair-symmetric
 launch (mf_sympair.cu): its step-to-block-pair map, that every block-sum slot
-is written once, and that the finish's row sums equal the direct sums.
+is written once, and that the finish's row sums equal the direct sums.  A
+third covers the FMM's near field once per box pair (mf_fmm.cu): the half
+stencil's plane indices, one writer per (plane, box), the read-back taking
+exactly what was written, and every unordered box pair covered once.
 """
 import itertools
 import random
@@ -218,3 +221,82 @@ def test_sym_sums_equal_the_direct_sums():
                     K, r = divmod(i, tb)
                     got = part[K, :, r].sum()
                     assert abs(got - f[i].sum()) < 1e-9 * (1 + np.abs(f[i]).sum())
+
+
+# ---------------------------------------------------------------------------
+# The FMM's near field of the force once per unordered box pair (mf_fmm.cu):
+# half-stencil rows from the near rows, plane indices, writers and readers.
+# ---------------------------------------------------------------------------
+def near_rows(R, radius):
+    """Rows (w, dy, dz) of a symmetric near stencil: |d| <= radius (box units)."""
+    rows = []
+    for dz in range(-R, R + 1):
+        for dy in range(-R, R + 1):
+            if dy * dy + dz * dz > radius * radius:
+                continue
+            w = 0
+            while w + 1 <= R and (w + 1) ** 2 + dy * dy + dz * dz <= radius * radius:
+                w += 1
+            rows.append((w, dy, dz))
+    return rows
+
+
+def half_rows(rows):
+    """As Fmm::build lays them out: (w, dy, dz, planes before the row)."""
+    out, n_off = [], 0
+    for w, dy, dz in rows:
+        if dz > 0 or (dz == 0 and dy > 0):
+            out.append((w, dy, dz, n_off))
+            n_off += 2 * w + 1
+        elif dy == 0 and dz == 0 and w > 0:
+            out.append((w, 0, 0, n_off))
+            n_off += w
+    return out, n_off
+
+
+def near_plane(hr, dx):
+    w, dy, dz, base = hr
+    return 1 + base + ((dx - 1) if (dy == 0 and dz == 0) else (dx + w))
+
+
+def test_fmm_half_stencil_planes():
+    rng = random.Random(17)
+    for trial in range(30):
+        R = rng.randint(1, 4)
+        radius = rng.uniform(0.9, R + 0.5)
+        rows = near_rows(R, radius)
+        hrows, n_off = half_rows(rows)
+        nx, ny, nz = rng.randint(1, 7), rng.randint(1, 7), rng.randint(1, 7)
+        occupied = {(x, y, z) for x in range(nx) for y in range(ny) for z in range(nz) if rng.random() < 0.7}
+        inside = lambda x, y, z: 0 <= x < nx and 0 <= y < ny and 0 <= z < nz  # noqa: E731
+        writes, pairs = {}, set()
+        for (ax, ay, az) in occupied:  # writer boxes (k_fmm_near_sym)
+            for hr in hrows:
+                w, dy, dz, _ = hr
+                for dx in range(1 if (dy == 0 and dz == 0) else -w, w + 1):
+                    b = (ax + dx, ay + dy, az + dz)
+                    if not inside(*b) or b not in occupied:
+                        continue
+                    o = near_plane(hr, dx)
+                    assert 1 <= o <= n_off
+                    assert (o, b) not in writes
+                    writes[(o, b)] = (ax, ay, az)
+                    pairs.add(frozenset([(ax, ay, az), b]))
+        reads = set()
+        for (bx, by, bz) in occupied:  # the read-back in k_fmm_p2p<Q, 1, true>
+            for hr in hrows:
+                w, dy, dz, _ = hr
+                for dx in range(1 if (dy == 0 and dz == 0) else -w, w + 1):
+                    a = (bx - dx, by - dy, bz - dz)
+                    if inside(*a) and a in occupied:
+                        reads.add((near_plane(hr, dx), (bx, by, bz)))
+        assert reads == set(writes)
+        # every unordered pair of distinct boxes in the full stencil, once
+        full = set()
+        for (ax, ay, az) in occupied:
+            for w, dy, dz in rows:
+                for dx in range(-w, w + 1):
+                    b = (ax + dx, ay + dy, az + dz)
+                    if b != (ax, ay, az) and inside(*b) and b in occupied:
+                        full.add(frozenset([(ax, ay, az), b]))
+        assert pairs == full
