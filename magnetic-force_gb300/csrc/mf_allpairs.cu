@@ -41,9 +41,17 @@ mf_status cuda_fail(cudaError_t e, const char* what) {
 // DevBuf / Scratch
 // ---------------------------------------------------------------------------
 namespace {
-std::mutex g_free_mu;
-std::vector<std::pair<void*, size_t>> g_dev_graveyard;
-std::vector<void*> g_host_graveyard;
+// Parked frees.  Never destroyed: device buffers owned by static objects of
+// other files may be released at process exit, after this file's statics.
+struct Parked {
+  std::mutex mu;
+  std::vector<std::pair<void*, size_t>> dev;
+  std::vector<void*> host;
+};
+Parked& parked() {
+  static Parked* p = new Parked();
+  return *p;
+}
 std::atomic<int> g_defer{0};
 std::atomic<size_t> g_deferred_bytes{0};
 }  // namespace
@@ -51,8 +59,9 @@ std::atomic<size_t> g_deferred_bytes{0};
 void device_free(void* p, size_t bytes) {
   if (!p) return;
   if (g_defer.load() > 0) {
-    std::lock_guard<std::mutex> lk(g_free_mu);
-    g_dev_graveyard.emplace_back(p, bytes);
+    Parked& k = parked();
+    std::lock_guard<std::mutex> lk(k.mu);
+    k.dev.emplace_back(p, bytes);
     g_deferred_bytes += bytes;
     return;
   }
@@ -62,8 +71,9 @@ void device_free(void* p, size_t bytes) {
 void pinned_free(void* p) {
   if (!p) return;
   if (g_defer.load() > 0) {
-    std::lock_guard<std::mutex> lk(g_free_mu);
-    g_host_graveyard.push_back(p);
+    Parked& k = parked();
+    std::lock_guard<std::mutex> lk(k.mu);
+    k.host.push_back(p);
     return;
   }
   cudaFreeHost(p);
@@ -76,9 +86,10 @@ void flush_deferred_frees() {
   std::vector<std::pair<void*, size_t>> dev;
   std::vector<void*> host;
   {
-    std::lock_guard<std::mutex> lk(g_free_mu);
-    dev.swap(g_dev_graveyard);
-    host.swap(g_host_graveyard);
+    Parked& k = parked();
+    std::lock_guard<std::mutex> lk(k.mu);
+    dev.swap(k.dev);
+    host.swap(k.host);
     g_deferred_bytes = 0;
   }
   for (auto& d : dev) cudaFree(d.first);
