@@ -14,9 +14,11 @@ Printed (rank 0, one JSON line):
   e2e        the same metric through the public API with host buffers: every
              step uploads positions from pinned memory, solves, evaluates the
              force, reads M, B/mu0 and F back and integrates on the host
-  roofline   FP32 FMA roofline of the dominant all-pairs kernel: algorithmic
-             FLOP (32 per field pair, 53 per force pair) / its event-timed
-             device time, against a dense-FFMA throughput measured in this run
+  roofline   FP32 FMA roofline of the dominant pair kernel: algorithmic FLOP
+             (32 per ordered field pair, 53 per ordered force pair; for a
+             product evaluated once per unordered pair, 49 / 55 per unordered
+             pair) / its event-timed device time, against a dense-FFMA
+             throughput measured in this run
   cpu_baseline  the CPU restatement of the reference's pair kernels (FP32,
              OpenMP over all host cores) on a bounded sample of the same step
 
@@ -281,7 +283,7 @@ def run_ours(args, rank, world, local):
     pairs_all = allreduce_sum(pairs, world)
     value = pairs_all / (t_max * 1e-3)
 
-    # dominant all-pairs kernel and its FP32 roofline
+    # dominant pair kernel and its FP32 roofline
     peak = mfgb.probe_fp32_peak()
     kern = {}
     names = {}
