@@ -62,6 +62,55 @@ def product_flop(name, st):
     if st.get("evals", st["pairs"]) < st["pairs"]:
         return (FLOP_FORCE_UPAIR if name == "force" else FLOP_FIELD_UPAIR) * st["evals"], f"k_sym<{name}>"
     return (FLOP_FIELD_PAIR if name == "field" else FLOP_FORCE_PAIR) * st["pairs"], f"allpairs_kernel<{name}>"
+
+# The FMA-pipe ceiling of each pair body: algorithmic FLOP per pipe cycle at a
+# fully busy FMA pipe, against the peak's 2 FLOP per cycle (packed f32x2
+# operations per target and pair item, counted from the bodies): the all-pairs
+# field 19 per 2 ordered pairs (64 FLOP), force 30 (106 FLOP); once per
+# unordered pair, field 30 per 2 unordered pairs (98 FLOP), force 39 (110 FLOP).
+BODY_BOUND = {"allpairs_kernel<field>": 64.0 / 76.0, "allpairs_kernel<force>": 106.0 / 120.0,
+              "k_sym<field>": 98.0 / 120.0, "k_sym<force>": 110.0 / 156.0}
+
+
+def pair_roofline(kf, kg, peak, n):
+    """Roofline of the dominant pair product of a timed run from the handle's
+    kernel statistics (field kf, force kg): per product its algorithmic
+    TFLOP/s, fraction of the measured FFMA peak and of its body's ceiling."""
+    kern = {}
+    names = {}
+    for name, st in (("field", kf), ("force", kg)):
+        if st["launches"]:
+            flop, names[name] = product_flop(name, st)
+            tflops = flop / (st["total_ms"] * 1e-3) / 1e12
+            bound = BODY_BOUND.get(names[name])
+            kern[name] = {"kernel": names[name], "launches": st["launches"], "total_ms": round(st["total_ms"], 4),
+                          "avg_ms": round(st["total_ms"] / st["launches"], 4),
+                          "pairs_per_launch": st["pairs"] / st["launches"],
+                          "evals_per_launch": st["evals"] / st["launches"],
+                          "flop_per_launch": flop / st["launches"],
+                          "tflops": tflops, "frac": tflops / peak,
+                          "body_bound": round(bound, 4) if bound else None,
+                          "frac_of_body_bound": round(tflops / peak / bound, 4) if bound else None,
+                          "pairs_per_s": st["pairs"] / (st["total_ms"] * 1e-3)}
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    ach = kern[dom]["tflops"]
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath) and n == 65536:
+        key = f"sym_{dom}_fp32_65536" if names[dom].startswith("k_sym") else f"allpairs_{dom}_fp32_65536"
+        traffic = json.load(open(tpath)).get(key)
+    return {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+            "frac": round(ach / peak, 4), "traffic": traffic, "kernel": names[dom],
+            "frac_of_body_bound": kern[dom]["frac_of_body_bound"],
+            "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
+            "kernels": kern,
+            "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores. "
+                    "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair; for a product "
+                    "evaluated once per unordered pair (k_sym; its timed bracket includes the per-particle "
+                    "finish) 49 (field) or 55 (force) per unordered pair. frac_of_body_bound: frac over the "
+                    "body's FMA-pipe ceiling (BODY_BOUND). DRAM traffic per launch: the 2 MB of pair-layout "
+                    "records, read a few times (L2 absorbs the rest)"}
+
 METRIC = "pair interactions/s; p50/p99 step latency, served vs plain at 1e-5 rel err"
 UNIT = "pairs/s"
 
@@ -284,35 +333,7 @@ def run_ours(args, rank, world, local):
     value = pairs_all / (t_max * 1e-3)
 
     # dominant pair kernel and its FP32 roofline
-    peak = mfgb.probe_fp32_peak()
-    kern = {}
-    names = {}
-    for name, st in (("field", kf), ("force", kg)):
-        if st["launches"]:
-            flop, names[name] = product_flop(name, st)
-            kern[name] = {"kernel": names[name], "launches": st["launches"], "total_ms": round(st["total_ms"], 4),
-                          "avg_ms": round(st["total_ms"] / st["launches"], 4),
-                          "pairs_per_launch": st["pairs"] / st["launches"],
-                          "evals_per_launch": st["evals"] / st["launches"],
-                          "flop_per_launch": flop / st["launches"],
-                          "tflops": flop / (st["total_ms"] * 1e-3) / 1e12,
-                          "pairs_per_s": st["pairs"] / (st["total_ms"] * 1e-3)}
-    dom = max(kern, key=lambda k: kern[k]["total_ms"])
-    ach = kern[dom]["tflops"]
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        key = f"sym_{dom}_fp32_65536" if names[dom].startswith("k_sym") else f"allpairs_{dom}_fp32_65536"
-        traffic = json.load(open(tpath)).get(key) if n == 65536 else None
-    roofline = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
-                "frac": round(ach / peak, 4), "traffic": traffic, "kernel": names[dom],
-                "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
-                "kernels": kern,
-                "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores. "
-                        "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair; for a product "
-                        "evaluated once per unordered pair (k_sym; its timed bracket includes the per-particle "
-                        "finish) 49 (field) or 55 (force) per unordered pair. DRAM traffic per launch: the 2 MB "
-                        "of pair-layout records, read a few times (L2 absorbs the rest)"}
+    roofline = pair_roofline(kf, kg, mfgb.probe_fp32_peak(), n)
 
     # accuracy on a sample: fixed-point residual and force, FP64 oracle
     errors = None
