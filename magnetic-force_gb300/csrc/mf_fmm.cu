@@ -647,7 +647,8 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
       s_row = 0;
       s_pos = -1;
     }
-    for (; !kParts;) {
+    // The row walk and its sweeps (not in the read-back mode).
+    if constexpr (!kParts) for (;;) {
       __syncthreads();  // the previous segment's steps are consumed
       if (tid == 0) fill();
       __syncthreads();
