@@ -383,7 +383,10 @@ mf_status mf_batch_reset_counters(mf_batch* b);
 /* (P = 6) as their own solver, on a host thread and a stream of their own */
 /* started at admission: their timesteps overlap the batch on the device   */
 /* and do not wait for ticks; a tick retires them once finished.  A server */
-/* is used by one host thread at a time.                                   */
+/* is used by one host thread at a time.  While a server exists, device    */
+/* memory the library frees is parked (cudaFree would wait for the FMM     */
+/* requests' kernels) and released at a tick with no FMM request running, */
+/* past 8 GB parked, on an allocation failure, or by mf_server_destroy.    */
 /* ---------------------------------------------------------------------- */
 typedef struct mf_server_config {
   double hbm_budget_bytes;   /* admission budget for request state (e.g. 120e9) */
