@@ -3,13 +3,19 @@
 Every .cu under csrc/ is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a`` and linked with the static
 CUDA runtime into ``libmfgb.so`` next to this file.  Objects go to ``_build/``.
-Rebuilds only what changed (source or header newer than the object).
+Rebuilds only what changed (source or header newer than the object).  A
+stamp in ``_build/`` records the machine, the nvcc version and the flags that
+built the objects; when any of them differs (objects carried from another
+host, a new toolkit) everything is rebuilt.  Objects whose source is gone are
+deleted, so they cannot be linked in.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import glob
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -51,10 +57,25 @@ def _compile(src: str, obj: str, extra: list[str]) -> None:
         raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")
 
 
+def _toolchain_stamp(extra: list[str]) -> str:
+    r = subprocess.run([nvcc(), "--version"], capture_output=True, text=True)
+    text = "\n".join([platform.machine(), r.stdout.strip(), " ".join(NVCC_FLAGS + extra)])
+    return hashlib.sha256(text.encode()).hexdigest()
+
+
 def build(verbose: bool = False, extra: list[str] | None = None, force: bool = False) -> str:
     extra = extra or []
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    names = {os.path.basename(s)[:-3] + ".o" for s in srcs}
+    for o in glob.glob(os.path.join(BUILD, "*.o")):
+        if os.path.basename(o) not in names:
+            os.remove(o)
+    stamp_path = os.path.join(BUILD, "toolchain.stamp")
+    stamp = _toolchain_stamp(extra)
+    old = open(stamp_path).read().strip() if os.path.exists(stamp_path) else ""
+    if old != stamp:
+        force = True
     hdr = max([os.path.getmtime(h) for h in _headers()] + [0.0])
     objs = []
     jobs = []
@@ -76,6 +97,9 @@ def build(verbose: bool = False, extra: list[str] | None = None, force: bool = F
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    if old != stamp:
+        with open(stamp_path, "w") as f:
+            f.write(stamp + "\n")
     if verbose:
         print(f"built {LIB} ({len(jobs)} objects recompiled)")
     return LIB
