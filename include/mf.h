@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MF_ABI_VERSION 1
+#define MF_ABI_VERSION 2
 
 typedef enum mf_status {
   MF_OK = 0,
@@ -92,12 +92,16 @@ typedef enum mf_option {
                                (default 1 for N >= 16384, else 4) */
   MF_OPT_KERNEL_TIMING = 8, /* 1: time every all-pairs launch (and every FMM product as a
                                whole) with CUDA events (mf_get_kernel_stats) */
-  MF_OPT_FMM = 9,           /* field and force products of FP32 handles: 0 auto (the FMM
-                               above 65,536 particles, all-pairs below), 1 always the FMM,
+  MF_OPT_FMM = 9,           /* field and force products of FP32 handles: 0 auto (field
+                               products through the FMM above 65,536 particles, the Kelvin
+                               force above 262,144; all-pairs below), 1 always the FMM,
                                2 always all-pairs.  FP64 handles are all-pairs. */
   MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
-                               (terms of degree n < P): 4..8, default 6 (magnetic_force.cu:661) */
-  MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture, default 0.5 (FMMOptions.hpp:118) */
+                               (terms of degree n < P): 4..8, default 8.  The reference's
+                               default is 6 (magnetic_force.cu:661); at 6 the field here is
+                               3e-5 from FP64 direct sums, at 8 2-3e-6. */
+  MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture of the field products, default 0.5
+                               (FMMOptions.hpp:118) */
   MF_OPT_FMM_LEAF = 12,     /* FMM leaf level: the deepest whose boxes hold at least this many
                                particles on average (default 64) */
   MF_OPT_AUTOTUNE = 13,     /* block shapes of the FP32 all-pairs launches: 0 fixed default,
@@ -105,14 +109,20 @@ typedef enum mf_option {
                                per process on the scene's own data), 2 tuned choices only when
                                already cached.  MF_AUTOTUNE=0 in the environment makes 0 the
                                default for handles and batches. */
-  MF_OPT_PAIR_SYMMETRIC = 14 /* FP32 packed field and force products of the handle's scene,
+  MF_OPT_PAIR_SYMMETRIC = 14,/* FP32 packed field and force products of the handle's scene,
                                each unordered pair evaluated once for both particles (a pair
                                kernel and a per-particle finish) instead of every ordered
                                pair: 0 never, 1 where tuning measured it faster (default;
                                without tuning, the force only), 2 always.  On the FMM path
                                the force's near field is evaluated once per unordered box
-                               pair with 2, and with 1 from 524,288 particles on.  Not in
+                               pair with 2, and with 1 from 1,048,576 particles on.  Not in
                                the reference. */
+  MF_OPT_FMM_FORCE_THETA = 15 /* aperture of the Kelvin force (and the external gradient tensor)
+                               products on the FMM path, default 0.3; they use the smaller of
+                               this and MF_OPT_FMM_THETA.  The force takes the Hessian of the
+                               local expansion, whose error relative to the small net force
+                               of a magnetised body is ~40x the field's: 1.3e-4 at 0.5 and
+                               5e-6 at 0.3 (P = 8, 1,048,576 particles).  Not in the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -244,7 +254,7 @@ mf_status mf_autotune_report(char* buf, int64_t cap, int64_t* len);
  * Replaces the tree and interaction-list state of the reference's
  * fmmtl::kernel_matrix plans (KernelMatrixPlan.hpp:75-113). */
 typedef struct mf_fmm_stats {
-  int32_t active;            /* 1 if the handle's products use the FMM */
+  int32_t active;            /* 1 if the handle's field products use the FMM */
   int32_t levels;            /* box grid levels, root included */
   int32_t leaf_level;
   int32_t degree;            /* expansion degree (order - 1) */
@@ -255,9 +265,13 @@ typedef struct mf_fmm_stats {
   double p2p_pairs;          /* near-field pairs executed per product */
   double m2l_per_product;    /* multipole-to-local translations per product */
   int32_t launches_per_product;
-  int32_t pad;
+  int32_t force_active;      /* 1 if the handle's Kelvin force uses the FMM */
   int64_t field_products;    /* FMM products since the last mf_reset_counters */
   int64_t force_products;
+  double theta;              /* aperture of the field products */
+  double force_theta;        /* aperture of the force products */
+  double force_p2p_pairs;    /* near-field pairs per force product (0 unless force_active) */
+  double force_m2l_per_product;
 } mf_fmm_stats;
 mf_status mf_get_fmm_stats(mf_solver* s, mf_fmm_stats* out);
 
@@ -310,8 +324,10 @@ mf_status mf_release_scratch(void);
 /* ---------------------------------------------------------------------- */
 typedef struct mf_fmm mf_fmm;
 /* targets may be NULL (nt ignored): the targets are the sources.  order is
- * P as the reference counts it (4..8), theta the acceptance aperture,
- * leaf_min the mean particles per leaf box. */
+ * P as the reference counts it (4..8), theta the acceptance aperture of the
+ * field product, leaf_min the mean particles per leaf box.  The Hessian
+ * product uses the aperture min(theta, 0.3), as the handles' force does
+ * (MF_OPT_FMM_FORCE_THETA): its lists are built on its first call. */
 mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, int64_t nt, float h, int32_t order,
                         double theta, int32_t leaf_min, int32_t device, mf_fmm** out);
 mf_status mf_fmm_destroy(mf_fmm* f);
@@ -379,8 +395,9 @@ mf_status mf_batch_reset_counters(mf_batch* b);
 /* limit allow, advances every running request by one timestep in shared   */
 /* batched launches, and retires finished requests (their final state is   */
 /* kept for mf_server_result).  Particle state stays on the device while a  */
-/* request runs.  Requests above 65,536 particles run through the FMM      */
-/* (P = 6) as their own solver, on a host thread and a stream of their own */
+/* request runs.  Requests above 65,536 particles run as their own solver */
+/* handle (field products through the FMM at P = 8, the Kelvin force as    */
+/* MF_OPT_FMM's automatic choice picks it), on a host thread and a stream of their own */
 /* started at admission: their timesteps overlap the batch on the device   */
 /* and do not wait for ticks; a tick retires them once finished.  A server */
 /* is used by one host thread at a time.  While a server exists, device    */

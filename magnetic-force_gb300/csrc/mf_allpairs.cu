@@ -517,13 +517,20 @@ int default_sym_mode() {
   return mode;
 }
 
+namespace {
+thread_local int t_tune_override = -1;  // -1: none; else a Tune value for handles made on this thread
+}
+
 Tune default_tune_mode() {
   static const Tune mode = [] {
     const char* e = getenv("MF_AUTOTUNE");
     return (e && e[0] == '0') ? Tune::Off : Tune::OnMiss;
   }();
+  if (t_tune_override >= 0 && mode != Tune::Off) return Tune(t_tune_override);
   return mode;
 }
+
+void set_thread_tune_mode(int mode) { t_tune_override = mode; }
 
 int default_shape(Body body, const std::vector<SceneSpec>& specs, bool allow_sym) {
   return allow_sym && body == Body::ForceF2 && sym_eligible(body, specs) ? kShapeSym : 0;

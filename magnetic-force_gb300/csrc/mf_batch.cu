@@ -597,8 +597,9 @@ class Batch {
 // ---------------------------------------------------------------------------
 // Serving with continuous batching.
 // ---------------------------------------------------------------------------
-// Requests above this many particles run as their own solver handle through
-// the FMM (P = 6), each on a host thread and a stream of its own, so their
+// Requests above this many particles run as their own solver handle (field
+// products through the FMM at P = 8, the Kelvin force as the handle's
+// automatic choice picks it), each on a host thread and a stream of its own, so their
 // kernels overlap the batch's on the device and their host-side waits never
 // hold up the serving loop; smaller ones join the all-pairs batch.
 constexpr int64_t kServeFmmMin = 65536;
@@ -639,9 +640,14 @@ class Server {
   // scratch.  FMM request: a solver handle's vectors, published arrays, cell
   // list and octree.
   static double need_bytes(int64_t n) {
-    // FMM requests: the handle's state and tree, plus ~1.2 KB per particle of
-    // near-field partial sums (the force's near field once per box pair).
-    if (n > kServeFmmMin) return double(n) * (720.0 + 1200.0) + 64.0 * 1024 * 1024;
+    // FMM requests: the handle's state and trees, ~1.2 KB per particle of
+    // near-field partial sums where the force's near field runs once per box
+    // pair, and, where the force is the all-pairs product once per unordered
+    // pair, its block sums (12 KB per ordered pair of 1,024-particle blocks).
+    if (n > kServeFmmMin) {
+      const double nb = std::ceil(double(n) / 1024.0);
+      return double(n) * (720.0 + 1200.0) + 12288.0 * nb * nb + 64.0 * 1024 * 1024;
+    }
     return double(n) * 320.0 + 4.0 * 1024 * 1024;
   }
 
@@ -885,13 +891,16 @@ class Server {
   };
 
   // The thread of an FMM request: a solver handle on its own non-blocking
-  // stream (CG to the server's tolerance, FMM order 6), a converged cold
+  // stream (CG to the server's tolerance, the handle's automatic choice of
+  // FMM or all-pairs per product, tuned block shapes only where already
+  // cached, so no timing lands on the request), a converged cold
   // solve, the request's timesteps, then the read-back of its final state.
   static void fmm_worker(FmmJob* j, mf_scene_desc d, const float* pos, mf_server_config cfg) {
     mf_solver* sv = nullptr;
     cudaStream_t stream = nullptr;
     auto run = [&]() -> mf_status {
       MF_CUDA_TRY(cudaSetDevice(cfg.device));
+      set_thread_tune_mode(int(Tune::CachedOnly));
       mf_params p{};
       p.num_particles = d.n;
       p.h = d.h;
@@ -911,8 +920,7 @@ class Server {
       MF_TRY(mf_set_stream(sv, stream));
       MF_TRY(mf_set_option(sv, MF_OPT_SOLVER, MF_SOLVER_CG));
       MF_TRY(mf_set_option(sv, MF_OPT_REL_TOL, cfg.rel_tol));
-      MF_TRY(mf_set_option(sv, MF_OPT_FMM, 1));
-      MF_TRY(mf_set_option(sv, MF_OPT_FMM_ORDER, 6));
+      MF_TRY(mf_set_option(sv, MF_OPT_FMM, 0));
       int64_t it = 0;
       double rr = 0;
       mf_status s = mf_solve(sv, 500, &it, &rr);

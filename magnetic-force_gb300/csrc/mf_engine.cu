@@ -178,8 +178,15 @@ struct EngineBase {
   int device = 0;
 };
 
-// Particle count above which FP32 handles take the FMM by default.
+// Particle counts above which FP32 handles take the FMM by default: the
+// field products above kFmmAutoMin, the Kelvin force above kFmmForceAutoMin.
+// The force's near field is wider (FmmConfig::theta_force), so in a compact
+// scene of up to ~200k particles it covers most of the scene, and the
+// all-pairs product once per unordered pair is as fast (measured on the
+// r = 0.3 cylinder: 11.6 / 11.0 ms at 131,072, 25.2 / 25.2 at 196,608, 44.9
+// / 35.3 at 262,144, all-pairs / FMM) and exact to FP32 rounding.
 constexpr int64_t kFmmAutoMin = 65536;
+constexpr int64_t kFmmForceAutoMin = 196608;
 
 template <class Real>
 class Engine final : public EngineBase {
@@ -353,7 +360,7 @@ class Engine final : public EngineBase {
   // ---- evaluate_fitted_near_foece ----------------------------------------------
   mf_status eval_force() override {
     MF_TRY(publish_b());  // M = c b (magnetic_force.cu:899, :915)
-    if (use_fmm()) {
+    if (use_fmm_force()) {
       MF_TRY(fmm_product(true, plan_force_, mom4(), nullptr, nullptr, nullptr, nullptr));
       ctr_.force_passes += 1;
       ctr_.force_pairs += plan_force_.pairs;
@@ -467,26 +474,33 @@ class Engine final : public EngineBase {
       case MF_OPT_KERNEL_TIMING: timing_ = v != 0.0; return MF_OK;
       case MF_OPT_FMM: {
         if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "fmm mode must be 0, 1 or 2");
-        const bool was = use_fmm();
+        const bool was_field = use_fmm_field(), was_force = use_fmm_force();
         fmm_mode_ = int(v);
-        // all-pairs from now on: its plans were built untuned
-        if (was && !use_fmm() && plans_ready_ && tune_ != Tune::Off) MF_TRY(build_plans());
+        // a product on all-pairs from now on: its plan was built untuned
+        if (((was_field && !use_fmm_field()) || (was_force && !use_fmm_force())) && plans_ready_ &&
+            tune_ != Tune::Off)
+          MF_TRY(build_plans());
         return MF_OK;
       }
       case MF_OPT_FMM_ORDER:
         if (v < 4 || v > 8 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..8");
         fmm_cfg_.order = int(v);
-        fmm_dirty_ = ext_fmm_dirty_ = true;
+        fmm_dirty_ = fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_FMM_THETA:
         if (!(v > 0.0 && v <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm theta must be in (0, 1]");
         fmm_cfg_.theta = v;
-        fmm_dirty_ = ext_fmm_dirty_ = true;
+        fmm_dirty_ = fmmf_dirty_ = ext_fmm_dirty_ = true;
+        return MF_OK;
+      case MF_OPT_FMM_FORCE_THETA:
+        if (!(v > 0.0 && v <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm force theta must be in (0, 1]");
+        fmm_cfg_.theta_force = v;
+        fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_FMM_LEAF:
         if (v < 1 || v > 4096) return fail(MF_ERR_INVALID_ARG, "fmm leaf size must be 1..4096");
         fmm_cfg_.leaf_min = int(v);
-        fmm_dirty_ = ext_fmm_dirty_ = true;
+        fmm_dirty_ = fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_AUTOTUNE:
         if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "autotune mode must be 0, 1 or 2");
@@ -521,6 +535,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM: *v = fmm_mode_; return MF_OK;
       case MF_OPT_FMM_ORDER: *v = fmm_cfg_.order; return MF_OK;
       case MF_OPT_FMM_THETA: *v = fmm_cfg_.theta; return MF_OK;
+      case MF_OPT_FMM_FORCE_THETA: *v = fmm_cfg_.theta_force; return MF_OK;
       case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
       case MF_OPT_AUTOTUNE: *v = double(int(tune_)); return MF_OK;
       case MF_OPT_PAIR_SYMMETRIC: *v = double(sym_mode_); return MF_OK;
@@ -547,11 +562,15 @@ class Engine final : public EngineBase {
   CellList cells_;
   bool cells_dirty_ = true;
   Plan<Real> plan_resid_, plan_grad_, plan_dd_, plan_cgq_, plan_force_, plan_ext_field_, plan_ext_tensor_, plan_apply_;
-  // FMM state (FP32 handles): the octree of the current positions.
-  Fmm fmm_;
-  // External dipoles through the FMM: their octree (particles as targets),
-  // their cell list and the near-field correction records.
-  Fmm ext_fmm_;
+  // FMM state (FP32 handles): the octree of the current positions, its lists
+  // at the field's aperture (fmm_) and, where it is smaller, at the force's
+  // (fmmf_).
+  Fmm fmm_, fmmf_;
+  bool fmmf_dirty_ = true;
+  // External dipoles through the FMM: their octree (particles as targets) at
+  // the field's aperture and at the force's (the gradient tensor), their cell
+  // list and the near-field correction records.
+  Fmm ext_fmm_, ext_fmmt_;
   CellList ext_cells_;
   DevBuf ext_corr_;
   bool ext_fmm_dirty_ = true;
@@ -647,22 +666,22 @@ class Engine final : public EngineBase {
     int fshape = 0, gshape = 0;
     const bool offer = sym_mode_ == 1;
     if constexpr (kF32) {
-      // A handle on the FMM path launches no all-pairs product: its plans
-      // only carry the epilogue coefficients, so they are not timed.
-      if (!use_fmm()) {
-        fshape = default_shape(fb, {base}, offer);
-        gshape = default_shape(gb, {base}, offer);
-      }
-      if (tune_ != Tune::Off && !use_fmm()) {
+      // A product on the FMM path launches no all-pairs kernel: its plan only
+      // carries the epilogue coefficients, so it is not timed.
+      if (!use_fmm_field()) fshape = default_shape(fb, {base}, offer);
+      if (!use_fmm_force()) gshape = default_shape(gb, {base}, offer);
+      Plan<Real> tp;
+      if (tune_ != Tune::Off && !use_fmm_field()) {
         LaunchIO<Real> io;
         io.tpos = pos4();
         io.spos = fb == Body::FieldF2 ? pos2_.template as<float4>() : pos4();
         io.smom = fb == Body::FieldF2 ? mom2_.template as<float4>() : v4(V_B);
         io.corr4 = fb == Body::FieldF2 ? corr_.template as<float4>() : nullptr;
         io.out4 = v4(V_DD);
-        Plan<Real> tp;
         MF_TRY(tuned_plan(fb, {base}, tp, io, scr_, st_, tune_, offer));
         fshape = tp.shape;
+      }
+      if (tune_ != Tune::Off && !use_fmm_force()) {
         LaunchIO<Real> ig;
         ig.tpos = pos4();
         ig.tmom = mom4();
@@ -673,9 +692,9 @@ class Engine final : public EngineBase {
         MF_TRY(tuned_plan(gb, {base}, tp, ig, scr_, st_, tune_, offer));
         gshape = tp.shape;
       }
-      if (sym_mode_ == 2 && !use_fmm()) {
-        if (sym_eligible(fb, {base})) fshape = kShapeSym;
-        if (sym_eligible(gb, {base})) gshape = kShapeSym;
+      if (sym_mode_ == 2) {
+        if (!use_fmm_field() && sym_eligible(fb, {base})) fshape = kShapeSym;
+        if (!use_fmm_force() && sym_eligible(gb, {base})) gshape = kShapeSym;
       }
     }
     MF_TRY(build_plan<Real>(fb, {s}, plan_resid_, fshape));
@@ -778,8 +797,18 @@ class Engine final : public EngineBase {
   mf_status fmm_stats(mf_fmm_stats* out) override {
     if (!out) return fail(MF_ERR_INVALID_ARG, "NULL");
     *out = mf_fmm_stats{};
-    out->active = use_fmm() ? 1 : 0;
-    if (use_fmm()) MF_TRY(ensure_fmm());
+    out->active = use_fmm_field() ? 1 : 0;
+    out->force_active = use_fmm_force() ? 1 : 0;
+    out->theta = fmm_cfg_.theta;
+    out->force_theta = fmm_cfg_.force_theta();
+    if (use_fmm_field() || use_fmm_force()) MF_TRY(ensure_fmm());
+    if (use_fmm_force()) {
+      Fmm* ff = nullptr;
+      MF_TRY(ensure_fmm_force(&ff));
+      const FmmStats& g = ff->stats();
+      out->force_p2p_pairs = g.p2p_pairs;
+      out->force_m2l_per_product = g.m2l_per_product;
+    }
     const FmmStats& f = fmm_.stats();
     out->levels = f.levels;
     out->leaf_level = f.leaf_level;
@@ -877,13 +906,18 @@ class Engine final : public EngineBase {
       ++ctr_.kernel_launches;
       cells_dirty_ = true;
       fmm_dirty_ = true;
+      fmmf_dirty_ = true;
       ext_fmm_dirty_ = true;
     }
   }
 
-  bool use_fmm() const {
+  bool use_fmm_field() const {
     if constexpr (!kF32) return false;
     return fmm_mode_ == 1 || (fmm_mode_ == 0 && np_ > kFmmAutoMin);
+  }
+  bool use_fmm_force() const {
+    if constexpr (!kF32) return false;
+    return fmm_mode_ == 1 || (fmm_mode_ == 0 && np_ > kFmmForceAutoMin);
   }
   // Many external dipoles go through the FMM as well (the reference's
   // fmm_hext_evaluator, magnetic_force.cu:688-697): an octree over the
@@ -907,6 +941,12 @@ class Engine final : public EngineBase {
         }
         MF_TRY(ext_fmm_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, fmm_cfg_, st_));
         ctr_.kernel_launches += 17;
+        if (fmm_cfg_.force_theta() < fmm_cfg_.theta) {
+          FmmConfig ct = fmm_cfg_;
+          ct.theta = fmm_cfg_.force_theta();
+          MF_TRY(ext_fmmt_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, ct, st_));
+          ctr_.kernel_launches += 17;
+        }
         ext_fmm_dirty_ = false;
       }
       MF_TRY(scr_.ensure(0, 0));
@@ -928,8 +968,9 @@ class Engine final : public EngineBase {
       t.corr4 = corr;
       for (int k = 0; k < 9; ++k) t.out[k] = rext(k);
       t.err = scr_.err.template as<int32_t>();
-      MF_TRY(ext_fmm_.product(2, sp, sm, t, plan_ext_tensor_.host[0], st_, nullptr));
-      ctr_.kernel_launches += 2 * (ext_fmm_.launches_per_product() + 1);
+      Fmm& ft = fmm_cfg_.force_theta() < fmm_cfg_.theta ? ext_fmmt_ : ext_fmm_;
+      MF_TRY(ft.product(2, sp, sm, t, plan_ext_tensor_.host[0], st_, nullptr));
+      ctr_.kernel_launches += ext_fmm_.launches_per_product() + ft.launches_per_product() + 2;
     }
     return MF_OK;
   }
@@ -945,12 +986,37 @@ class Engine final : public EngineBase {
     }
     return MF_OK;
   }
+  // The octree whose lists serve the Kelvin force: fmm_ when the force's
+  // aperture is the field's, else fmmf_ built at the smaller one.
+  mf_status ensure_fmm_force(Fmm** out) {
+    if constexpr (kF32) {
+      if (fmm_cfg_.force_theta() >= fmm_cfg_.theta) {
+        MF_TRY(ensure_fmm());
+        *out = &fmm_;
+        return MF_OK;
+      }
+      MF_TRY(ensure_cells());
+      if (fmmf_dirty_) {
+        FmmConfig ct = fmm_cfg_;
+        ct.theta = fmm_cfg_.force_theta();
+        MF_TRY(fmmf_.build(pos4(), np_, nullptr, 0, h_, cells_.bbox(0), ct, st_));
+        ctr_.kernel_launches += 8;
+        fmmf_dirty_ = false;
+      }
+      MF_TRY(scr_.ensure(0, 0));
+      *out = &fmmf_;
+    }
+    return MF_OK;
+  }
   // One FMM product with the epilogue of `plan` (field: out4 / add4 / add4b;
   // force: the published force arrays), timed as a whole when timing is on.
   mf_status fmm_product(bool force, const Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4,
                         const R4* add4b, const double* done) {
     if constexpr (kF32) {
-      MF_TRY(ensure_fmm());
+      Fmm* fp = &fmm_;
+      if (force) MF_TRY(ensure_fmm_force(&fp));
+      else MF_TRY(ensure_fmm());
+      Fmm& fm = *fp;
       float4* corr = corr_.template as<float4>();
       if (force) MF_TRY(cells_.force_correction(pos4(), src_mom, corr, st_));
       else MF_TRY(cells_.field_correction(pos4(), src_mom, corr, st_, done, 0));
@@ -981,10 +1047,10 @@ class Engine final : public EngineBase {
         t.body = force ? MF_K_FORCE : MF_K_FIELD;
         t.pairs = t.evals = plan.pairs;
         tf.body = MF_K_FMM_FAR;
-        tf.pairs = tf.evals = fmm_.stats().m2l_per_product;
+        tf.pairs = tf.evals = fm.stats().m2l_per_product;
         tn.body = force ? MF_K_FMM_NEAR_FORCE : MF_K_FMM_NEAR_FIELD;
-        tn.pairs = tn.evals = fmm_.stats().p2p_pairs;
-        if (sym_near) tn.evals = fmm_.sym_near_evals();
+        tn.pairs = tn.evals = fm.stats().p2p_pairs;
+        if (sym_near) tn.evals = fm.sym_near_evals();
         for (TimedLaunch* x : {&t, &tf, &tn}) {
           MF_CUDA_TRY(cudaEventCreate(&x->start));
           MF_CUDA_TRY(cudaEventCreate(&x->stop));
@@ -995,7 +1061,7 @@ class Engine final : public EngineBase {
         marks[2] = tn.start;
         marks[3] = tn.stop;
       }
-      MF_TRY(fmm_.product(force ? 1 : 0, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr,
+      MF_TRY(fm.product(force ? 1 : 0, pos4(), src_mom, a, plan.host[0], st_, done, timing_ ? marks : nullptr,
                           sym_near));
       if (timing_) {
         MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
@@ -1003,7 +1069,7 @@ class Engine final : public EngineBase {
         timed_.push_back(tf);
         timed_.push_back(tn);
       }
-      ctr_.kernel_launches += fmm_.launches_per_product() + 1;
+      ctr_.kernel_launches += fm.launches_per_product() + 1;
       if (force) ++fmm_force_products_;
       else ++fmm_field_products_;
     }
@@ -1012,7 +1078,7 @@ class Engine final : public EngineBase {
 
   mf_status field(Plan<Real>& plan, const R4* src_mom, R4* out4, const R4* add4, const R4* add4b,
                   const double* done = nullptr) {
-    if (use_fmm()) {
+    if (use_fmm_field()) {
       MF_TRY(fmm_product(false, plan, src_mom, out4, add4, add4b, done));
       ctr_.field_products += 1;
       ctr_.field_pairs += plan.pairs;  // effective pairs (N^2), the FMM convention

@@ -1479,6 +1479,12 @@ struct mf_fmm {
   int device = 0;
   cudaStream_t st = nullptr;
   mfgb::Fmm fmm;
+  // The Hessian product's lists at the force aperture, built on its first
+  // call when that aperture is smaller than the field's.
+  mfgb::Fmm fmmh;
+  bool fmmh_built = false;
+  mfgb::FmmConfig cfg;
+  double h = 0.0, bbox[6] = {0, 0, 0, 0, 0, 0};
   mfgb::CellList cells;  // over the sources: the near-field correction
   mfgb::Scratch scr;
   mfgb::DevBuf spos, smom, tpos, corr, out4, out9, staging;
@@ -1582,10 +1588,12 @@ mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, 
           bbox[k] = std::min(bbox[k], double(targets[3 * i + k]));
           bbox[3 + k] = std::max(bbox[3 + k], double(targets[3 * i + k]));
         }
-    FmmConfig cfg;
+    FmmConfig& cfg = f->cfg;
     cfg.order = order;
     cfg.theta = theta;
     cfg.leaf_min = leaf_min;
+    f->h = double(h);
+    for (int k = 0; k < 6; ++k) f->bbox[k] = bbox[k];
     MF_TRY(f->fmm.build(f->spos.as<float4>(), ns, f->same ? nullptr : f->tpos.as<float4>(), f->nt, double(h), bbox,
                         cfg, f->st));
     MF_TRY(f->corr.reserve(size_t(f->nt + 2) * sizeof(float4), false, true));
@@ -1648,7 +1656,18 @@ mf_status mf_fmm_hessian(mf_fmm* f, const float* charges, float* results9) {
     a.corr4 = x.corr.as<float4>();
     for (int k = 0; k < 9; ++k) a.out[k] = x.out9.as<float>() + size_t(k) * size_t(x.nt);
     a.err = x.scr.err.as<int32_t>();
-    MF_TRY(x.fmm.product(2, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
+    Fmm* fh = &x.fmm;
+    if (x.cfg.force_theta() < x.cfg.theta) {
+      if (!x.fmmh_built) {
+        FmmConfig ct = x.cfg;
+        ct.theta = x.cfg.force_theta();
+        MF_TRY(x.fmmh.build(x.spos.as<float4>(), x.ns, x.same ? nullptr : x.tpos.as<float4>(), x.nt, x.h, x.bbox, ct,
+                            x.st));
+        x.fmmh_built = true;
+      }
+      fh = &x.fmmh;
+    }
+    MF_TRY(fh->product(2, x.spos.as<float4>(), x.smom.as<float4>(), a, x.sc, x.st, nullptr));
     MF_TRY(x.staging.reserve(size_t(9 * x.nt) * sizeof(float) + 16));
     k_soa9_to_aos<<<blocks_for(x.nt), 256, 0, x.st>>>(x.out9.as<float>(), x.nt, x.staging.as<float>());
     MF_CUDA_TRY(cudaGetLastError());
@@ -1675,6 +1694,16 @@ mf_status mf_fmm_get_stats(mf_fmm* f, mf_fmm_stats* out) {
     out->p2p_pairs = s.p2p_pairs;
     out->m2l_per_product = s.m2l_per_product;
     out->launches_per_product = x.fmm.launches_per_product();
+    out->force_active = 1;
+    out->theta = x.cfg.theta;
+    out->force_theta = x.cfg.force_theta();
+    if (x.fmmh_built) {
+      out->force_p2p_pairs = x.fmmh.stats().p2p_pairs;
+      out->force_m2l_per_product = x.fmmh.stats().m2l_per_product;
+    } else if (x.cfg.force_theta() >= x.cfg.theta) {
+      out->force_p2p_pairs = s.p2p_pairs;
+      out->force_m2l_per_product = s.m2l_per_product;
+    }
     return MF_OK;
   });
 }

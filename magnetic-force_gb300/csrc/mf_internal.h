@@ -120,11 +120,12 @@ constexpr int64_t kBatchPackedForceMin = 4096;
 // (0.206 against 0.213 ms).
 constexpr int64_t kSymDirectMin = 32768;
 // FMM handles: the force's near field once per unordered box pair from this
-// size on.  At 1,048,576 particles (P = 8) it measured 18.7 ms against 20.2 ms
-// for every ordered pair; with it on for the served stream's FMM requests
-// (75,000-225,000 particles, P = 6) the served capacity fell from 7.1 to 5.0
-// requests/s.
-constexpr int64_t kSymNearMin = 524288;
+// size on.  With the force's aperture of 0.3 (its half stencil ~4x the
+// partial-sum planes of 0.5), force products on the r = 0.3 cylinder took
+// 84.0 against 90.2 ms for every ordered pair at 1,048,576 particles, but
+// 188.6 against 128.8 at 524,288 (leaf boxes of ~330 particles there) and
+// 49.3 against 35.3 at 262,144.
+constexpr int64_t kSymNearMin = 1048576;
 
 template <class Real, Body B>
 struct KCfg;
@@ -288,6 +289,10 @@ int default_shape(Body body, const std::vector<SceneSpec>& specs, bool allow_sym
 // Default tuning mode of new handles and batches: OnMiss unless the
 // environment sets MF_AUTOTUNE=0.
 Tune default_tune_mode();
+// Handles and batches created on the calling thread from now on start in
+// this tune mode (a Tune value; -1 restores the process default).  The
+// process default MF_AUTOTUNE=0 still wins.
+void set_thread_tune_mode(int mode);
 // Default pair-symmetric mode of new handles and batches (MF_OPT_PAIR_SYMMETRIC:
 // 0 never, 1 tuned, 2 always): 1 unless the environment sets MF_PAIR_SYMMETRIC.
 int default_sym_mode();
@@ -378,9 +383,18 @@ class CellList {
 // Uniform-octree FMM for one scene (mf_fmm.cu)
 // ---------------------------------------------------------------------------
 struct FmmConfig {
-  int order = 6;         // expansion terms per degree as the reference counts them (n < P); degree P-1
+  int order = 8;         // expansion terms per degree as the reference counts them (n < P); degree P-1
   double theta = 0.5;    // multipole acceptance aperture (FMMOptions.hpp:56-78)
   int leaf_min = 64;     // leaf level: the deepest with at least this many particles per box on average
+  // Aperture of the Kelvin force and force-tensor products, which take the
+  // Hessian of the local expansion: it converges one degree later than the
+  // field, and inside a magnetised body the far boxes' Hessians cancel to a
+  // small net force, so the same truncation error is ~40x larger relative to
+  // the result.  Measured against FP64 direct sums at P = 8 on a cylinder of
+  // 1,048,576 particles: 1.3e-4 at 0.5, 3.1e-5 at 0.42, 1.1e-5 at 0.35,
+  // 5.4e-6 at 0.3 (field at 0.5: 3.3e-6).  The force uses min(theta, this).
+  double theta_force = 0.3;
+  double force_theta() const { return theta_force < theta ? theta_force : theta; }
 };
 
 // One level of the uniform box grid (level 0 is one box holding the scene).

@@ -40,7 +40,7 @@ Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyfor
      "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
        "crit_size": 6, "check_interval": 7, "kernel_timing": 8, "fmm": 9, "fmm_order": 10, "fmm_theta": 11,
-       "fmm_leaf": 12, "autotune": 13, "pair_symmetric": 14}
+       "fmm_leaf": 12, "autotune": 13, "pair_symmetric": 14, "fmm_force_theta": 15}
 FMM_AUTO, FMM_ON, FMM_OFF = 0, 1, 2
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
@@ -76,7 +76,9 @@ class mf_fmm_stats(ctypes.Structure):
                 ("degree", ctypes.c_int32), ("leaf_boxes", ctypes.c_int64), ("occupied_leaves", ctypes.c_int64),
                 ("max_leaf", ctypes.c_int32), ("near_rows", ctypes.c_int32), ("p2p_pairs", ctypes.c_double),
                 ("m2l_per_product", ctypes.c_double), ("launches_per_product", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("field_products", ctypes.c_int64), ("force_products", ctypes.c_int64)]
+                ("force_active", ctypes.c_int32), ("field_products", ctypes.c_int64),
+                ("force_products", ctypes.c_int64), ("theta", ctypes.c_double), ("force_theta", ctypes.c_double),
+                ("force_p2p_pairs", ctypes.c_double), ("force_m2l_per_product", ctypes.c_double)]
 
 
 KERNEL = {"field": 0, "force": 1, "tensor": 2, "fmm_near_field": 3, "fmm_near_force": 4, "fmm_far": 5}
@@ -298,7 +300,7 @@ class Solver:
     def fmm_stats(self) -> dict:
         st = mf_fmm_stats()
         check(load().mf_get_fmm_stats(self._h, ctypes.byref(st)))
-        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_ if f != "pad"}
+        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_}
 
     def apply_field(self, moments) -> np.ndarray:
         """G(m) at the particles: the reference's cuda_magnet_cgOptimizer::G."""
@@ -553,7 +555,7 @@ class FmmMatrix:
     def stats(self) -> dict:
         st = mf_fmm_stats()
         check(load().mf_fmm_get_stats(self._h, ctypes.byref(st)))
-        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_ if f != "pad"}
+        return {f: getattr(st, f) for f, _ in mf_fmm_stats._fields_}
 
     def close(self):
         if self._h is not None:

@@ -83,11 +83,13 @@ def test_budget_enforced(mf):
     srv.close()
 
 
-def test_fmm_request_in_the_mix(mf):
-    # A request above 65,536 particles runs as its own FMM solver (P = 6) on
-    # a host thread and a stream of its own beside the batch; its result
-    # equals the same solver run alone with the same settings, and the small
-    # requests are unaffected.
+def test_fmm_request_in_the_mix(mf, oracle):
+    # A request above 65,536 particles runs as its own solver handle (field
+    # products through the FMM at P = 8, the force as the handle's automatic
+    # choice picks it) on a host thread and a stream of its own beside the
+    # batch; its result equals the same solver run alone with the same
+    # settings, is within 1e-5 of FP64 oracle sums, and the small requests
+    # are unaffected.
     import scenes
     big = scenes.jittered_lattice(70000, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=77)
     small = scenes_for((900, 1700), seed=51)
@@ -107,8 +109,6 @@ def test_fmm_request_in_the_mix(mf):
     s = mf.Solver(big.n, big.h, big.h, big.volume, big.chi, big.H0, None, None, big.pos)
     s.set_option("solver", mf.SOLVER_CG)
     s.set_option("rel_tol", 1e-7)
-    s.set_option("fmm", mf.FMM_ON)
-    s.set_option("fmm_order", 6)
     s.solve(500)
     for _ in range(steps):
         s.advance(1e-3, 8)
@@ -116,6 +116,23 @@ def test_fmm_request_in_the_mix(mf):
     assert np.max(np.abs(srv.result(ids[1], "positions") - s.xyz)) < 1e-6
     assert rel(srv.result(ids[1], "magnetic_bodyforce"), s.magnetic_bodyforce) < 1e-5
     assert rel(srv.result(ids[1], "total_B_over_mu0"), s.total_B_over_mu0) < 1e-5
+    # The same handle solved and its force evaluated at the final positions
+    # (a timestep ends by moving the particles), against FP64 oracle sums
+    # over all N at 512 particles: the fixed-point residual of b and the
+    # force at its M.
+    s.solve(500)
+    s.evaluate_fitted_near_foece()
+    idx = np.sort(np.random.default_rng(3).choice(big.n, 512, replace=False))
+    pos = np.asarray(s.xyz, np.float64)
+    b = np.asarray(s.total_B_over_mu0, np.float64)
+    M = np.asarray(s.M, np.float64)
+    G = oracle.field(pos[idx], pos, M, big.h)
+    H0 = np.tile(np.asarray(big.H0, np.float64), (len(idx), 1))
+    res = np.linalg.norm(b[idx] - H0 - G) / np.linalg.norm(H0)
+    T = oracle.tensor_sum(pos[idx], pos, M, big.h).reshape(-1, 3, 3)
+    F = np.einsum("icr,ic->ir", T, M[idx])
+    ef = rel(s.magnetic_bodyforce[idx], F)
+    assert res < 1e-5 and ef < 1e-5, (res, ef)
     for k, sc in ((0, small[0]), (2, small[1])):
         alone = run_alone(mf, sc, steps)
         assert rel(srv.result(ids[k], "magnetic_bodyforce"), alone["magnetic_bodyforce"]) < 1e-5

@@ -167,3 +167,24 @@ def test_main_cu_scene(oracle):
     b, it, rr = oracle.solve_cg(g, 1.0, 0.5, hext, rel_tol=1e-14)
     F = oracle.force(g, 0.5 * b, 1.0, rext)
     assert np.all(np.isfinite(F))
+
+
+def test_config2_fixture_is_the_oracle_solution(oracle):
+    # tests/golden/config2_oracle.npz (make_config2.py): the FP64 oracle's CG
+    # solution of the 65,536-particle sphere and its Kelvin force.  Pin it
+    # here on a sample: the fixed-point residual b - Hext - c G b at 64
+    # particles (G over all N in FP64), and the force at 16.
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "config2_oracle.npz"))
+    pos = z["pos"].astype(np.float64)
+    b = z["b"].astype(np.float64)
+    c = float(z["volume"]) * float(z["chi"]) / (1.0 + float(z["chi"]))
+    h = float(z["h"])
+    assert len(pos) == 65536 and float(z["rel_res"]) < 1e-10
+    idx = np.random.default_rng(5).choice(len(pos), 64, replace=False)
+    hext = np.tile(z["H0"], (64, 1))
+    r = b[idx] - hext - c * oracle.field(pos[idx], pos, b, h)
+    assert np.linalg.norm(r) / np.linalg.norm(hext) < 1e-7  # float32 storage of b: ~1e-7
+    jdx = idx[:16]
+    T = oracle.tensor_sum(pos[jdx], pos, c * b, h).reshape(-1, 3, 3)
+    F = np.einsum("icr,ic->ir", T, c * b[jdx])
+    assert rel(z["F"][jdx], F) < 1e-6
