@@ -17,8 +17,18 @@ Printed (rank 0, one JSON line):
   roofline   FP32 FMA roofline of the dominant pair kernel: algorithmic FLOP
              (32 per ordered field pair, 53 per ordered force pair; for a
              product evaluated once per unordered pair, 49 / 55 per unordered
-             pair) / its event-timed device time, against a dense-FFMA
-             throughput measured in this run
+             pair) / its event-timed device time, against the FP32 peak
+             SMs x 128 lanes x 2 FLOP x max SM clock (a dense-FFMA probe
+             measured in this run is reported beside it)
+  errors     M, B/mu0 and the Kelvin force of a cold solve of the same scene
+             against the FP64 oracle's solution over all particles
+             (tests/golden/config2_oracle.npz)
+  batched_vs_plain, served_vs_plain
+             the spec comparison: 256 scenes of 512..32,768 particles
+             stepped in one launch per stage against the same scenes one at a
+             time; a Poisson stream of scenes of 1,024..262,144 particles
+             served with continuous batching against the same arrivals one
+             request at a time (pairs/s and p50/p99 step and request latency)
   cpu_baseline  the CPU restatement of the reference's pair kernels (FP32,
              OpenMP over all host cores) on a bounded sample of the same step
 
@@ -72,10 +82,19 @@ BODY_BOUND = {"allpairs_kernel<field>": 64.0 / 76.0, "allpairs_kernel<force>": 1
               "k_sym<field>": 98.0 / 120.0, "k_sym<force>": 110.0 / 156.0}
 
 
-def pair_roofline(kf, kg, peak, n):
+def fp32_peak(sm_max_mhz):
+    """Nominal FP32 FMA peak of device 0 in TFLOP/s: SMs x 128 FP32 lanes x 2
+    FLOP per FMA x the maximum SM clock (nvidia-smi clocks.max.sm)."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_max_mhz or 2070.0
+    return sms * 128 * 2 * mhz * 1e6 / 1e12, sms, mhz
+
+
+def pair_roofline(kf, kg, peak, n, probe=None):
     """Roofline of the dominant pair product of a timed run from the handle's
     kernel statistics (field kf, force kg): per product its algorithmic
-    TFLOP/s, fraction of the measured FFMA peak and of its body's ceiling."""
+    TFLOP/s, fraction of the FP32 peak and of its body's ceiling."""
     kern = {}
     names = {}
     for name, st in (("field", kf), ("force", kg)):
@@ -102,7 +121,9 @@ def pair_roofline(kf, kg, peak, n):
     return {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
             "frac": round(ach / peak, 4), "traffic": traffic, "kernel": names[dom],
             "frac_of_body_bound": kern[dom]["frac_of_body_bound"],
-            "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
+            "peak_source": "SMs x 128 FP32 lanes x 2 FLOP x max SM clock (nvidia-smi clocks.max.sm)",
+            "probe_tflops": round(probe, 3) if probe else None,
+            "frac_of_probe": round(ach / probe, 4) if probe else None,
             "kernels": kern,
             "note": "pairwise sums are not a contraction: FP32 FMA pipe, not tensor cores. "
                     "Algorithmic FLOP: 32 per ordered field pair, 53 per ordered force pair; for a product "
@@ -139,6 +160,11 @@ def parse():
                          "jittered-lattice cylinder through the FMM (P=8, theta=0.5)")
     ap.add_argument("--fmm-order", type=int, default=8)
     ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--rel-tol", type=float, default=1e-6, help="CG relative residual tolerance of every solve")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="default workload: skip the batched-vs-plain and served-vs-plain comparisons")
+    ap.add_argument("--compare-steps", type=int, default=5,
+                    help="default workload: timed batched timesteps of the batched-vs-plain comparison")
     return ap.parse_args()
 
 
@@ -291,7 +317,7 @@ def run_ours(args, rank, world, local):
     n = sc.n
     s = mfgb.Solver(n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
     s.set_option("solver", mfgb.SOLVER_CG)
-    s.set_option("rel_tol", 1e-6)
+    s.set_option("rel_tol", args.rel_tol)
     s.set_option("kernel_timing", 1)
 
     # cold solve (reported) + warm-up steps
@@ -333,12 +359,18 @@ def run_ours(args, rank, world, local):
     value = pairs_all / (t_max * 1e-3)
 
     # dominant pair kernel and its FP32 roofline
-    roofline = pair_roofline(kf, kg, mfgb.probe_fp32_peak(), n)
+    peak, sms, mhz = fp32_peak(clk.get("sm_max_mhz"))
+    roofline = pair_roofline(kf, kg, peak, n, probe=mfgb.probe_fp32_peak())
+    roofline["peak_inputs"] = {"sms": sms, "sm_max_mhz": mhz}
 
-    # accuracy on a sample: fixed-point residual and force, FP64 oracle
+    # accuracy: a cold solve of the same scene against the FP64 oracle's
+    # solution over all particles, and the final state's fixed-point residual
+    # and force on a sample (FP64 oracle sums over all N)
     errors = None
     if rank == 0:
-        errors = sample_errors(s, sc)
+        errors = {"final_state_sample": sample_errors(s, sc)}
+        if n == 65536:
+            errors.update(config2_errors(args, local))
 
     # end to end through the public API with host buffers
     e2e = None
@@ -355,6 +387,13 @@ def run_ours(args, rank, world, local):
         cpu = {"value": (fp + gp) / cpu_time, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
                "sample": sample + "; value = the timed step's field/force pair mix at these rates",
                "field_pairs_per_s": rf, "force_pairs_per_s": rg}
+    s.close()
+
+    # the spec comparison: batched and served against plain
+    batched = served = None
+    if not args.no_compare and n == 65536:
+        batched = measure_batch(args, rank, world, local, steps=args.compare_steps, plain_passes=1)
+        served = measure_served(args, rank, world, local)
 
     if rank == 0:
         out = {
@@ -362,21 +401,57 @@ def run_ours(args, rank, world, local):
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded jittered-lattice sphere (the reference ships no dataset)",
-            "config": {"workload": f"allpairs_fp32_{n}: jittered lattice sphere r=0.5, N={n}, h=2*spacing="
-                                   f"{sc.h:.5f}, chi=2, H0=(0,0,1), dt={args.dt}, CG rel tol 1e-6",
-                       "N": n, "step": "one timestep: warm-started CG solve + Kelvin force + symplectic Euler",
-                       "l2": "flushed before every timed step (256 MiB write, not timed)",
-                       "parallelism": f"replicas x{world}"},
+            "config": config_allpairs(n, sc.h, args),
             "field_pairs": ctr["field_pairs"], "force_pairs": ctr["force_pairs"],
             "solve_iters_per_step": iters, "step_ms": [round(v, 4) for v in step_ms],
             "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
             "gpu_launches": ctr["kernel_launches"],
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "errors": errors, "clocks": clk,
+            "batched_vs_plain": summarize_batch(batched) if batched else None,
+            "served_vs_plain": summarize_served(served) if served else None,
             "autotune": mfgb.autotune_report(),
         }
         print(json.dumps(out), flush=True)
+
+
+def config_allpairs(n, h, args):
+    """The default workload's config, shared by both arms of the bench."""
+    return {"workload": f"allpairs_fp32_{n}: jittered lattice sphere r=0.5, N={n}, h=2*spacing={h:.5f}, chi=2, "
+                        f"H0=(0,0,1), dt={args.dt}, CG rel tol {args.rel_tol:g}",
+            "N": n, "step": "one timestep: warm-started CG solve + Kelvin force + symplectic Euler",
+            "l2": "flushed before every timed step (256 MiB write, not timed)",
+            "parallelism": f"replicas x{int(os.environ.get('WORLD_SIZE', '1'))}"}
+
+
+def config2_errors(args, local):
+    """A fresh handle at the fixture's positions (the same scene), solved cold
+    to the bench's tolerance, its force evaluated: relative L2 of B/mu0, M and
+    F over all particles against the FP64 oracle's solution, read from the
+    committed fixture (oracle CG to a relative residual of 6e-12)."""
+    import mfgb
+    path = os.path.join(ROOT, "tests", "golden", "config2_oracle.npz")
+    if not os.path.exists(path):
+        return {"oracle_solution": "fixture missing"}
+    z = np.load(path)
+    pos = z["pos"]
+    s = mfgb.Solver(len(pos), float(z["h"]), float(z["h"]), float(z["volume"]), float(z["chi"]), z["H0"], None,
+                    None, pos, device=local)
+    s.set_option("solver", mfgb.SOLVER_CG)
+    s.set_option("rel_tol", args.rel_tol)
+    it, rr = s.solve(500)
+    s.evaluate_fitted_near_foece()
+    c = float(z["volume"]) * float(z["chi"]) / (1.0 + float(z["chi"]))
+    b = z["b"].astype(np.float64)
+    rel = lambda a, w: float(np.linalg.norm(np.asarray(a, np.float64) - w) / np.linalg.norm(w))  # noqa: E731
+    out = {"B_rel_l2": rel(s.total_B_over_mu0, b), "M_rel_l2": rel(s.M, c * b),
+           "F_rel_l2": rel(s.magnetic_bodyforce, z["F"].astype(np.float64)),
+           "over": f"all {len(pos)} particles x 3 components",
+           "against": f"FP64 oracle CG solution (rel res {float(z['rel_res']):.1e}) and its Kelvin force "
+                      "(tests/golden/config2_oracle.npz)",
+           "solve": {"iters": int(it), "rel_res": float(rr), "rel_tol": args.rel_tol}}
     s.close()
+    return out
 
 
 def sample_errors(s, sc, k: int = 256):
@@ -435,8 +510,13 @@ def run_reference(args, rank, world):
     The reference sources are not present where this runs, so the port stands
     in for them (the port is bit-identical to the reference's FP32 field
     kernel and within 2e-6 on the force tensor, pinned by tests/test_oracle.py).
-    Each step is a bounded sample: 1024 field targets and 128 force targets
-    against all N sources; value = executed pairs / wall time."""
+    Same scene, metric and config as the GPU arm, and the same work mix: the
+    GPU's timed step evaluates one field product and one force product over
+    all N^2 pairs, so each CPU step is a bounded sample of both, the same
+    number of targets for each (1:1), against all N sources, with the
+    dipoles of the solved magnetization (M = c b of the FP64 oracle's
+    solution of this scene, tests/golden/config2_oracle.npz); value =
+    executed pairs / wall time."""
     if rank != 0:
         return
     import oracle as orc
@@ -444,17 +524,25 @@ def run_reference(args, rank, world):
     sc = scenes.config_allpairs_65k() if args.n == 65536 else scenes.jittered_lattice(args.n, "sphere", 0.5, chi=2.0)
     o = orc.Oracle()
     n = sc.n
-    rng = np.random.default_rng(1)
-    mom = (rng.normal(size=(n, 3)) * sc.volume).astype(np.float32)
-    nf, ng = 1024, 128
+    path = os.path.join(ROOT, "tests", "golden", "config2_oracle.npz")
+    if n == 65536 and os.path.exists(path):
+        z = np.load(path)
+        pos = np.ascontiguousarray(z["pos"], np.float32)
+        mom = (sc.c * z["b"].astype(np.float64)).astype(np.float32)
+        dipoles = "M = c b of the FP64 oracle's solution of this scene"
+    else:
+        pos = sc.pos
+        rng = np.random.default_rng(1)
+        mom = ((np.array([0.0, 0.0, 1.0]) + 0.1 * rng.normal(size=(n, 3))) * sc.c).astype(np.float32)
+        dipoles = "seeded moments c (H0 + 0.1 N(0,1))"
+    nt = 256
 
     def step(k):
-        i0 = (k * nf) % n
-        idx = np.arange(i0, i0 + nf) % n
-        o.field(sc.pos[idx], sc.pos, mom, sc.h, prec=32)
-        jdx = np.arange(i0, i0 + ng) % n
-        o.tensor_sum(sc.pos[jdx], sc.pos, mom, sc.h, prec=32)
-        return (nf + ng) * n
+        i0 = (k * nt) % n
+        idx = np.arange(i0, i0 + nt) % n
+        o.field(pos[idx], pos, mom, sc.h, prec=32)
+        o.tensor_sum(pos[idx], pos, mom, sc.h, prec=32)
+        return 2 * nt * n
 
     for k in range(args.warmup):
         step(k)
@@ -465,22 +553,22 @@ def run_reference(args, rank, world):
     dt = time.perf_counter() - t0
     value = pairs / dt
     cores = cpu_threads()
+    sample = (f"{nt} field targets + {nt} force-tensor targets x {n} sources per step (the GPU step's 1:1 "
+              f"field:force pair mix), {dipoles}, FP32, OpenMP {cores} threads")
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
            "data": "synthetic: seeded jittered-lattice sphere (the reference ships no dataset)",
-           "config": {"workload": f"allpairs_fp32_{n}: jittered lattice sphere r=0.5, N={n}, chi=2, H0=(0,0,1)",
-                      "N": n, "step": f"sample: {nf} field targets + {ng} force-tensor targets x {n} sources"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{nf}+{ng} targets x {n} sources per step, FP32, OpenMP {cores} threads"},
+           "config": config_allpairs(n, sc.h, args),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
-def run_batch(args, rank, world, local):
+def measure_batch(args, rank, world, local, steps, plain_passes):
     """Batched scenes (one launch per stage for all, graph-captured timesteps)
     against the plain path (each scene through its own solver, one after the
-    other), same scenes, kernels, tolerance and step."""
+    other), same scenes, kernels, tolerance and step.  Returns the record."""
     import torch
     import mfgb
     import scenes
@@ -491,19 +579,19 @@ def run_batch(args, rank, world, local):
     gen_s = time.perf_counter() - t0
     n_tot = sum(s.n for s in scs)
     b = mfgb.Batch(scs, device=local)
-    cold_it, cold_res = b.solve(500, 1e-6)
-    b.advance(args.dt, args.warmup, iters_per_step=4, rel_tol=1e-6, graph=True)
+    cold_it, cold_res = b.solve(500, args.rel_tol)
+    b.advance(args.dt, max(3, args.warmup), iters_per_step=4, rel_tol=args.rel_tol, graph=True)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     b.reset_counters()
     clocks = ClockSampler(local)
     barrier(world)
     clocks.start()
     step_ms = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        b.advance(args.dt, 1, iters_per_step=4, rel_tol=1e-6, graph=True)
+        b.advance(args.dt, 1, iters_per_step=4, rel_tol=args.rel_tol, graph=True)
         step_ms.append((time.perf_counter() - t) * 1e3)
     barrier(world)
     clk = clocks.stop()
@@ -513,13 +601,14 @@ def run_batch(args, rank, world, local):
     total_ms = sum(step_ms)
     t_max = allreduce_max(total_ms, world)
     value = allreduce_sum(pairs, world) / (t_max * 1e-3)
+    b.close()
 
     # plain path: the same scenes one at a time through the single-scene solver
     solvers = []
     for sc in scs:
         s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
         s.set_option("solver", mfgb.SOLVER_CG)
-        s.set_option("rel_tol", 1e-6)
+        s.set_option("rel_tol", args.rel_tol)
         s.solve(500)
         s.advance(args.dt, 500)
         s.reset_counters()
@@ -527,41 +616,67 @@ def run_batch(args, rank, world, local):
     torch.cuda.synchronize()
     plain_ms = 0.0
     plain_pairs = 0.0
-    for _ in range(max(1, min(args.steps, 3))):
+    plain_steps = []
+    for _ in range(plain_passes):
+        t_pass = 0.0
         for s in solvers:
-            t = time.perf_counter()
-            s.advance(args.dt, 500)
+            flush.zero_()
             torch.cuda.synchronize()
-            plain_ms += (time.perf_counter() - t) * 1e3
+            t = time.perf_counter()
+            s.advance(args.dt, 4)
+            torch.cuda.synchronize()
+            t_pass += (time.perf_counter() - t) * 1e3
+        plain_steps.append(t_pass)
+        plain_ms += t_pass
     for s in solvers:
         cc = s.counters()
         plain_pairs += cc["field_pairs"] + cc["force_pairs"]
         s.close()
     plain_value = plain_pairs / (plain_ms * 1e-3)
+    return {
+        "value": value, "ms_per_step": t_max / steps, "steps": steps,
+        "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+        "step_ms": [round(v, 3) for v in step_ms],
+        "field_pairs": c["field_pairs"], "force_pairs": c["force_pairs"], "gpu_launches": c["kernel_launches"],
+        "cold_solve": {"max_iters": cold_it, "worst_rel_res": cold_res},
+        "worst_rel_res_last_step": float(np.max(rr)), "max_iters_last_step": float(np.max(its)),
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / plain_passes,
+                  "passes": plain_passes, "path": "one mf_solver per scene, scenes one after the other, "
+                                                  "L2 flushed before each scene's step"},
+        "batched_over_plain": value / plain_value,
+        "scenes": len(scs), "particles": n_tot, "scene_generation_s": round(gen_s, 1), "clocks": clk,
+        "config": {"workload": f"batch{len(scs)}: {len(scs)} scenes, N log-uniform in [512, 32768] "
+                               f"(total {n_tot}), radius U(0.2,0.5), chi U(0.5,3), H0 random unit, dt={args.dt}, "
+                               f"CG rel tol {args.rel_tol:g}, <= 4 CG iterations per step, one CUDA graph per "
+                               "timestep", "scenes": len(scs), "particles": n_tot,
+                   "l2": "flushed before every timed step (256 MiB write, not timed)"},
+    }
+
+
+def summarize_batch(r):
+    """The batched-vs-plain comparison as carried on the default line."""
+    return {"batched": {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms_per_step"],
+                        "p50_step_ms": r["p50_step_ms"], "p99_step_ms": r["p99_step_ms"], "steps": r["steps"],
+                        "gpu_launches": r["gpu_launches"], "max_iters_last_step": r["max_iters_last_step"]},
+            "plain": {"value": r["plain"]["value"], "unit": UNIT, "ms_per_step": r["plain"]["ms_per_step"],
+                      "passes": r["plain"]["passes"]},
+            "ratio": r["batched_over_plain"], "config": r["config"], "clocks": r["clocks"]}
+
+
+def run_batch(args, rank, world, local):
+    import mfgb
+    r = measure_batch(args, rank, world, local, steps=args.steps, plain_passes=max(1, min(args.steps, 3)))
     if rank == 0:
         out = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded jittered-lattice spheres (the reference ships no dataset)",
-            "config": {"workload": f"batch{len(scs)}: {len(scs)} scenes, N log-uniform in [512, 32768] "
-                                   f"(total {n_tot}), radius U(0.2,0.5), chi U(0.5,3), H0 random unit, dt={args.dt}, "
-                                   "CG rel tol 1e-6, <= 4 CG iterations per step, one CUDA graph per timestep",
-                       "scenes": len(scs), "particles": n_tot,
-                       "l2": "flushed before every timed step (256 MiB write, not timed)"},
-            "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-            "step_ms": [round(v, 3) for v in step_ms],
-            "field_pairs": c["field_pairs"], "force_pairs": c["force_pairs"], "gpu_launches": c["kernel_launches"],
-            "cold_solve": {"max_iters": cold_it, "worst_rel_res": cold_res},
-            "worst_rel_res_last_step": float(np.max(rr)), "max_iters_last_step": float(np.max(its)),
-            "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / max(1, min(args.steps, 3)),
-                      "path": "one mf_solver per scene, scenes one after the other"},
-            "batched_over_plain": value / plain_value,
-            "scene_generation_s": round(gen_s, 1), "clocks": clk,
+            "config": r["config"],
             "autotune": mfgb.autotune_report(),
         }
+        out.update({k: v for k, v in r.items() if k not in ("value", "ms_per_step", "config", "steps")})
         print(json.dumps(out), flush=True)
-    b.close()
 
 
 def run_plain_fp64(args, rank, world, local):
@@ -606,23 +721,11 @@ def run_plain_fp64(args, rank, world, local):
     s.close()
 
 
-def run_served(args, rank, world, local):
-    """Served stream: Poisson arrivals (seeded) of scenes with N log-uniform
-    in [1024, 262144] and the batched config's per-scene distributions, 20
-    timesteps each, continuous batching under a 120 GB budget.  Scenes up to
-    65,536 particles join the all-pairs batch; larger ones run through the
-    FMM (P = 6), each on its own host thread and stream beside the batch.
-    The mean rate is --rate, or by default 80 % of the served capacity,
-    measured first by submitting every request at once.  Pairs are executed
-    pairs for batch members and effective pairs (N^2 per product) for FMM
-    scenes.  Reports p50/p99 per step, per tick and per request and aggregate
-    pairs/s, beside the plain path on the same arrivals (run_served_plain)."""
+def served_requests(args, rank):
+    """The served stream's requests (seeded): N log-uniform in [1024, 262144],
+    the batched config's per-scene distributions."""
     import math
-    import torch
-    import mfgb
     import scenes
-
-    torch.cuda.set_device(local)
     rng = np.random.default_rng(99 + rank)
     reqs = []
     for k in range(args.requests):
@@ -632,12 +735,34 @@ def run_served(args, rank, world, local):
         H /= np.linalg.norm(H)
         reqs.append(scenes.jittered_lattice(n, "sphere", radius=float(r2.uniform(0.2, 0.5)),
                                             chi=float(r2.uniform(0.5, 3.0)), seed=5000 + k, H0=tuple(H)))
-    gaps = rng.exponential(1.0, size=len(reqs))  # unit-rate Poisson gaps, scaled by the rate below
+    gaps = rng.exponential(1.0, size=len(reqs))  # unit-rate Poisson gaps, scaled by the rate
+    return reqs, gaps
+
+
+def measure_served(args, rank, world, local):
+    """Served stream: Poisson arrivals (seeded) of scenes with N log-uniform
+    in [1024, 262144] and the batched config's per-scene distributions, 20
+    timesteps each, continuous batching under a 120 GB budget.  Scenes up to
+    65,536 particles join the all-pairs batch; larger ones run as their own
+    solver handle (field products through the FMM, the force as the handle's
+    automatic choice picks it), each on its own host thread and stream beside
+    the batch.  The mean rate is --rate, or by default 80 % of the served
+    capacity, measured first by submitting every request at once.  Pairs are
+    executed pairs for batch members and effective pairs (N^2 per product) for
+    FMM products.  Reports p50/p99 per step, per tick and per request and
+    aggregate pairs/s, beside the plain path on the same arrivals
+    (run_served_plain)."""
+    import torch
+    import mfgb
+    import scenes
+
+    torch.cuda.set_device(local)
+    reqs, gaps = served_requests(args, rank)
     capacity = None
     if args.rate <= 0:
         # Capacity: every request submitted at once, served to the last one.
         srv = mfgb.Server(hbm_budget_bytes=120e9, max_active=64, steps_per_request=20, iters_per_step=4,
-                          rel_tol=1e-6, dt=args.dt, device=local)
+                          rel_tol=args.rel_tol, dt=args.dt, device=local)
         t0 = time.perf_counter()
         cids = [srv.submit(r) for r in reqs]
         while any(srv.poll(i)[0] != 2 for i in cids):
@@ -649,7 +774,7 @@ def run_served(args, rank, world, local):
         rate = args.rate
     arrivals = np.cumsum(gaps / rate)
     srv = mfgb.Server(hbm_budget_bytes=120e9, max_active=64, steps_per_request=20, iters_per_step=4,
-                      rel_tol=1e-6, dt=args.dt, device=local)
+                      rel_tol=args.rel_tol, dt=args.dt, device=local)
     # warm-up request (kernel load, first allocations), not measured
     wid = srv.submit(scenes.jittered_lattice(2048, "sphere", 0.3, chi=1.0, seed=1))
     while srv.poll(wid)[0] != 2:
@@ -680,44 +805,75 @@ def run_served(args, rank, world, local):
     steps_all = np.concatenate([srv.step_times(i) for i in ids])
     steps_fmm = np.concatenate([srv.step_times(ids[k]) for k in big]) if big else np.zeros(0)
     steps_batch = np.concatenate([srv.step_times(ids[k]) for k in range(len(reqs)) if k not in big])
-    pct = lambda v, q: float(np.percentile(v, q)) if len(v) else None
+    pct = lambda v, q: float(np.percentile(v, q)) if len(v) else None  # noqa: E731
     srv.close()
     plain = run_served_plain(reqs, arrivals, args, local) if (rank == 0 and not args.no_plain) else None
+    ns = [r.n for r in reqs]
+    return {
+        "value": pairs / wall, "unit": UNIT,
+        "requests": len(reqs), "rate_per_s": rate,
+        "rate_basis": ("80 % of the measured served capacity" if capacity else "given"),
+        "capacity_req_per_s": capacity, "n_range": [min(ns), max(ns)], "n_mean": float(np.mean(ns)),
+        "wall_s": wall, "busy_s": (s1["busy_ms"] - s0["busy_ms"]) / 1e3,
+        "p50_step_ms": pct(steps_all, 50), "p99_step_ms": pct(steps_all, 99),
+        "step_ms_by_path": {"batch": {"steps": len(steps_batch), "p50": pct(steps_batch, 50),
+                                      "p99": pct(steps_batch, 99)},
+                            "fmm": {"steps": len(steps_fmm), "p50": pct(steps_fmm, 50), "p99": pct(steps_fmm, 99)}},
+        "p50_tick_ms": float(np.percentile(tick_ms, 50)) if tick_ms else None,
+        "p99_tick_ms": float(np.percentile(tick_ms, 99)) if tick_ms else None,
+        "p50_request_ms": float(np.percentile(lat, 50)), "p99_request_ms": float(np.percentile(lat, 99)),
+        "ticks": s1["ticks"] - s0["ticks"], "rebatches": s1["rebatches"] - s0["rebatches"],
+        "pairs": pairs, "budget_bytes": 120e9, "clocks": clk, "plain": plain,
+        "note": "N <= 65,536: all-pairs batch (executed pairs); N > 65,536: own solver handle on its own host "
+                "thread and stream, field products through the FMM (P=8, effective pairs), the force all-pairs "
+                "up to 196,608 particles and through the FMM above; 20 timesteps per request, <= 4 CG "
+                "iterations per step; step latency: per request timestep (batch members: their tick until the "
+                "step was done on the device; others: each timestep on their thread); tick: serving-loop "
+                "ticks in which the batch took a timestep",
+    }
+
+
+def summarize_served(r):
+    """The served-vs-plain comparison as carried on the default line."""
+    keys = ("value", "unit", "p50_step_ms", "p99_step_ms", "p50_request_ms", "p99_request_ms")
+    out = {"served": {k: r[k] for k in keys}, "plain": None, "ratio": None,
+           "requests": r["requests"], "rate_per_s": r["rate_per_s"], "rate_basis": r["rate_basis"],
+           "capacity_req_per_s": r["capacity_req_per_s"], "n_range": r["n_range"],
+           "p50_tick_ms": r["p50_tick_ms"], "p99_tick_ms": r["p99_tick_ms"],
+           "step_ms_by_path": r["step_ms_by_path"], "clocks": r["clocks"], "note": r["note"]}
+    if r["plain"]:
+        out["plain"] = {k: r["plain"][k] for k in keys}
+        out["plain"]["capacity_req_per_s"] = r["plain"]["capacity_req_per_s"]
+        out["ratio"] = r["value"] / r["plain"]["value"]
+        if r["capacity_req_per_s"]:
+            out["capacity_ratio"] = r["capacity_req_per_s"] / r["plain"]["capacity_req_per_s"]
+    return out
+
+
+def run_served(args, rank, world, local):
+    r = measure_served(args, rank, world, local)
     if rank == 0:
-        ns = [r.n for r in reqs]
-        print(json.dumps({
-            "metric": METRIC, "workload": "served", "value": pairs / wall, "unit": UNIT,
-            "requests": len(reqs), "rate_per_s": rate,
-            "rate_basis": ("80 % of the measured served capacity" if capacity else "given"),
-            "capacity_req_per_s": capacity, "n_range": [min(ns), max(ns)], "n_mean": float(np.mean(ns)),
-            "wall_s": wall, "busy_s": (s1["busy_ms"] - s0["busy_ms"]) / 1e3,
-            "p50_step_ms": pct(steps_all, 50), "p99_step_ms": pct(steps_all, 99),
-            "step_ms_by_path": {"batch": {"steps": len(steps_batch), "p50": pct(steps_batch, 50),
-                                          "p99": pct(steps_batch, 99)},
-                                "fmm": {"steps": len(steps_fmm), "p50": pct(steps_fmm, 50), "p99": pct(steps_fmm, 99)}},
-            "p50_tick_ms": float(np.percentile(tick_ms, 50)), "p99_tick_ms": float(np.percentile(tick_ms, 99)),
-            "p50_request_ms": float(np.percentile(lat, 50)), "p99_request_ms": float(np.percentile(lat, 99)),
-            "ticks": s1["ticks"] - s0["ticks"], "rebatches": s1["rebatches"] - s0["rebatches"],
-            "pairs": pairs, "budget_bytes": 120e9, "clocks": clk, "plain": plain,
-            "note": "N <= 65,536: all-pairs batch (executed pairs); N > 65,536: FMM P=6 on its own host thread "
-                    "and stream (effective pairs); 20 timesteps per request, <= 4 CG iterations per step; "
-                    "step latency: per request timestep (batch members: their tick until the step was done "
-                    "on the device; FMM requests: each timestep on their thread); tick: serving-loop ticks in "
-                    "which the batch took a timestep"}),
-            flush=True)
+        out = {"metric": METRIC, "workload": "served"}
+        out.update(r)
+        print(json.dumps(out), flush=True)
 
 
 def run_served_plain(reqs, arrivals, args, local):
     """The plain path on the served stream: the same requests, in arrival
-    order, one at a time through their own solver handle (all-pairs up to
-    65,536 particles, FMM P = 6 above, CG to the same tolerance, the same 20
-    timesteps of <= 4 iterations).  Each request's service time (handle
-    creation, cold solve, timesteps, read-back) is measured on the GPU; the
-    queue is replayed on those times with the served run's arrival times
-    (a request starts when it has arrived and the previous one is done)."""
+    order, one at a time through their own solver handle (the same automatic
+    choice of FMM or all-pairs per product as the served requests, CG to the
+    same tolerance, the same 20 timesteps of <= 4 iterations).  Each request's
+    service time (handle creation, cold solve, timesteps, read-back) is
+    measured on the GPU; the queue is replayed on those times with the served
+    run's arrival times (a request starts when it has arrived and the previous
+    one is done).  Handles of every request are created once beforehand, so
+    the autotuner's first timings (cached per process) are not charged to the
+    plain path."""
     import torch
     import mfgb
 
+    for sc in reqs:
+        mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local).close()
     step_ms, lat_ms = [], []
     pairs = 0.0
     busy = 0.0
@@ -728,10 +884,7 @@ def run_served_plain(reqs, arrivals, args, local):
         t0 = time.perf_counter()
         s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
         s.set_option("solver", mfgb.SOLVER_CG)
-        s.set_option("rel_tol", 1e-6)
-        if sc.n > 65536:
-            s.set_option("fmm", mfgb.FMM_ON)
-            s.set_option("fmm_order", 6)
+        s.set_option("rel_tol", args.rel_tol)
         s.solve(500)
         for _ in range(20):
             torch.cuda.synchronize()
@@ -750,6 +903,7 @@ def run_served_plain(reqs, arrivals, args, local):
         lat_ms.append((done_at - float(arrivals[k])) * 1e3)
     makespan = done_at - t_first
     return {"value": pairs / makespan, "unit": UNIT, "makespan_s": makespan, "busy_s": busy,
+            "capacity_req_per_s": len(reqs) / busy,
             "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
             "p50_request_ms": float(np.percentile(lat_ms, 50)), "p99_request_ms": float(np.percentile(lat_ms, 99)),
             "path": "one solver handle per request, requests one after the other in arrival order; queue "
@@ -759,7 +913,8 @@ def run_served_plain(reqs, arrivals, args, local):
 def run_fmm(args, rank, world, local):
     """Config 3: N = 1,048,576 jittered-lattice cylinder (r = 0.3, height 1,
     h = 2 spacings, chi = 1.5, H0 = (0,0,1)) through the FMM (P = 8, theta =
-    0.5, leaf boxes of >= 64 particles).  A step is one timestep as in the
+    0.5 for the field products and 0.3 for the Kelvin force, leaf boxes of
+    >= 64 particles).  A step is one timestep as in the
     headline workload.  value counts effective pairs (N^2 per product, the FMM
     convention); executed near-field pairs are reported beside it.  Errors:
     against the FP64 oracle on 2,048 seeded targets (CPU) and against the FP32
@@ -773,7 +928,7 @@ def run_fmm(args, rank, world, local):
     n = sc.n
     s = mfgb.Solver(n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
     s.set_option("solver", mfgb.SOLVER_CG)
-    s.set_option("rel_tol", 1e-6)
+    s.set_option("rel_tol", args.rel_tol)
     s.set_option("fmm", mfgb.FMM_ON)
     s.set_option("fmm_order", args.fmm_order)
     s.set_option("fmm_theta", 0.5)
@@ -814,7 +969,8 @@ def run_fmm(args, rank, world, local):
     value = pairs / (t_max * 1e-3)
     executed = (st["field_products"] + st["force_products"]) * st["p2p_pairs"]
 
-    peak = mfgb.probe_fp32_peak()
+    peak, _, _ = fp32_peak(clk.get("sm_max_mhz"))
+    probe = mfgb.probe_fp32_peak()
     kern = {}
     for name, fpp, fpu in (("fmm_near_field", FLOP_FIELD_PAIR, FLOP_FIELD_UPAIR),
                            ("fmm_near_force", FLOP_FORCE_PAIR, FLOP_FORCE_UPAIR)):
@@ -838,7 +994,8 @@ def run_fmm(args, rank, world, local):
                 "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": traffic,
                 "kernel": ("k_fmm_near_sym + k_fmm_p2p<force>" if kern[dom].get("once_per_box_pair")
                            else f"k_fmm_p2p<{'force' if dom.endswith('force') else 'field'}>"),
-                "peak_source": "measured in this run: dense FFMA chains on all SMs (mf_probe_fp32_peak)",
+                "peak_source": "SMs x 128 FP32 lanes x 2 FLOP x max SM clock (nvidia-smi clocks.max.sm)",
+                "probe_tflops": round(probe, 3),
                 "kernels": kern,
                 "far_field": {"launches": far["launches"], "total_ms": round(far["total_ms"], 4),
                               "m2l_per_product": st["m2l_per_product"]},
@@ -888,7 +1045,7 @@ def run_fmm(args, rank, world, local):
             "data": "synthetic: seeded jittered-lattice cylinder (the reference ships no dataset)",
             "config": {"workload": f"fmm_fp32_{n}: jittered lattice cylinder r=0.3 height 1, N={n}, "
                                    f"h=2*spacing={sc.h:.5f}, chi=1.5, H0=(0,0,1), FMM P={args.fmm_order} "
-                                   f"theta=0.5 leaf>=64, dt={args.dt}, CG rel tol 1e-6",
+                                   f"theta=0.5 (force 0.3) leaf>=64, dt={args.dt}, CG rel tol {args.rel_tol:g}",
                        "N": n, "step": "one timestep: octree rebuild, warm-started CG solve (FMM products), "
                                        "Kelvin force (FMM), symplectic Euler",
                        "l2": "flushed before every timed step (256 MiB write, not timed)",
