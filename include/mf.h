@@ -315,6 +315,15 @@ mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h
 /* Frees the scratch the mf_direct_* calls keep per device. */
 mf_status mf_release_scratch(void);
 
+/* Debug (off by default; not in the reference, whose kernels check nothing,
+ * cuda_abstract_vector.cuh:169-175): the staging waits of the all-pairs and
+ * once-per-pair kernels launched from now on give up after `limit` try-waits
+ * (0: at once), so the bounded-wait error path can be exercised: the launch
+ * reports MF_ERR_TIMEOUT, its copies in flight are drained with the default
+ * bound before each CTA leaves, and the scratch is reset for the next call.
+ * limit < 0 restores the default bound.  Process-wide. */
+mf_status mf_debug_stage_wait_limit(int64_t limit);
+
 /* ---------------------------------------------------------------------- */
 /* FMM matrix over a source set and a target set: the replacement of       */
 /* fmmtl::kernel_matrix<DipoleBSpherical>(kernel, sources, targets) and    */

@@ -275,6 +275,7 @@ struct Launcher {
     a.partials = partials;
     a.counters = counters;
     a.err = err;
+    a.stage_wait_debug = stage_wait_debug();
     kernel()<<<unsigned(g), C::TPB, kSmem, st>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "allpairs_kernel launch");
@@ -531,6 +532,12 @@ Tune default_tune_mode() {
 }
 
 void set_thread_tune_mode(int mode) { t_tune_override = mode; }
+
+namespace {
+std::atomic<uint32_t> g_stage_wait_debug{0};
+}
+uint32_t stage_wait_debug() { return g_stage_wait_debug.load(std::memory_order_relaxed); }
+void set_stage_wait_debug(uint32_t v) { g_stage_wait_debug.store(v, std::memory_order_relaxed); }
 
 int default_shape(Body body, const std::vector<SceneSpec>& specs, bool allow_sym) {
   return allow_sym && body == Body::ForceF2 && sym_eligible(body, specs) ? kShapeSym : 0;

@@ -82,6 +82,9 @@ struct AllPairsArgs {
   double* partials;    // [grid][2][TPB*TPT][kOut]
   int32_t* counters;   // [total target blocks], zero between launches
   int32_t* err;        // device error word
+  // 0: staging waits take the default bound; k > 0: they give up after
+  // k - 1 try-waits (debug: mf_debug_stage_wait_limit; drains keep the default).
+  uint32_t stage_wait_debug;
 };
 
 // ----------------------------------------------------------------------------
@@ -559,7 +562,7 @@ __global__ void __launch_bounds__(TPB) allpairs_kernel(const AllPairsArgs<Real> 
     PairConsts<Real> pc = sc.pc;
     pc.tbl = s_fit;
 
-    const bool ok = mbar_wait_bounded(&full_bar[s], parity);
+    const bool ok = mbar_wait_bounded(&full_bar[s], parity, stage_wait_limit(a.stage_wait_debug));
     if (__syncthreads_or(!ok)) {
       k_fail = k;
       break;

@@ -66,12 +66,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar`.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it)
+// Bounded wait for phase `parity` of `bar`: at most `limit` try-waits.
+// Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+
+// Try-waits of a staging wait: the default bound, or, with the debug setting
+// a launch carries (mf_debug_stage_wait_limit), debug - 1 of them.  Drains
+// after an error always wait with the default bound.
+__device__ __forceinline__ uint32_t stage_wait_limit(uint32_t debug) { return debug ? debug - 1 : kWaitLimit; }
 
 __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");

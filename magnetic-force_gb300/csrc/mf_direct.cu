@@ -5,6 +5,7 @@
 // tiles can be staged by bulk copies; that packing space, the plan table and
 // the kernel scratch live in one context per device, created on first use
 // and kept until mf_release_scratch() or process exit.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -205,6 +206,12 @@ mf_status mf_direct_force(const float* pos, const float* mom, int64_t n, float h
   if (n > 0 && !force) return fail(MF_ERR_INVALID_ARG, "NULL force");
   return direct_impl(Body::Force, pos, n, pos, mom, n, h, rext9, naive_quirks ? 1 : 0, force,
                      static_cast<cudaStream_t>(stream));
+}
+
+mf_status mf_debug_stage_wait_limit(int64_t limit) {
+  if (limit < 0) set_stage_wait_debug(0);
+  else set_stage_wait_debug(uint32_t(std::min<int64_t>(limit, int64_t(kWaitLimit)) + 1));
+  return MF_OK;
 }
 
 mf_status mf_release_scratch(void) {

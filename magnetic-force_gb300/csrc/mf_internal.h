@@ -293,6 +293,11 @@ Tune default_tune_mode();
 // this tune mode (a Tune value; -1 restores the process default).  The
 // process default MF_AUTOTUNE=0 still wins.
 void set_thread_tune_mode(int mode);
+// Debug setting carried by every all-pairs and once-per-pair launch
+// (AllPairsArgs::stage_wait_debug): 0 the default staging-wait bound, k > 0
+// staging waits give up after k - 1 try-waits.  Process-wide.
+uint32_t stage_wait_debug();
+void set_stage_wait_debug(uint32_t v);
 // Default pair-symmetric mode of new handles and batches (MF_OPT_PAIR_SYMMETRIC:
 // 0 never, 1 tuned, 2 always): 1 unless the environment sets MF_PAIR_SYMMETRIC.
 int default_sym_mode();

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(kSymTPB) k_sym(const AllPairsArgs<float> a, fl
       cur_si = si;
       cur_I = I;
     }
-    const bool ok = mbar_wait_bounded(&full_bar[s], uint32_t((u / STAGES) & 1));
+    const bool ok = mbar_wait_bounded(&full_bar[s], uint32_t((u / STAGES) & 1), stage_wait_limit(a.stage_wait_debug));
     if (__syncthreads_or(!ok)) {
       k_fail = k;
       break;
@@ -469,6 +469,7 @@ mf_status run_sym(const Plan<float>& plan, const LaunchIO<float>& io, double* pa
   a.done_count = io.done_count;
   a.done_total = io.done_total;
   a.err = err;
+  a.stage_wait_debug = stage_wait_debug();
   float* part = reinterpret_cast<float*>(partials);
   const int64_t g = std::min<int64_t>(plan.total_steps, gmax);
   const int64_t g0 = plan.host.front().t_off;

@@ -122,6 +122,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mf_direct_force_tensor": (i32, [vp, i64, vp, vp, i64, f32, vp, vp]),
         "mf_direct_force": (i32, [vp, vp, i64, f32, vp, i32, vp, vp]),
         "mf_release_scratch": (i32, []),
+        "mf_debug_stage_wait_limit": (i32, [i64]),
         "mf_get_kernel_stats": (i32, [vp, i32, ctypes.POINTER(mf_kernel_stats)]),
         "mf_probe_fp32_peak": (i32, [ctypes.POINTER(f64)]),
         "mf_get_fmm_stats": (i32, [vp, ctypes.POINTER(mf_fmm_stats)]),
