@@ -10,7 +10,9 @@ device ms per call (packing included), pairs/s and algorithmic TFLOP/s.
 
     python magnetic-force_gb300/microbench.py --kernel fmm_field --n 262144 --reps 3
 
-``fmm_field`` / ``fmm_force`` run FMM products (P = 8, theta = 0.5) on a seeded
+``fmm_field`` / ``fmm_force`` run FMM products (P = 8, theta = 0.5, the force at
+its own aperture 0.3; --pair-symmetric 2 for the force's near field once per
+unordered box pair) on a seeded
 jittered-lattice cylinder (r = 0.3, height 1) of N particles: the field
 operator G(m) through mf_apply_field, the force through mf_eval_force after a
 CG solve; per-stage device times come from the handle's event timing.
@@ -60,6 +62,8 @@ def main():
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--pair-symmetric", type=int, default=-1,
+                    help="fmm_* / engine_*: MF_OPT_PAIR_SYMMETRIC of the handle (-1: its default)")
     args = ap.parse_args()
 
     import numpy as np
@@ -115,6 +119,8 @@ def fmm(args, np, torch, mfgb, scenes):
     s.set_option("fmm", mfgb.FMM_ON)
     s.set_option("fmm_order", 8)
     s.set_option("solver", mfgb.SOLVER_CG)
+    if args.pair_symmetric >= 0:
+        s.set_option("pair_symmetric", args.pair_symmetric)
     rng = np.random.default_rng(2)
     m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.volume).astype(np.float32)
     if args.kernel == "fmm_force":
@@ -186,6 +192,8 @@ def engine(args, np, torch, mfgb, scenes):
     sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
     s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
     s.set_option("fmm", mfgb.FMM_OFF)
+    if args.pair_symmetric >= 0:
+        s.set_option("pair_symmetric", args.pair_symmetric)
     rng = np.random.default_rng(2)
     m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.volume).astype(np.float32)
     field = args.kernel == "engine_field"
