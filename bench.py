@@ -77,9 +77,9 @@ def product_flop(name, st):
 # fully busy FMA pipe, against the peak's 2 FLOP per cycle (packed f32x2
 # operations per target and pair item, counted from the bodies): the all-pairs
 # field 19 per 2 ordered pairs (64 FLOP), force 30 (106 FLOP); once per
-# unordered pair, field 30 per 2 unordered pairs (98 FLOP), force 39 (110 FLOP).
+# unordered pair, field 30 per 2 unordered pairs (98 FLOP), force 36 (110 FLOP).
 BODY_BOUND = {"allpairs_kernel<field>": 64.0 / 76.0, "allpairs_kernel<force>": 106.0 / 120.0,
-              "k_sym<field>": 98.0 / 120.0, "k_sym<force>": 110.0 / 156.0}
+              "k_sym<field>": 98.0 / 120.0, "k_sym<force>": 110.0 / 144.0}
 
 
 def fp32_peak(sm_max_mhz):
