@@ -150,6 +150,43 @@ class Oracle:
         return b, it, rr.value
 
 
+class RefFmm:
+    """The reference's own CPU FMM (fmmtl::kernel_matrix, FP64 spherical
+    expansions, OpenMP), built from its sources into _ref/libmfref_fmm.so."""
+
+    PATH = os.path.join(HERE, "_ref", "libmfref_fmm.so")
+
+    def __init__(self, path: str = PATH):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        for f in (self.lib.ref_fmm_field, self.lib.ref_fmm_hessian):
+            f.restype = ctypes.c_int
+            f.argtypes = [_i64, _p, _p, ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                          _p, _p]
+
+    @staticmethod
+    def available(path: str = PATH) -> bool:
+        return os.path.exists(path)
+
+    def _run(self, fn, cols, pos, mom, h, order, ncrit, theta, reps):
+        x = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+        m = np.ascontiguousarray(mom, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros((len(x), cols), np.float32)
+        sec = np.zeros(2, np.float64)
+        fn(_i64(len(x)), _p(_ptr(x)), _p(_ptr(m)), ctypes.c_float(h), int(order), int(ncrit), float(theta),
+           int(reps), _p(_ptr(out)), _p(_ptr(sec)))
+        return out, float(sec[0]), float(sec[1])
+
+    def field(self, pos, mom, h, order=6, ncrit=384, theta=0.5, reps=0):
+        """B/mu0 at every particle; returns (result, set-up + first product s, s per further product)."""
+        return self._run(self.lib.ref_fmm_field, 3, pos, mom, h, order, ncrit, theta, reps)
+
+    def hessian(self, pos, mom, h, order=6, ncrit=384, theta=0.5, reps=0):
+        """The force tensors [n][9] (glm column-major) at every particle."""
+        return self._run(self.lib.ref_fmm_hessian, 9, pos, mom, h, order, ncrit, theta, reps)
+
+
 class RefKernels:
     """The reference's own FMMTL kernels (FP32), built from its sources."""
 

@@ -188,3 +188,23 @@ def test_config2_fixture_is_the_oracle_solution(oracle):
     T = oracle.tensor_sum(pos[jdx], pos, c * b, h).reshape(-1, 3, 3)
     F = np.einsum("icr,ic->ir", T, c * b[jdx])
     assert rel(z["F"][jdx], F) < 1e-6
+
+
+def test_reference_fmm_runs(oracle):
+    # The reference's own CPU FMM (oracle/_ref/libmfref_fmm.so), where its
+    # sources were present to build it: at P = 8 its field is within 1e-5 of
+    # the FP64 oracle on a small cylinder, and its Hessian within 1e-3.
+    import oracle as orc
+    import scenes
+    if not orc.RefFmm.available():
+        pytest.skip("oracle/_ref/libmfref_fmm.so (the reference's FMM) is not built here")
+    ref = orc.RefFmm()
+    sc = scenes.config_fmm_1m(4096)
+    rng = np.random.default_rng(3)
+    m = ((np.array([0.0, 0.0, 1.0]) + 0.3 * rng.normal(size=(sc.n, 3))) * sc.c).astype(np.float32)
+    p64, m64 = sc.pos.astype(np.float64), m.astype(np.float64)
+    idx = np.sort(rng.choice(sc.n, 256, replace=False))
+    f, _, _ = ref.field(sc.pos, m, sc.h, order=8)
+    assert rel(f[idx], oracle.field(p64[idx], p64, m64, sc.h)) < 1e-5
+    t, _, _ = ref.hessian(sc.pos, m, sc.h, order=8)
+    assert rel(t[idx], oracle.tensor_sum(p64[idx], p64, m64, sc.h)) < 1e-3
