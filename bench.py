@@ -826,7 +826,7 @@ def measure_served(args, rank, world, local):
         "pairs": pairs, "budget_bytes": 120e9, "clocks": clk, "plain": plain,
         "note": "N <= 65,536: all-pairs batch (executed pairs); N > 65,536: own solver handle on its own host "
                 "thread and stream, field products through the FMM (P=8, effective pairs), the force all-pairs "
-                "up to 196,608 particles and through the FMM above; 20 timesteps per request, <= 4 CG "
+                "up to 131,072 particles and through the FMM above; 20 timesteps per request, <= 4 CG "
                 "iterations per step; step latency: per request timestep (batch members: their tick until the "
                 "step was done on the device; others: each timestep on their thread); tick: serving-loop "
                 "ticks in which the batch took a timestep",
@@ -932,7 +932,6 @@ def run_fmm(args, rank, world, local):
     s.set_option("fmm", mfgb.FMM_ON)
     s.set_option("fmm_order", args.fmm_order)
     s.set_option("fmm_theta", 0.5)
-    s.set_option("fmm_leaf", 64)
     s.set_option("kernel_timing", 1)
     t0 = time.perf_counter()
     cold_iters, cold_res = s.solve(500)
@@ -1045,7 +1044,7 @@ def run_fmm(args, rank, world, local):
             "data": "synthetic: seeded jittered-lattice cylinder (the reference ships no dataset)",
             "config": {"workload": f"fmm_fp32_{n}: jittered lattice cylinder r=0.3 height 1, N={n}, "
                                    f"h=2*spacing={sc.h:.5f}, chi=1.5, H0=(0,0,1), FMM P={args.fmm_order} "
-                                   f"theta=0.5 (force 0.3) leaf>=64, dt={args.dt}, CG rel tol {args.rel_tol:g}",
+                                   f"theta=0.5 (force 0.3) leaf>=12, dt={args.dt}, CG rel tol {args.rel_tol:g}",
                        "N": n, "step": "one timestep: octree rebuild, warm-started CG solve (FMM products), "
                                        "Kelvin force (FMM), symplectic Euler",
                        "l2": "flushed before every timed step (256 MiB write, not timed)",

@@ -94,7 +94,7 @@ typedef enum mf_option {
                                whole) with CUDA events (mf_get_kernel_stats) */
   MF_OPT_FMM = 9,           /* field and force products of FP32 handles: 0 auto (field
                                products through the FMM above 65,536 particles, the Kelvin
-                               force above 262,144; all-pairs below), 1 always the FMM,
+                               force above 131,072; all-pairs below), 1 always the FMM,
                                2 always all-pairs.  FP64 handles are all-pairs. */
   MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
                                (terms of degree n < P): 4..8, default 8.  The reference's
@@ -103,7 +103,7 @@ typedef enum mf_option {
   MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture of the field products, default 0.5
                                (FMMOptions.hpp:118) */
   MF_OPT_FMM_LEAF = 12,     /* FMM leaf level: the deepest whose boxes hold at least this many
-                               particles on average (default 64) */
+                               particles on average (default 12) */
   MF_OPT_AUTOTUNE = 13,     /* block shapes of the FP32 all-pairs launches: 0 fixed default,
                                1 tuned (default; each new body and size class is timed once
                                per process on the scene's own data), 2 tuned choices only when

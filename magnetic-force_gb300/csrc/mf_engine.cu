@@ -181,12 +181,15 @@ struct EngineBase {
 // Particle counts above which FP32 handles take the FMM by default: the
 // field products above kFmmAutoMin, the Kelvin force above kFmmForceAutoMin.
 // The force's near field is wider (FmmConfig::theta_force), so in a compact
-// scene of up to ~200k particles it covers most of the scene, and the
-// all-pairs product once per unordered pair is as fast (measured on the
-// r = 0.3 cylinder: 11.6 / 11.0 ms at 131,072, 25.2 / 25.2 at 196,608, 44.9
-// / 35.3 at 262,144, all-pairs / FMM) and exact to FP32 rounding.
+// scene of up to ~130k particles it covers most of the scene, and the
+// all-pairs product once per unordered pair is as fast and exact to FP32
+// rounding (all-pairs / FMM force ms, cylinder r = 0.3 and sphere r = 0.4:
+// 6.5 / 8.4-8.8 at 98,304, 11.4 / 10.9-11.0 at 131,072, 17.5 / 14.3-16.3 at
+// 163,840, 24.8 / 17.0-17.2 at 196,608).
 constexpr int64_t kFmmAutoMin = 65536;
-constexpr int64_t kFmmForceAutoMin = 196608;
+constexpr int64_t kFmmForceAutoMin = 131072;
+// Leaf size of the external dipoles' trees unless the caller sets one.
+constexpr int kExtLeafMin = 64;
 
 template <class Real>
 class Engine final : public EngineBase {
@@ -500,6 +503,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_LEAF:
         if (v < 1 || v > 4096) return fail(MF_ERR_INVALID_ARG, "fmm leaf size must be 1..4096");
         fmm_cfg_.leaf_min = int(v);
+        leaf_set_ = true;
         fmm_dirty_ = fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
       case MF_OPT_AUTOTUNE:
@@ -567,6 +571,7 @@ class Engine final : public EngineBase {
   // (fmmf_).
   Fmm fmm_, fmmf_;
   bool fmmf_dirty_ = true;
+  bool leaf_set_ = false;  // MF_OPT_FMM_LEAF given by the caller
   // External dipoles through the FMM: their octree (particles as targets) at
   // the field's aperture and at the force's (the gradient tensor), their cell
   // list and the near-field correction records.
@@ -939,10 +944,17 @@ class Engine final : public EngineBase {
           bbox[k] = std::min(ext_cells_.bbox(0)[k], cells_.bbox(0)[k]);
           bbox[3 + k] = std::max(ext_cells_.bbox(0)[3 + k], cells_.bbox(0)[3 + k]);
         }
-        MF_TRY(ext_fmm_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, fmm_cfg_, st_));
+        // The external sources' trees keep leaf boxes of >= kExtLeafMin on
+        // average unless the caller set the leaf size: with the handle's
+        // default of 12 the gradient tensor of 70,000 scattered dipoles at
+        // 8,000 particles came out 1.7e-5 from the all-pairs sums, under 1e-5
+        // at 64 (deeper trees move more nearby sources into expansions).
+        FmmConfig ce = fmm_cfg_;
+        if (!leaf_set_) ce.leaf_min = kExtLeafMin;
+        MF_TRY(ext_fmm_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, ce, st_));
         ctr_.kernel_launches += 17;
         if (fmm_cfg_.force_theta() < fmm_cfg_.theta) {
-          FmmConfig ct = fmm_cfg_;
+          FmmConfig ct = ce;
           ct.theta = fmm_cfg_.force_theta();
           MF_TRY(ext_fmmt_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, ct, st_));
           ctr_.kernel_launches += 17;

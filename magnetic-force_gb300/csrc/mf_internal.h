@@ -390,7 +390,15 @@ class CellList {
 struct FmmConfig {
   int order = 8;         // expansion terms per degree as the reference counts them (n < P); degree P-1
   double theta = 0.5;    // multipole acceptance aperture (FMMOptions.hpp:56-78)
-  int leaf_min = 64;     // leaf level: the deepest with at least this many particles per box on average
+  // Leaf level: the deepest with at least this many particles per box on
+  // average over the grid's boxes.  Levels differ by 8x in occupancy, and
+  // boxes of ~15 at the deeper level measured faster than ~120 at the coarser
+  // one (196,608-particle cylinder, force / field ms: 17.0 / 5.9 against
+  // 26.1 / 6.2), boxes of ~10 slower than ~80 (1,048,576: 122 / 36 against
+  // 90 / 18), so 12 keeps the mean occupancy in [12, 96).  Scenes that fill
+  // their bounding box sparsely (spheres) gained most: 196,608 particles in a
+  // sphere, 17 / 4 ms against 65 / 24 at the former default of 64.
+  int leaf_min = 12;
   // Aperture of the Kelvin force and force-tensor products, which take the
   // Hessian of the local expansion: it converges one degree later than the
   // field, and inside a magnetised body the far boxes' Hessians cancel to a

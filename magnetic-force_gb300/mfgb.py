@@ -526,7 +526,7 @@ class FmmMatrix:
     targets) and its operator* (fmmtl/KernelMatrix.hpp:127-131).  targets=None
     means the targets are the sources."""
 
-    def __init__(self, sources, h, targets=None, order=8, theta=0.5, leaf_min=64, device=0):
+    def __init__(self, sources, h, targets=None, order=8, theta=0.5, leaf_min=12, device=0):
         self._h = None
         src = _f32(sources)
         tgt = None if targets is None else _f32(targets)
