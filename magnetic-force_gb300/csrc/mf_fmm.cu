@@ -463,10 +463,12 @@ __global__ void __launch_bounds__(128) k_fmm_m2l(const M2LArgs p) {
 // Locals of a level: the M2L partials plus the parent's locals shifted to the
 // child centre,  L^c_beta += 2^(-2-|beta|) sum_delta L^p_(beta+delta) v_c^delta / delta!.
 // `occ` counts targets: boxes without targets need no locals.
+// kmin: coefficients below it are not computed (zero): a Hessian-only product
+// has no degree-1 partials (kmin 3).
 template <int Q>
 __global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_t* __restrict__ occ,
                           const float* __restrict__ Lpart, int chunks, float* __restrict__ L,
-                          const double* __restrict__ done) {
+                          const double* __restrict__ done, int kmin) {
   constexpr int NC = ncoef(Q) - 1;
   if (done && *done != 0.0) return;
   const float* Lpar = L + lp.box_off * NC;
@@ -476,7 +478,7 @@ __global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_
     const int k = int(t / lv.nbox);
     const int64_t b = t % lv.nbox;
     float v = 0.f;
-    if (occ[lv.box_off + b] > 0) {
+    if (k >= kmin && occ[lv.box_off + b] > 0) {
       for (int ch = 0; ch < chunks; ++ch) v += Lpart[(int64_t(ch) * NC + k) * lv.nbox + b];
       if (has_parent) {
         const char4 e = c_mi[k + 1];
@@ -503,11 +505,12 @@ __global__ void k_fmm_l2l(FmmLevel lv, FmmLevel lp, int has_parent, const int32_
 // shared memory by bulk copies on an mbarrier pipeline, as in the all-pairs
 // kernel, and swept with the packed clamped pair body.
 // ---------------------------------------------------------------------------
-constexpr int kP2PThreads = 128;
-constexpr int kP2PTile = 256;  // sources (slots) per stage
+// The CTA shape (threads per leaf box, one target each with rounds for
+// larger boxes; sources per stage) is a template parameter of the kernel.
 constexpr int kP2PStages = 3;
 constexpr int kP2PMaxSteps = 128;  // tile steps per refill of the row walk (1 KB of shared memory)
-constexpr int kP2PSmem = kP2PStages * 2 * kP2PTile * int(sizeof(float4));
+template <int TILE>
+constexpr int p2p_smem() { return kP2PStages * 2 * TILE * int(sizeof(float4)); }
 
 struct P2PArgs {
   FmmLevel lv;
@@ -542,8 +545,8 @@ __device__ __forceinline__ int near_plane(const int4& hr, int dx) {
 // added from k_fmm_near_sym's partial sums -- the box's own plane, then the
 // plane of every writer box (this box minus a half-stencil offset, inside the
 // grid and not empty), in a fixed order with compensated FP32.
-template <int Q, int kKind, bool kParts = false>
-__global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const AllPairsArgs<float> a,
+template <int Q, int kKind, bool kParts, int TPB, int TILE>
+__global__ void __launch_bounds__(TPB) k_fmm_p2p(const P2PArgs p, const AllPairsArgs<float> a,
                                                          const SceneDesc<float> sc) {
   static_assert(!kParts || kKind == 1, "partial sums: the Kelvin force only");
   using Body = std::conditional_t<kKind == 0, FieldF2Body, std::conditional_t<kKind == 1, ForceF2Body, TensorF2Body>>;
@@ -563,9 +566,9 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   const int tid = threadIdx.x;
   const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
   const int32_t st0 = p.tstart[c];
-  for (int k = tid; k < NC; k += kP2PThreads) s_L[k] = p.L[int64_t(k) * lv.nbox + c];
-  auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + s * 2 * kP2PTile; };
-  auto stage_mom = [&](int s) { return stage_pos(s) + kP2PTile; };
+  for (int k = tid; k < NC; k += TPB) s_L[k] = p.L[int64_t(k) * lv.nbox + c];
+  auto stage_pos = [&](int s) { return reinterpret_cast<float4*>(smem_raw) + s * 2 * TILE; };
+  auto stage_mom = [&](int s) { return stage_pos(s) + TILE; };
   if (tid == 0) {
     for (int s = 0; s < kP2PStages; ++s) mbar_init(&bar[s], 1);
     fence_mbar_init();
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
         pos = -1;
         continue;
       }
-      const int32_t m = min(kP2PTile, e - pos);
+      const int32_t m = min(TILE, e - pos);
       s_steps[k++] = make_int2(pos, m);
       pos += m;
     }
@@ -612,7 +615,7 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
   uint32_t u = 0;  // steps consumed so far (stage and parity of the next)
   bool failed = false;
   int fail_k = 0, fail_ns = 0;
-  for (int t0 = 0; t0 < n && !failed; t0 += kP2PThreads) {
+  for (int t0 = 0; t0 < n && !failed; t0 += TPB) {
     const bool act = t0 + tid < n;
     // A warp without a live target (the last warps of a small box) skips
     // the pair sweeps; it still takes part in every barrier and wait.
@@ -700,11 +703,11 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
       float v = 1.f;
-      pw[(ax * Q) * kP2PThreads + tid] = 1.f;
+      pw[(ax * Q) * TPB + tid] = 1.f;
 #pragma unroll
       for (int k = 1; k < Q; ++k) {
         v = v * w[ax] * (1.f / float(k));
-        pw[(ax * Q + k) * kP2PThreads + tid] = v;
+        pw[(ax * Q + k) * TPB + tid] = v;
       }
     }
     double v[kOut];
@@ -714,8 +717,8 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
       float h0 = 0.f, h1 = 0.f, h2 = 0.f;
       for (int g = 0; g < ncoef(Q - 1); ++g) {
         const char4 e = c_mi[g];
-        const float mono = pw[e.x * kP2PThreads + tid] * pw[(Q + e.y) * kP2PThreads + tid] *
-                           pw[(2 * Q + e.z) * kP2PThreads + tid];
+        const float mono = pw[e.x * TPB + tid] * pw[(Q + e.y) * TPB + tid] *
+                           pw[(2 * Q + e.z) * TPB + tid];
         h0 = fmaf(s_L[gidx(e.x + 1, e.y, e.z) - 1], mono, h0);
         h1 = fmaf(s_L[gidx(e.x, e.y + 1, e.z) - 1], mono, h1);
         h2 = fmaf(s_L[gidx(e.x, e.y, e.z + 1) - 1], mono, h2);
@@ -729,8 +732,8 @@ __global__ void __launch_bounds__(kP2PThreads) k_fmm_p2p(const P2PArgs p, const 
       float hxx = 0.f, hyy = 0.f, hzz = 0.f, hxy = 0.f, hxz = 0.f, hyz = 0.f;
       for (int g = 0; g < ncoef(Q - 2); ++g) {
         const char4 e = c_mi[g];
-        const float mono = pw[e.x * kP2PThreads + tid] * pw[(Q + e.y) * kP2PThreads + tid] *
-                           pw[(2 * Q + e.z) * kP2PThreads + tid];
+        const float mono = pw[e.x * TPB + tid] * pw[(Q + e.y) * TPB + tid] *
+                           pw[(2 * Q + e.z) * TPB + tid];
         hxx = fmaf(s_L[gidx(e.x + 2, e.y, e.z) - 1], mono, hxx);
         hyy = fmaf(s_L[gidx(e.x, e.y + 2, e.z) - 1], mono, hyy);
         hzz = fmaf(s_L[gidx(e.x, e.y, e.z + 2) - 1], mono, hzz);
@@ -1321,45 +1324,64 @@ mf_status Fmm::product(int kind, const float4* pos4, const float4* smom, const A
 }
 
 namespace {
+// M2L launches of one level, split by local degree so the multipole and the
+// accumulators stay in registers.  hess: the product needs only the Hessian
+// of the local expansion (the Kelvin force, the force tensor), which no local
+// of degree 1 reaches (L2L maps degree >= 2 only from degree >= 2, and L2P of
+// the Hessian reads degree >= 2), so the degree-1 locals are not computed.
 template <int Q>
 struct M2LVariants;
 template <>
 struct M2LVariants<3> {
-  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
-    k_fmm_m2l<3, 1, 3><<<g, 128, 0, st>>>(p);
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) k_fmm_m2l<3, 2, 3><<<g, 128, 0, st>>>(p);
+    else k_fmm_m2l<3, 1, 3><<<g, 128, 0, st>>>(p);
     *n += 1;
   }
 };
 template <>
 struct M2LVariants<4> {
-  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
-    k_fmm_m2l<4, 1, 4><<<g, 128, 0, st>>>(p);
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) k_fmm_m2l<4, 2, 4><<<g, 128, 0, st>>>(p);
+    else k_fmm_m2l<4, 1, 4><<<g, 128, 0, st>>>(p);
     *n += 1;
   }
 };
 template <>
 struct M2LVariants<5> {
-  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
-    k_fmm_m2l<5, 1, 5><<<g, 128, 0, st>>>(p);
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) k_fmm_m2l<5, 2, 5><<<g, 128, 0, st>>>(p);
+    else k_fmm_m2l<5, 1, 5><<<g, 128, 0, st>>>(p);
     *n += 1;
   }
 };
 template <>
 struct M2LVariants<6> {
-  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
-    k_fmm_m2l<6, 1, 2><<<g, 128, 0, st>>>(p);
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) k_fmm_m2l<6, 2, 2><<<g, 128, 0, st>>>(p);
+    else k_fmm_m2l<6, 1, 2><<<g, 128, 0, st>>>(p);
     k_fmm_m2l<6, 3, 6><<<g, 128, 0, st>>>(p);
     *n += 2;
   }
 };
 template <>
 struct M2LVariants<7> {
-  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n) {
-    k_fmm_m2l<7, 1, 3><<<g, 128, 0, st>>>(p);
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) k_fmm_m2l<7, 2, 3><<<g, 128, 0, st>>>(p);
+    else k_fmm_m2l<7, 1, 3><<<g, 128, 0, st>>>(p);
     k_fmm_m2l<7, 4, 7><<<g, 128, 0, st>>>(p);
     *n += 2;
   }
 };
+// One CTA of 128 threads per leaf box, 256-source stages, also for small
+// boxes: 64 threads with 128-source stages measured slower at 262,144
+// particles (boxes of <= 40: near field 3.9 against 2.7 ms for the field,
+// 11.3 against 7.3 for the force): the step and barrier count per box doubles.
+template <int Q, int kKind, bool kParts>
+void launch_p2p(unsigned grid, cudaStream_t st, const P2PArgs& pp, const AllPairsArgs<float>& a,
+                const SceneDesc<float>& sc) {
+  k_fmm_p2p<Q, kKind, kParts, 128, 256><<<grid, 128, p2p_smem<256>(), st>>>(pp, a, sc);
+}
 }  // namespace
 
 template <int Q>
@@ -1409,9 +1431,9 @@ mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const
     p.per_class = ((int64_t(p.hx) * p.hy * p.hz) + 31) / 32 * 32;
     p.done = done;
     const int64_t threads = int64_t(p.chunks) * 8 * p.per_class;
-    M2LVariants<Q>::launch(p, unsigned((threads + 127) / 128), st, &nl);
+    M2LVariants<Q>::launch(p, unsigned((threads + 127) / 128), st, &nl, kind != 0);
     k_fmm_l2l<Q><<<blocks_for(int64_t(NC) * v.nbox, 256, int64_t(sms) * 32), 256, 0, st>>>(
-        v, lv_[size_t(l - 1)], l > 2 ? 1 : 0, tocc, lpart_.as<float>(), p.chunks, Lc, done);
+        v, lv_[size_t(l - 1)], l > 2 ? 1 : 0, tocc, lpart_.as<float>(), p.chunks, Lc, done, kind != 0 ? 3 : 0);
     ++nl;
   }
   P2PArgs pp{};
@@ -1456,13 +1478,13 @@ mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const
     ns.done = done;
     k_fmm_near_sym<<<unsigned((leaf.nbox + kNearSymWarps - 1) / kNearSymWarps), 32 * kNearSymWarps, 0, st>>>(ns, a, sc);
     ++nl;
-    k_fmm_p2p<Q, 1, true><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+    launch_p2p<Q, 1, true>(unsigned(leaf.nbox), st, pp, a, sc);
   } else if (kind == 1)
-    k_fmm_p2p<Q, 1><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+    launch_p2p<Q, 1, false>(unsigned(leaf.nbox), st, pp, a, sc);
   else if (kind == 2)
-    k_fmm_p2p<Q, 2><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+    launch_p2p<Q, 2, false>(unsigned(leaf.nbox), st, pp, a, sc);
   else
-    k_fmm_p2p<Q, 0><<<unsigned(leaf.nbox), kP2PThreads, kP2PSmem, st>>>(pp, a, sc);
+    launch_p2p<Q, 0, false>(unsigned(leaf.nbox), st, pp, a, sc);
   ++nl;
   if (marks) MF_CUDA_TRY(cudaEventRecord(marks[3], st));
   launches_ = nl;
