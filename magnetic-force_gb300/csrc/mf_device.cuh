@@ -79,6 +79,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // after an error always wait with the default bound.
 __device__ __forceinline__ uint32_t stage_wait_limit(uint32_t debug) { return debug ? debug - 1 : kWaitLimit; }
 
+// Asynchronous 16-byte copy global -> shared (L2 only), grouped per thread:
+// cp_async_commit closes the thread's current group, cp_async_wait<N> waits
+// until at most N of its groups are in flight.  Other threads see the data
+// after a barrier that includes them (__syncwarp / __syncthreads).  Both
+// addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ void mbar_inval(uint64_t* bar) {
   asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }

@@ -803,17 +803,67 @@ struct NearSymArgs {
 };
 constexpr int kNearSymWarps = 4, kNearSymTPT = 4, kNearSymChunk = 64;
 
-__global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
+// The walk over the half stencil's source boxes in units of up to
+// kNearSymChunk pair items (a box in one or more chunks), in the order
+// rows, x offsets, chunks.
+struct NearUnit {
+  int32_t sb;     // first slot of the box
+  int32_t cs;     // first item of the chunk in the box
+  int32_t cn;     // items in the chunk
+  int32_t plane;  // partial-sum plane of the box's offset (-1: no unit)
+};
+struct NearCursor {
+  int r, dx;         // next half-stencil row and x offset to examine
+  int32_t sb, ni;    // the box being chunked (ni items; 0: none)
+  int32_t cs, plane;
+};
+
+__device__ __forceinline__ NearUnit near_next(NearCursor& cur, const NearSymArgs& p, int ix, int iy, int iz) {
+  constexpr int CH = kNearSymChunk;
+  const FmmLevel& lv = p.lv;
+  for (;;) {
+    if (cur.cs < cur.ni) {
+      const NearUnit u{cur.sb, cur.cs, min(CH, cur.ni - cur.cs), cur.plane};
+      cur.cs += CH;
+      return u;
+    }
+    if (cur.r >= p.n_hrows) return NearUnit{0, 0, 0, -1};
+    const int4 hr = p.hrows[cur.r];
+    const int cy = iy + hr.y, cz = iz + hr.z;
+    const int dx = cur.dx;
+    if (cy < 0 || cy >= lv.ny || cz < 0 || cz >= lv.nz || dx > hr.x) {  // next row
+      ++cur.r;
+      if (cur.r < p.n_hrows) {
+        const int4 h2 = p.hrows[cur.r];
+        cur.dx = (h2.y == 0 && h2.z == 0) ? 1 : -h2.x;
+      }
+      continue;
+    }
+    ++cur.dx;
+    const int cx = ix + dx;
+    if (cx < 0 || cx >= lv.nx) continue;
+    const int64_t b = (int64_t(cz) * lv.ny + cy) * lv.nx + cx;
+    const int32_t nb = p.cnt[b];
+    if (nb == 0) continue;
+    cur.sb = p.start[b];
+    cur.ni = (nb + 1) >> 1;
+    cur.cs = 0;
+    cur.plane = near_plane(hr, dx);
+  }
+}
+
+__global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
                                                                      const SceneDesc<float> sc) {
   constexpr int TPT = kNearSymTPT, CH = kNearSymChunk;
-  // per warp: a chunk of a source box's pair items (positions, then dipoles)
-  __shared__ float4 s_pos[kNearSymWarps][2 * CH], s_mom[kNearSymWarps][2 * CH];
+  // per warp, two buffers: a unit of a source box's pair items (positions,
+  // then dipoles); the next unit is copied into one while the current one is
+  // swept from the other
+  __shared__ __align__(16) float4 s_pos[kNearSymWarps][2][2 * CH], s_mom[kNearSymWarps][2][2 * CH];
   if (p.done && *p.done != 0.0) return;
   const FmmLevel& lv = p.lv;
   const int lane = threadIdx.x & 31;
-  float4* const wpos = s_pos[threadIdx.x >> 5];
-  float4* const wmom = s_mom[threadIdx.x >> 5];
-  const int64_t c = int64_t(blockIdx.x) * kNearSymWarps + (threadIdx.x >> 5);
+  const int w = threadIdx.x >> 5;
+  const int64_t c = int64_t(blockIdx.x) * kNearSymWarps + w;
   if (c >= lv.nbox) return;  // warp-uniform; the kernel has no block barrier
   const int32_t n = p.cnt[c];
   if (n == 0) return;
@@ -822,6 +872,19 @@ __global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearS
   const float near2 = sc.pc.near2_force;
   const float kk = float(kForceK);
   const PairItems::Item zero_item{{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  // Every lane copies its share of a unit and commits one group per unit
+  // (possibly empty), so the lanes' group counts stay in step.
+  auto stage = [&](const NearUnit& u, int buf) {
+    if (u.plane >= 0) {
+      const float4* sp = p.pos2s + u.sb + 2 * u.cs;
+      const float4* sm = p.mom2s + u.sb + 2 * u.cs;
+      for (int k = lane; k < 2 * u.cn; k += 32) {
+        cp_async16(&s_pos[w][buf][k], sp + k);
+        cp_async16(&s_mom[w][buf][k], sm + k);
+      }
+    }
+    cp_async_commit();
+  };
   for (int t0 = 0; t0 < n; t0 += 32 * TPT) {
     float2 tx[TPT], ty[TPT], tz[TPT], tmx[TPT], tmy[TPT], tmz[TPT];
     float2 acc[TPT][3];
@@ -831,16 +894,25 @@ __global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearS
       const bool live = li < n;
       const int32_t i = p.perm[st0 + (live ? li : 0)];
       const float4 q = a.tpos[i];
-      const float4 w = live ? a.tmom[i] : make_float4(0.f, 0.f, 0.f, 0.f);  // a dead slot adds nothing to sources
+      const float4 wm = live ? a.tmom[i] : make_float4(0.f, 0.f, 0.f, 0.f);  // a dead slot adds nothing to sources
       tx[t] = f2_dup(q.x);
       ty[t] = f2_dup(q.y);
       tz[t] = f2_dup(q.z);
-      tmx[t] = f2_dup(w.x);
-      tmy[t] = f2_dup(w.y);
-      tmz[t] = f2_dup(w.z);
+      tmx[t] = f2_dup(wm.x);
+      tmy[t] = f2_dup(wm.y);
+      tmz[t] = f2_dup(wm.z);
       acc[t][0] = acc[t][1] = acc[t][2] = make_float2(0.f, 0.f);
     }
-    {  // the box's own pairs, target side only
+    NearCursor cur{0, 0, 0, 0, 0, 0};
+    if (p.n_hrows > 0) {
+      const int4 h0 = p.hrows[0];
+      cur.dx = (h0.y == 0 && h0.z == 0) ? 1 : -h0.x;
+    }
+    NearUnit u = near_next(cur, p, ix, iy, iz);
+    int buf = 0;
+    __syncwarp();  // the previous round's reads of both buffers are done
+    stage(u, 0);
+    {  // the box's own pairs, target side only (the first unit's copy is in flight)
       const float4* sp = p.pos2s + st0;
       const float4* sm = p.mom2s + st0;
       const int ni = (n + 1) >> 1;
@@ -851,65 +923,49 @@ __global__ void __launch_bounds__(32 * kNearSymWarps) k_fmm_near_sym(const NearS
         for (int t = 0; t < TPT; ++t) sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
       }
     }
-    for (int r = 0; r < p.n_hrows; ++r) {
-      const int4 hr = p.hrows[r];
-      const int cy = iy + hr.y, cz = iz + hr.z;
-      if (cy < 0 || cy >= lv.ny || cz < 0 || cz >= lv.nz) continue;
-      for (int dx = (hr.y == 0 && hr.z == 0) ? 1 : -hr.x; dx <= hr.x; ++dx) {
-        const int cx = ix + dx;
-        if (cx < 0 || cx >= lv.nx) continue;
-        const int64_t b = (int64_t(cz) * lv.ny + cy) * lv.nx + cx;
-        const int32_t nb = p.cnt[b];
-        if (nb == 0) continue;
-        const int32_t sb = p.start[b];
-        const float4* sp = p.pos2s + sb;
-        const float4* sm = p.mom2s + sb;
-        float* plane = p.part + int64_t(near_plane(hr, dx)) * 3 * p.n_slots;
-        const int ni = (nb + 1) >> 1;
-        // The box's items in chunks of CH, staged by the warp with coalesced
-        // loads and read back as broadcasts.  Past the box's last item: a zero
-        // dipole at the origin, nothing on either side.
-        for (int cs = 0; cs < ni; cs += CH) {
-          const int cn = min(CH, ni - cs);
-          __syncwarp();
-          for (int k = lane; k < 2 * cn; k += 32) {
-            wpos[k] = sp[2 * cs + k];
-            wmom[k] = sm[2 * cs + k];
+    while (u.plane >= 0) {
+      const NearUnit nxt = near_next(cur, p, ix, iy, iz);
+      stage(nxt, buf ^ 1);
+      cp_async_wait<1>();  // this lane's copies of unit u have landed
+      __syncwarp();        // and every lane's
+      const float4* wpos = s_pos[w][buf];
+      const float4* wmom = s_mom[w][buf];
+      float* plane = p.part + int64_t(u.plane) * 3 * p.n_slots;
+      const int cn = u.cn;
+      // Past the unit's last item: a zero dipole at the origin, nothing on either side.
+      for (int j0 = 0; j0 < cn; j0 += 2) {
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = 0.f;
+#pragma unroll
+        for (int q2 = 0; q2 < 2; ++q2) {
+          const PairItems::Item it = (q2 == 0 || j0 + 1 < cn) ? PairItems::load_item(wpos, wmom, j0 + q2) : zero_item;
+          float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+          for (int t = 0; t < TPT; ++t) sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            v[q2 * 6 + 2 * k] = src[k].x;
+            v[q2 * 6 + 2 * k + 1] = src[k].y;
           }
-          __syncwarp();
-          for (int j0 = 0; j0 < cn; j0 += 2) {
-            float v[16];
-#pragma unroll
-            for (int q = 0; q < 16; ++q) v[q] = 0.f;
-#pragma unroll
-            for (int q2 = 0; q2 < 2; ++q2) {
-              const PairItems::Item it =
-                  (q2 == 0 || j0 + 1 < cn) ? PairItems::load_item(wpos, wmom, j0 + q2) : zero_item;
-              float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-#pragma unroll
-              for (int t = 0; t < TPT; ++t)
-                sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
-#pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                v[q2 * 6 + 2 * k] = src[k].x;
-                v[q2 * 6 + 2 * k + 1] = src[k].y;
-              }
-            }
-            const float w = warp_reduce_scatter<16>(v, lane);
-            const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
-            if ((lane & 1) == 0 && kv < 12) {
-              const int jl = j0 + kv / 6, rem = kv % 6;
-              if (jl < cn) {
-                float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(sb) + 2 * (cs + jl) + (rem & 1));
-                const float val = -w * kk;  // f_ji = -f_ij
-                if (t0 == 0) *dst = val;
-                else *dst += val;
-              }
-            }
+        }
+        const float wr = warp_reduce_scatter<16>(v, lane);
+        const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
+        if ((lane & 1) == 0 && kv < 12) {
+          const int jl = j0 + kv / 6, rem = kv % 6;
+          if (jl < cn) {
+            float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(u.sb) + 2 * (u.cs + jl) + (rem & 1));
+            const float val = -wr * kk;  // f_ji = -f_ij
+            if (t0 == 0) *dst = val;
+            else *dst += val;
           }
         }
       }
+      __syncwarp();  // every lane is done with buffer buf before it is refilled
+      buf ^= 1;
+      u = nxt;
     }
+    cp_async_wait<0>();
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
       const int li = t0 + t * 32 + lane;
