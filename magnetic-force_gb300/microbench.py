@@ -19,6 +19,10 @@ CG solve; per-stage device times come from the handle's event timing.
 
     python magnetic-force_gb300/microbench.py --kernel fmm_step --n 1048576 --reps 1
 
+``--density-of 1048576 --n 131072`` keeps the spacing of the 1,048,576-particle
+cylinder in one of half its radius and height: the same leaf boxes (one level
+higher) and near lists, an eighth of the particles (a small case for captures).
+
 ``fmm_step`` runs whole timesteps (mf_advance: octree rebuild from the moved
 positions, CG solve, force) of the same cylinder through the FMM, so a
 capture sees the tree and expansion passes as well as the products.
@@ -64,6 +68,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--pair-symmetric", type=int, default=-1,
                     help="fmm_* / engine_*: MF_OPT_PAIR_SYMMETRIC of the handle (-1: its default)")
+    ap.add_argument("--density-of", type=int, default=0,
+                    help="fmm_*: keep the particle spacing of the cylinder of this many particles (r 0.3, "
+                         "height 1) and scale its radius and height to --n particles (0: r 0.3, height 1)")
     args = ap.parse_args()
 
     import numpy as np
@@ -114,7 +121,8 @@ def main():
 
 
 def fmm(args, np, torch, mfgb, scenes):
-    sc = scenes.jittered_lattice(args.n, "cylinder", radius=0.3, height=1.0, chi=1.5, seed=1)
+    f = (args.n / args.density_of) ** (1.0 / 3.0) if args.density_of > 0 else 1.0
+    sc = scenes.jittered_lattice(args.n, "cylinder", radius=0.3 * f, height=f, chi=1.5, seed=1)
     s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
     s.set_option("fmm", mfgb.FMM_ON)
     s.set_option("fmm_order", 8)
