@@ -776,15 +776,17 @@ __global__ void __launch_bounds__(TPB) k_fmm_p2p(const P2PArgs p, const AllPairs
 
 // ---------------------------------------------------------------------------
 // Near field of the Kelvin force once per unordered box pair (targets are the
-// sources): one warp per leaf box A, up to 4 targets per lane (rounds of 128
-// for larger boxes).
+// sources): one warp per leaf box A.  Both half-warps hold the same 128
+// target slots (8 per lane; rounds of 128 for larger boxes) and sweep
+// alternate pairs of source items, so every shuffle tree of the source sums
+// spans 16 lanes and serves 8 targets per lane.
 //   * A's own pairs: every ordered pair, target side only.
 //   * The boxes B of the half stencil: each pair item's force adds into the
-//     targets' sums and, reduced over the warp by a fixed shuffle tree, into
-//     the sources' sums (f_ji = -f_ij), stored at plane near_plane(B - A) of
-//     the source's slot.  A later target round adds to the entries of the
+//     targets' sums and, reduced over the half-warp by a fixed shuffle tree,
+//     into the sources' sums (f_ji = -f_ij), stored at plane near_plane(B - A)
+//     of the source's slot.  A later target round adds to the entries of the
 //     earlier ones (the same lane, in order).
-//   * The targets' sums go to plane 0.
+//   * The targets' sums (the two halves' added) go to plane 0.
 // Every (plane, slot) entry has one writer, so results do not depend on
 // scheduling.  Sums are in the all-pairs kernels' units (times K).
 // ---------------------------------------------------------------------------
@@ -801,7 +803,7 @@ struct NearSymArgs {
   int64_t n_slots;
   const double* done;
 };
-constexpr int kNearSymWarps = 4, kNearSymTPT = 4, kNearSymChunk = 64;
+constexpr int kNearSymWarps = 4, kNearSymTPT = 8, kNearSymChunk = 64;
 
 // The walk over the half stencil's source boxes in units of up to
 // kNearSymChunk pair items (a box in one or more chunks), in the order
@@ -852,9 +854,36 @@ __device__ __forceinline__ NearUnit near_next(NearCursor& cur, const NearSymArgs
   }
 }
 
-__global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
-                                                                     const SceneDesc<float> sc) {
+// Reduce-scatter of NV values over each half-warp (16 lanes): lane l ends
+// with value l & 15 summed over its half, by a fixed shuffle tree.
+template <int NV>
+__device__ __forceinline__ float half_reduce_scatter(const float (&v)[NV], int lane) {
+  static_assert(NV == 16, "one value per lane of a half-warp");
+  float w[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) w[q] = v[q];
+  int b = 8;
+#pragma unroll
+  for (int n = NV; n > 1; n >>= 1, b >>= 1) {
+    const bool hi = lane & b;
+#pragma unroll
+    for (int q = 0; q < n / 2; ++q) {
+      const float send = hi ? w[q] : w[q + n / 2];
+      const float keep = hi ? w[q + n / 2] : w[q];
+      w[q] = keep + __shfl_xor_sync(0xffffffffu, send, b);
+    }
+  }
+  return w[0];
+}
+
+// 255 registers with 2 CTAs per SM; one warp per box with 4 targets per
+// lane (168 registers, 3 CTAs per SM) measured 69.4 against 64.2 ms at
+// 1,048,576 particles: its 32-lane trees served half the targets each.
+__global__ void __launch_bounds__(32 * kNearSymWarps, 2) k_fmm_near_sym(const NearSymArgs p, const AllPairsArgs<float> a,
+                                                                   const SceneDesc<float> sc) {
   constexpr int TPT = kNearSymTPT, CH = kNearSymChunk;
+  constexpr int TL = 16;    // lanes per target set (a half-warp)
+  constexpr int STEP = 4;   // items per sweep step of the warp (2 per half)
   // per warp, two buffers: a unit of a source box's pair items (positions,
   // then dipoles); the next unit is copied into one while the current one is
   // swept from the other
@@ -863,6 +892,8 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
   const FmmLevel& lv = p.lv;
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
+  const int tl = lane & (TL - 1);  // slot lane within the target set
+  const int half = lane >> 4;      // which items of a step this lane sweeps
   const int64_t c = int64_t(blockIdx.x) * kNearSymWarps + w;
   if (c >= lv.nbox) return;  // warp-uniform; the kernel has no block barrier
   const int32_t n = p.cnt[c];
@@ -885,12 +916,12 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
     }
     cp_async_commit();
   };
-  for (int t0 = 0; t0 < n; t0 += 32 * TPT) {
+  for (int t0 = 0; t0 < n; t0 += TL * TPT) {
     float2 tx[TPT], ty[TPT], tz[TPT], tmx[TPT], tmy[TPT], tmz[TPT];
     float2 acc[TPT][3];
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
-      const int li = t0 + t * 32 + lane;
+      const int li = t0 + t * TL + tl;
       const bool live = li < n;
       const int32_t i = p.perm[st0 + (live ? li : 0)];
       const float4 q = a.tpos[i];
@@ -916,7 +947,7 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
       const float4* sp = p.pos2s + st0;
       const float4* sm = p.mom2s + st0;
       const int ni = (n + 1) >> 1;
-      for (int j = 0; j < ni; ++j) {
+      for (int j = half; j < ni; j += 2) {
         const PairItems::Item it = PairItems::load_item(sp, sm, j);
         float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
@@ -933,13 +964,14 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
       float* plane = p.part + int64_t(u.plane) * 3 * p.n_slots;
       const int cn = u.cn;
       // Past the unit's last item: a zero dipole at the origin, nothing on either side.
-      for (int j0 = 0; j0 < cn; j0 += 2) {
+      for (int j0 = 0; j0 < cn; j0 += STEP) {
+        const int jb = j0 + 2 * half;  // this lane's first item of the step
         float v[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) v[q] = 0.f;
 #pragma unroll
         for (int q2 = 0; q2 < 2; ++q2) {
-          const PairItems::Item it = (q2 == 0 || j0 + 1 < cn) ? PairItems::load_item(wpos, wmom, j0 + q2) : zero_item;
+          const PairItems::Item it = (jb + q2 < cn) ? PairItems::load_item(wpos, wmom, jb + q2) : zero_item;
           float2 src[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
           for (int t = 0; t < TPT; ++t) sym_force_pair2(tx[t], ty[t], tz[t], tmx[t], tmy[t], tmz[t], it, near2, acc[t], src);
@@ -949,10 +981,11 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
             v[q2 * 6 + 2 * k + 1] = src[k].y;
           }
         }
-        const float wr = warp_reduce_scatter<16>(v, lane);
-        const int kv = lane >> 1;  // value kv: item j0 + kv / 6, component (kv % 6) / 2, source kv % 2
-        if ((lane & 1) == 0 && kv < 12) {
-          const int jl = j0 + kv / 6, rem = kv % 6;
+        // value kv: item jb + kv / 6, component (kv % 6) / 2, source kv % 2
+        const float wr = half_reduce_scatter<16>(v, lane);
+        const int kv = tl;
+        if (kv < 12) {
+          const int jl = jb + kv / 6, rem = kv % 6;
           if (jl < cn) {
             float* dst = plane + int64_t(rem >> 1) * p.n_slots + (int64_t(u.sb) + 2 * (u.cs + jl) + (rem & 1));
             const float val = -wr * kk;  // f_ji = -f_ij
@@ -968,10 +1001,16 @@ __global__ void __launch_bounds__(32 * kNearSymWarps, 3) k_fmm_near_sym(const Ne
     cp_async_wait<0>();
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
-      const int li = t0 + t * 32 + lane;
-      if (li < n) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) p.part[int64_t(k) * p.n_slots + st0 + li] = (acc[t][k].x + acc[t][k].y) * kk;
+      for (int k = 0; k < 3; ++k) {
+        float s2 = acc[t][k].x + acc[t][k].y;
+        s2 += __shfl_xor_sync(0xffffffffu, s2, 16);  // the other half's items
+        acc[t][k].x = s2;
+      }
+      const int li = t0 + t * TL + tl;
+      if (li < n && half == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) p.part[int64_t(k) * p.n_slots + st0 + li] = acc[t][k].x * kk;
       }
     }
   }
