@@ -340,8 +340,11 @@ class CellList {
   // Bins the particles of every scene into cells of edge >= 2h; particles of
   // a cell are listed in increasing index order (deterministic sums).
   // Synchronises `st` once (the bounding boxes are read on the host).
+  // pair_planes: also reserve the partial sums of the corrections once per
+  // pair (~4.4 KB per particle), so later corrections, also inside a CUDA
+  // graph capture, allocate nothing; otherwise the first correction does.
   mf_status build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st,
-                  double margin_h = 0.0);
+                  double margin_h = 0.0, bool pair_planes = false);
   // Re-bins moved particles on the grids of the last build (no host
   // synchronisation, so it can be captured in a CUDA graph).  Particles that
   // left a grid are binned into its border cells, which keeps every
@@ -349,7 +352,8 @@ class CellList {
   mf_status rebin(const float4* pos4, cudaStream_t st);
   // corr_i = sum over j within 2h (resp. 4h) of [exact pair term - the
   // clamped far term the packed all-pairs loop gave that pair], in the
-  // all-pairs kernels' output units.  Targets = sources = the binned set.
+  // all-pairs kernels' output units.  Targets = sources = the binned set;
+  // each unordered near pair is evaluated once.
   // done_flags (per-scene solver rows) skip stopped scenes; done_count /
   // done_total make the launch a no-op once every scene has stopped.
   mf_status field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st,
@@ -378,6 +382,7 @@ class CellList {
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
   bool skip_field_on_ = false, skip_force_on_ = false;  // a list is in use
   DevBuf spos_, smom_;              // positions and dipoles in cell order (per correction)
+  mutable DevBuf cpart_;            // partial sums of the correction once per pair (planes x 3 x particles)
   std::vector<CellGrid> host_grids_;
   std::vector<double> host_bbox_;
   int64_t n_total_ = 0, n_cells_ = 0;
@@ -404,9 +409,14 @@ struct FmmConfig {
   // field, and inside a magnetised body the far boxes' Hessians cancel to a
   // small net force, so the same truncation error is ~40x larger relative to
   // the result.  Measured against FP64 direct sums at P = 8 on a cylinder of
-  // 1,048,576 particles: 1.3e-4 at 0.5, 3.1e-5 at 0.42, 1.1e-5 at 0.35,
-  // 5.4e-6 at 0.3 (field at 0.5: 3.3e-6).  The force uses min(theta, this).
-  double theta_force = 0.3;
+  // 1,048,576 particles: 1.3e-4 at 0.5, 3.1e-5 at 0.42, 9.3e-6 at 0.36,
+  // 7.6e-6 at 0.34, 4.7e-6 at 0.32, 4.0e-6 at 0.3 (field at 0.5: 3.3e-6); on
+  // the same cylinder's shape at 262,144 particles 1.3e-5 at 0.34, 6.6e-6 at
+  // 0.32 and 4.5e-6 at 0.3; spheres of 150,000-262,144 particles 2.1e-6 at
+  // 0.32.  0.32 holds every one of these within 1e-5 with a margin of 1.5x,
+  // and takes 66 against 75 ms per force product at 1,048,576 particles.
+  // The force uses min(theta, this).
+  double theta_force = 0.32;
   double force_theta() const { return theta_force < theta ? theta_force : theta; }
 };
 
