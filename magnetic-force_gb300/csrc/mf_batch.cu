@@ -263,7 +263,7 @@ class Batch {
 
     std::vector<CellSceneSpec> cs;
     for (const SI& si : sc_) cs.push_back(CellSceneSpec{si.off, si.n, si.h});
-    MF_TRY(cells_.build(pos4_.as<float4>(), cs, st_, /*margin_h=*/2.0, /*pair_planes=*/true));
+    MF_TRY(cells_.build(pos4_.as<float4>(), cs, st_, /*margin_h=*/2.0));
     MF_TRY(cells_.set_skips(skip_field, skip_force));
     to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
     MF_CUDA_TRY(cudaGetLastError());
@@ -640,18 +640,15 @@ class Server {
   // scratch.  FMM request: a solver handle's vectors, published arrays, cell
   // list and octree.
   static double need_bytes(int64_t n) {
-    // Every request: the near-field correction's partial sums once per pair
-    // (366 planes of 3 floats per particle).
-    constexpr double kCorrPlaneBytes = 366.0 * 12.0;
     // FMM requests: the handle's state and trees, ~1.2 KB per particle of
     // near-field partial sums where the force's near field runs once per box
     // pair, and, where the force is the all-pairs product once per unordered
     // pair, its block sums (12 KB per ordered pair of 1,024-particle blocks).
     if (n > kServeFmmMin) {
       const double nb = std::ceil(double(n) / 1024.0);
-      return double(n) * (720.0 + 1200.0 + kCorrPlaneBytes) + 12288.0 * nb * nb + 64.0 * 1024 * 1024;
+      return double(n) * (720.0 + 1200.0) + 12288.0 * nb * nb + 64.0 * 1024 * 1024;
     }
-    return double(n) * (320.0 + kCorrPlaneBytes) + 4.0 * 1024 * 1024;
+    return double(n) * 320.0 + 4.0 * 1024 * 1024;
   }
 
   mf_status submit(const mf_scene_desc& d, int64_t* id) {

@@ -11,11 +11,9 @@
 // benchmark densities.
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 
 #include "mf_internal.h"
-#include "mf_sym.cuh"
 
 namespace mfgb {
 namespace {
@@ -255,7 +253,7 @@ __global__ void k_gather_sorted(const int32_t* __restrict__ perm, const float4* 
 // 32 candidates whatever the rows' lengths.  Each lane sweeps its candidates
 // in increasing order, and every target's sum is finished by a fixed shuffle
 // tree, so results are deterministic.
-template <bool kForce, int kT = 8>
+template <bool kForce>
 __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __restrict__ grids, int n_scenes,
                                                           int64_t n_cells, const int32_t* __restrict__ perm,
                                                           const int32_t* __restrict__ start,
@@ -264,6 +262,7 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
                                                           const int32_t* __restrict__ skip_scene,
                                                           const double* __restrict__ done_flags, int done_stride,
                                                           const int32_t* __restrict__ done_count, int done_total) {
+  constexpr int kT = 8;
   constexpr int kRows = 81;  // (2R + 1)^2 row slots, R <= 4 (cells are at least h wide)
   if (done_count && *done_count >= done_total) return;
   __shared__ float s_tbl[40];
@@ -401,329 +400,6 @@ __global__ void __launch_bounds__(128) k_correction_cells(const CellGrid* __rest
   }
 }
 
-// ---------------------------------------------------------------------------
-// The correction once per unordered near pair.
-//
-// The correction of a pair is antisymmetric for the force (f_ji = -f_ij) and
-// has the same scalars on both sides for the field (the target's dipole in
-// place of the source's), so each unordered pair is evaluated once:
-//   * k_correction_half: one warp per cell c; its particles are the targets,
-//     the candidates are the particles of c itself paired with a later one
-//     (and the target itself, target side only: the field's SPH self term)
-//     and of the cells c + o for the offsets o after the centre of the
-//     (2R + 1)^3 cube in linear order (dz, dy, dx) that lie within the near
-//     reach.  A target's sum goes to plane 0, a candidate's to plane 1 (its
-//     own cell) or 2 + k (offset k): every (plane, particle) entry has one
-//     writer, a later pass of targets over the same cell adds to it in order.
-//   * k_correction_gather: one warp per cell adds, per particle, plane 0,
-//     plane 1 and the plane of every writer cell (c - o inside the grid,
-//     within reach, not empty) in a fixed order with compensated FP32.
-// Results do not depend on scheduling.  Planes are SoA [plane][component][
-// particle in cell order].
-// ---------------------------------------------------------------------------
-__host__ __device__ constexpr int half_count(int R) { return ((2 * R + 1) * (2 * R + 1) * (2 * R + 1) - 1) / 2; }
-constexpr int kMaxReachForce = 4, kMaxReachField = 2;  // cells are at least h wide
-__host__ __device__ constexpr int half_planes(bool force) {
-  return 2 + half_count(force ? kMaxReachForce : kMaxReachField);
-}
-
-__device__ __forceinline__ void half_offset(int R, int k, int& dx, int& dy, int& dz) {
-  const int sd = 2 * R + 1;
-  const int l = (sd * sd * sd - 1) / 2 + 1 + k;
-  dx = l % sd - R;
-  dy = (l / sd) % sd - R;
-  dz = l / (sd * sd) - R;
-}
-
-// Whether cell offset (dx, dy, dz) can hold a particle within the near radius
-// of one in the centre cell: the rows of k_correction_cells trimmed to the
-// cell-level distance bound.
-__device__ __forceinline__ bool in_reach(const CellGrid& g, int R, float near2, int dx, int dy, int dz) {
-  const float cs = 1.f / g.inv_cs;
-  const float gy = float(max(abs(dy) - 1, 0)) * cs, gz = float(max(abs(dz) - 1, 0)) * cs;
-  const float rem = near2 - gz * gz - gy * gy;
-  if (!(rem >= 0.f)) return false;
-  const int dxm = min(R, int(sqrtf(rem) * g.inv_cs) + 1);
-  return abs(dx) <= dxm;
-}
-
-template <bool kForce, int kT = 8>
-__global__ void __launch_bounds__(128) k_correction_half(const CellGrid* __restrict__ grids, int n_scenes,
-                                                         int64_t n_cells, const int32_t* __restrict__ start,
-                                                         const float4* __restrict__ spos,
-                                                         const float4* __restrict__ smom, float* __restrict__ part,
-                                                         int64_t stride, const int32_t* __restrict__ skip_scene,
-                                                         const double* __restrict__ done_flags, int done_stride,
-                                                         const int32_t* __restrict__ done_count, int done_total) {
-  constexpr int kCells = 1 + half_count(kForce ? kMaxReachForce : kMaxReachField);
-  if (done_count && *done_count >= done_total) return;
-  __shared__ float s_tbl[40];
-  __shared__ float4 s_tp[4][kT], s_tm[4][kT];
-  __shared__ int32_t s_cb[4][kCells], s_co[4][kCells + 1], s_pl[4][kCells];
-  if (threadIdx.x < 40) s_tbl[threadIdx.x] = c_fit_tbl[threadIdx.x];
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int wi = threadIdx.x >> 5;
-  const int64_t n_warps = int64_t(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + wi; c < n_cells; c += n_warps) {
-    const int32_t cb = start[c], ce = start[c + 1];
-    if (cb == ce) continue;
-    int lo = 0, hi = n_scenes - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (grids[mid].cell_off <= c) lo = mid;
-      else hi = mid - 1;
-    }
-    if (done_flags && done_flags[int64_t(lo) * done_stride] != 0.0) continue;  // scene's solve stopped
-    if (skip_scene && skip_scene[lo]) continue;  // scene evaluated by the exact-branch kernels
-    const CellGrid& g = grids[lo];
-    const int64_t lc = c - g.cell_off;
-    const int ix = int(lc % g.nx), iy = int((lc / g.nx) % g.ny), iz = int(lc / (int64_t(g.nx) * g.ny));
-    const int R = kForce ? g.reach_force : g.reach_field;
-    const float near2 = kForce ? g.pc.near2_force : g.pc.near2_field;
-    const float inv_h = g.pc.inv_h, ih3 = g.pc.ih3, ih4k = g.pc.ih4_over_k;
-    float cA, cB;
-    if (kForce) clamped_force_coeffs(near2, cA, cB);
-    else clamped_field_coeffs(near2, cA, cB);
-    // Candidate cells: slot 0 the cell itself (plane 1), then the non-empty
-    // half-stencil cells within reach (plane 2 + offset index), compacted.
-    const int nh = half_count(R);
-    __syncwarp();
-    if (lane == 0) {
-      s_cb[wi][0] = cb;
-      s_co[wi][0] = 0;
-      s_co[wi][1] = ce - cb;
-      s_pl[wi][0] = 1;
-    }
-    int n_list = 1;
-    int32_t total = ce - cb;
-    for (int k0 = 0; k0 < nh; k0 += 32) {
-      const int k = k0 + lane;
-      int32_t sb = 0, len = 0;
-      if (k < nh) {
-        int dx, dy, dz;
-        half_offset(R, k, dx, dy, dz);
-        const int cx = ix + dx, cy = iy + dy, cz = iz + dz;
-        if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz &&
-            in_reach(g, R, near2, dx, dy, dz)) {
-          const int64_t cc = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx + cx;
-          sb = start[cc];
-          len = start[cc + 1] - sb;
-        }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, len > 0);
-      int32_t inc = len;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += v;
-      }
-      if (len > 0) {
-        const int slot = n_list + __popc(m & ((1u << lane) - 1u));
-        s_cb[wi][slot] = sb;
-        s_co[wi][slot + 1] = total + inc;
-        s_pl[wi][slot] = 2 + k;
-      }
-      n_list += __popc(m);
-      total += __shfl_sync(0xffffffffu, inc, 31);
-    }
-    __syncwarp();
-    for (int32_t t0 = cb; t0 < ce; t0 += kT) {
-      const int nt = min(kT, ce - t0);
-      __syncwarp();
-      if (lane < nt) {
-        s_tp[wi][lane] = spos[t0 + lane];
-        s_tm[wi][lane] = smom[t0 + lane];
-      }
-      __syncwarp();
-      float acc[kT][3];
-#pragma unroll
-      for (int t = 0; t < kT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = 0.f;
-      int r = 0;  // this lane's cell cursor (its candidates only increase)
-      for (int32_t k = lane; k < total; k += 32) {
-        while (s_co[wi][r + 1] <= k) ++r;
-        const int32_t q = s_cb[wi][r] + (k - s_co[wi][r]);
-        const int pl = s_pl[wi][r];
-        const float4 pj = spos[q];
-        const float4 mj = smom[q];
-        float src[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int t = 0; t < kT; ++t) {
-          // Own cell: the pair once, with the later particle as the candidate;
-          // the target itself on its own side only.
-          const int32_t tq = t0 + t;
-          if (t < nt && (pl != 1 || q >= tq)) {
-            const float4 tp = s_tp[wi][t];
-            const float dx = tp.x - pj.x, dy2 = tp.y - pj.y, dz2 = tp.z - pj.z;
-            const float r2 = dx * dx + dy2 * dy2 + dz2 * dz2;
-            if (kForce ? (r2 <= near2) : (r2 < near2)) {
-              const bool both = q != tq;
-              if (kForce) {
-                const float4 tm = s_tm[wi][t];
-                float P, Q;
-                force_near_coeffs_fast(r2, s_tbl, inv_h, ih4k, P, Q);
-                const float dP = P - cA, dQ = Q - cB;
-                const float ds = dx * mj.x + dy2 * mj.y + dz2 * mj.z;
-                const float dm = dx * tm.x + dy2 * tm.y + dz2 * tm.z;
-                const float sm = mj.x * tm.x + mj.y * tm.y + mj.z * tm.z;
-                const float u = dP * ds, v = dP * dm, wv = dP * sm + dQ * ds * dm;
-                const float f0 = dx * wv + tm.x * u + mj.x * v;
-                const float f1 = dy2 * wv + tm.y * u + mj.y * v;
-                const float f2 = dz2 * wv + tm.z * u + mj.z * v;
-                acc[t][0] += f0;
-                acc[t][1] += f1;
-                acc[t][2] += f2;
-                if (both) {  // f_ji = -f_ij
-                  src[0] -= f0;
-                  src[1] -= f1;
-                  src[2] -= f2;
-                }
-              } else {
-                float al, be;
-                field_near_coeffs_fast(r2, inv_h, ih3, al, be);
-                const float da3 = 3.f * (al - cA), db = be - cB;
-                const float t3 = (dx * mj.x + dy2 * mj.y + dz2 * mj.z) * da3;
-                acc[t][0] += dx * t3 - mj.x * db;
-                acc[t][1] += dy2 * t3 - mj.y * db;
-                acc[t][2] += dz2 * t3 - mj.z * db;
-                if (both) {  // the same tensor (even in d) on the target's dipole
-                  const float4 tm = s_tm[wi][t];
-                  const float s3 = (dx * tm.x + dy2 * tm.y + dz2 * tm.z) * da3;
-                  src[0] += dx * s3 - tm.x * db;
-                  src[1] += dy2 * s3 - tm.y * db;
-                  src[2] += dz2 * s3 - tm.z * db;
-                }
-              }
-            }
-          }
-        }
-        float* dst = part + int64_t(pl) * 3 * stride + q;
-        if (t0 == cb) {
-          dst[0] = src[0];
-          dst[stride] = src[1];
-          dst[2 * stride] = src[2];
-        } else {
-          dst[0] += src[0];
-          dst[stride] += src[1];
-          dst[2 * stride] += src[2];
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < kT; ++t) {
-        if (t < nt) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            float v = acc[t][k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            acc[t][k] = v;
-          }
-          if (lane == 0) {
-            part[t0 + t] = acc[t][0];
-            part[stride + t0 + t] = acc[t][1];
-            part[2 * stride + t0 + t] = acc[t][2];
-          }
-        }
-      }
-    }
-  }
-}
-
-// corr[perm[q]] = plane 0 + plane 1 + the planes of q's writer cells, in the
-// output units.  Skips the cells the writer skipped.  One warp per cell: the
-// writer planes are listed once per cell in shared memory; lane (slot p, group
-// g) takes particle p of a round of 8 and the listed planes g, g + 4, ...,
-// four independent loads in flight, each group's sum compensated, and the
-// groups are added by a fixed shuffle tree.
-template <bool kForce>
-__global__ void __launch_bounds__(128) k_correction_gather(const CellGrid* __restrict__ grids, int n_scenes,
-                                                           int64_t n_cells, const int32_t* __restrict__ perm,
-                                                           const int32_t* __restrict__ start,
-                                                           const float* __restrict__ part, int64_t stride,
-                                                           float4* __restrict__ corr,
-                                                           const int32_t* __restrict__ skip_scene,
-                                                           const double* __restrict__ done_flags, int done_stride,
-                                                           const int32_t* __restrict__ done_count, int done_total) {
-  constexpr int kPlanes = half_planes(kForce);
-  if (done_count && *done_count >= done_total) return;
-  __shared__ int32_t s_list[4][kPlanes];
-  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-  const int slot = lane & 7, grp = lane >> 3;
-  const int64_t n_warps = int64_t(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t c = int64_t(blockIdx.x) * (blockDim.x >> 5) + wi; c < n_cells; c += n_warps) {
-    const int32_t cb = start[c], ce = start[c + 1];
-    if (cb == ce) continue;
-    int lo = 0, hi = n_scenes - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (grids[mid].cell_off <= c) lo = mid;
-      else hi = mid - 1;
-    }
-    if (done_flags && done_flags[int64_t(lo) * done_stride] != 0.0) continue;
-    if (skip_scene && skip_scene[lo]) continue;
-    const CellGrid& g = grids[lo];
-    const int64_t lc = c - g.cell_off;
-    const int ix = int(lc % g.nx), iy = int((lc / g.nx) % g.ny), iz = int(lc / (int64_t(g.nx) * g.ny));
-    const int R = kForce ? g.reach_force : g.reach_field;
-    const float near2 = kForce ? g.pc.near2_force : g.pc.near2_field;
-    const int nh = half_count(R);
-    // Planes to add: 0 and 1, then 2 + k for each writer cell c - o_k
-    // (inside the grid, within reach, not empty), in increasing k.
-    __syncwarp();
-    if (lane < 2) s_list[wi][lane] = lane;
-    int np = 2;
-    for (int k0 = 0; k0 < nh; k0 += 32) {
-      const int k = k0 + lane;
-      bool v = false;
-      if (k < nh) {
-        int dx, dy, dz;
-        half_offset(R, k, dx, dy, dz);
-        const int cx = ix - dx, cy = iy - dy, cz = iz - dz;
-        if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz &&
-            in_reach(g, R, near2, dx, dy, dz)) {
-          const int64_t cc = g.cell_off + (int64_t(cz) * g.ny + cy) * g.nx + cx;
-          v = start[cc + 1] > start[cc];
-        }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, v);
-      if (v) s_list[wi][np + __popc(m & ((1u << lane) - 1u))] = 2 + k;
-      np += __popc(m);
-    }
-    __syncwarp();
-    const float scale = kForce ? float(kForceK) : float(kInv4Pi);
-    for (int32_t q0 = cb; q0 < ce; q0 += 8) {
-      const int32_t q = q0 + slot;
-      const bool live = q < ce;
-      const int32_t qq = live ? q : cb;
-      float s[4][3], e[4][3];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) s[u][k] = e[u][k] = 0.f;
-      for (int j = grp; j < np; j += 16) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int jj = j + 4 * u;
-          if (jj < np) {
-            const float* src = part + int64_t(s_list[wi][jj]) * 3 * stride + qq;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) two_sum_acc(s[u][k], e[u][k], src[int64_t(k) * stride]);
-          }
-        }
-      }
-      float tot[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float v = ((s[0][k] + e[0][k]) + (s[1][k] + e[1][k])) + ((s[2][k] + e[2][k]) + (s[3][k] + e[3][k]));
-        v += __shfl_xor_sync(0xffffffffu, v, 8);
-        v += __shfl_xor_sync(0xffffffffu, v, 16);
-        tot[k] = v;
-      }
-      if (live && grp == 0) corr[perm[q]] = make_float4(tot[0] * scale, tot[1] * scale, tot[2] * scale, 0.f);
-    }
-  }
-}
-
 // Targets are either the binned particles themselves (tpos == nullptr; they
 // are visited in cell order so a warp's neighbours share cells) or a separate
 // set tpos[0..n_total) of targets of scene 0.
@@ -857,7 +533,7 @@ void to_pairs(const float4* src, float4* dst, int64_t n, cudaStream_t st, const 
 }
 
 mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st,
-                          double margin_h, bool pair_planes) {
+                          double margin_h) {
   const int ns = int(scenes.size());
   if (ns == 0) return fail(MF_ERR_INVALID_ARG, "cell list: no scenes");
   n_scenes_ = ns;
@@ -936,7 +612,6 @@ mf_status CellList::build(const float4* pos4, const std::vector<CellSceneSpec>& 
   MF_TRY(cell_of_.reserve(sizeof(int32_t) * size_t(n_total_)));
   MF_TRY(spos_.reserve(sizeof(float4) * size_t(n_total_)));
   MF_TRY(smom_.reserve(sizeof(float4) * size_t(n_total_)));
-  if (pair_planes) MF_TRY(cpart_.reserve_grow(size_t(half_planes(true)) * 3 * size_t(n_total_) * sizeof(float)));
   return rebin(pos4, st);
 }
 
@@ -964,14 +639,6 @@ mf_status CellList::rebin(const float4* pos4, cudaStream_t st) {
   return MF_OK;
 }
 
-static int half_mode() {
-  static const int m = [] {
-    const char* e = getenv("MF_CORR_HALF");
-    return e ? atoi(e) : 0;
-  }();
-  return m;
-}
-
 static unsigned cell_grid(int64_t cells) {
   int64_t g = cells;
   if (g > 65535) g = 65535;
@@ -983,26 +650,9 @@ mf_status CellList::field_correction(const float4* pos4, const float4* mom4, flo
                                      int done_total) const {
   k_gather_sorted<<<grid_for(n_total_), 256, 0, st>>>(perm_.as<int32_t>(), pos4, mom4, n_total_, spos_.as<float4>(),
                                                       smom_.as<float4>(), done_count, done_total);
-  const int32_t* skip = skip_field_on_ ? skip_field_.as<int32_t>() : nullptr;
-  if (half_mode() == 1 || half_mode() == 2) {
-    MF_TRY(cpart_.reserve_grow(size_t(half_planes(false)) * 3 * size_t(n_total_) * sizeof(float)));
-    if (half_mode() == 2) k_correction_half<false, 16><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, cell_start_.as<int32_t>(), spos_.as<float4>(), smom_.as<float4>(),
-        cpart_.as<float>(), n_total_, skip, done_flags, done_stride, done_count, done_total);
-    else k_correction_half<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, cell_start_.as<int32_t>(), spos_.as<float4>(), smom_.as<float4>(),
-        cpart_.as<float>(), n_total_, skip, done_flags, done_stride, done_count, done_total);
-    k_correction_gather<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), cpart_.as<float>(),
-        n_total_, corr, skip, done_flags, done_stride, done_count, done_total);
-  } else {
-  if (half_mode() == 3) k_correction_cells<false, 16><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
+  k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip, done_flags, done_stride, done_count, done_total);
-  else k_correction_cells<false><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip, done_flags, done_stride, done_count, done_total);
-  }
+      smom_.as<float4>(), corr, skip_field_on_ ? skip_field_.as<int32_t>() : nullptr, done_flags, done_stride, done_count, done_total);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }
@@ -1047,26 +697,9 @@ mf_status CellList::set_skips(const std::vector<int32_t>& field, const std::vect
 mf_status CellList::force_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st) const {
   k_gather_sorted<<<grid_for(n_total_), 256, 0, st>>>(perm_.as<int32_t>(), pos4, mom4, n_total_, spos_.as<float4>(),
                                                       smom_.as<float4>(), nullptr, 0);
-  const int32_t* skip = skip_force_on_ ? skip_force_.as<int32_t>() : nullptr;
-  if (half_mode() == 1 || half_mode() == 2) {
-    MF_TRY(cpart_.reserve_grow(size_t(half_planes(true)) * 3 * size_t(n_total_) * sizeof(float)));
-    if (half_mode() == 2) k_correction_half<true, 16><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, cell_start_.as<int32_t>(), spos_.as<float4>(), smom_.as<float4>(),
-        cpart_.as<float>(), n_total_, skip, nullptr, 0, nullptr, 0);
-    else k_correction_half<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, cell_start_.as<int32_t>(), spos_.as<float4>(), smom_.as<float4>(),
-        cpart_.as<float>(), n_total_, skip, nullptr, 0, nullptr, 0);
-    k_correction_gather<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-        grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), cpart_.as<float>(),
-        n_total_, corr, skip, nullptr, 0, nullptr, 0);
-  } else {
-  if (half_mode() == 3) k_correction_cells<true, 16><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
+  k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
       grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip, nullptr, 0, nullptr, 0);
-  else k_correction_cells<true><<<cell_grid((n_cells_ + 3) / 4), 128, 0, st>>>(
-      grids_.as<CellGrid>(), n_scenes_, n_cells_, perm_.as<int32_t>(), cell_start_.as<int32_t>(), spos_.as<float4>(),
-      smom_.as<float4>(), corr, skip, nullptr, 0, nullptr, 0);
-  }
+      smom_.as<float4>(), corr, skip_force_on_ ? skip_force_.as<int32_t>() : nullptr, nullptr, 0, nullptr, 0);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

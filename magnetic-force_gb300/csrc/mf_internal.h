@@ -340,11 +340,8 @@ class CellList {
   // Bins the particles of every scene into cells of edge >= 2h; particles of
   // a cell are listed in increasing index order (deterministic sums).
   // Synchronises `st` once (the bounding boxes are read on the host).
-  // pair_planes: also reserve the partial sums of the corrections once per
-  // pair (~4.4 KB per particle), so later corrections, also inside a CUDA
-  // graph capture, allocate nothing; otherwise the first correction does.
   mf_status build(const float4* pos4, const std::vector<CellSceneSpec>& scenes, cudaStream_t st,
-                  double margin_h = 0.0, bool pair_planes = false);
+                  double margin_h = 0.0);
   // Re-bins moved particles on the grids of the last build (no host
   // synchronisation, so it can be captured in a CUDA graph).  Particles that
   // left a grid are binned into its border cells, which keeps every
@@ -352,8 +349,7 @@ class CellList {
   mf_status rebin(const float4* pos4, cudaStream_t st);
   // corr_i = sum over j within 2h (resp. 4h) of [exact pair term - the
   // clamped far term the packed all-pairs loop gave that pair], in the
-  // all-pairs kernels' output units.  Targets = sources = the binned set;
-  // each unordered near pair is evaluated once.
+  // all-pairs kernels' output units.  Targets = sources = the binned set.
   // done_flags (per-scene solver rows) skip stopped scenes; done_count /
   // done_total make the launch a no-op once every scene has stopped.
   mf_status field_correction(const float4* pos4, const float4* mom4, float4* corr, cudaStream_t st,
@@ -382,7 +378,6 @@ class CellList {
   DevBuf skip_field_, skip_force_;  // per scene: 1 = not on the packed path
   bool skip_field_on_ = false, skip_force_on_ = false;  // a list is in use
   DevBuf spos_, smom_;              // positions and dipoles in cell order (per correction)
-  mutable DevBuf cpart_;            // partial sums of the correction once per pair (planes x 3 x particles)
   std::vector<CellGrid> host_grids_;
   std::vector<double> host_bbox_;
   int64_t n_total_ = 0, n_cells_ = 0;

@@ -72,9 +72,8 @@ def test_budget_enforced(mf):
         srv.submit(sc)
     assert e.value.status == 6  # MF_ERR_BUDGET
     srv.close()
-    # a budget for one request at a time (320 B of state and 366 x 12 B of
-    # correction partial sums per particle): the second waits in the queue
-    srv = mf.Server(hbm_budget_bytes=4000 * (320 + 366 * 12) + 4.2 * 1024 * 1024, steps_per_request=2)
+    # a budget for one request at a time: the second waits in the queue
+    srv = mf.Server(hbm_budget_bytes=4000 * 320 + 4.2 * 1024 * 1024, steps_per_request=2)
     a, b = srv.submit(sc), srv.submit(sc)
     srv.step()
     assert srv.poll(a)[0] == 1 and srv.poll(b)[0] == 0
