@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MF_ABI_VERSION 2
+#define MF_ABI_VERSION 3
 
 typedef enum mf_status {
   MF_OK = 0,
@@ -117,12 +117,16 @@ typedef enum mf_option {
                                the force's near field is evaluated once per unordered box
                                pair with 2, and with 1 from 1,048,576 particles on.  Not in
                                the reference. */
-  MF_OPT_FMM_FORCE_THETA = 15 /* aperture of the Kelvin force (and the external gradient tensor)
-                               products on the FMM path, default 0.32; they use the smaller of
+  MF_OPT_FMM_FORCE_THETA = 15,/* aperture of the Kelvin force (and the external gradient tensor)
+                               products on the FMM path, default 0.36; they use the smaller of
                                this and MF_OPT_FMM_THETA.  The force takes the Hessian of the
                                local expansion, whose error relative to the small net force
                                of a magnetised body is ~40x the field's: 1.3e-4 at 0.5 and
-                               4.7e-6 at 0.32 (P = 8, 1,048,576 particles).  Not in the reference. */
+                               P = 8, 4.8e-6 at 0.36 and P = 9 (1,048,576 particles).  Not in
+                               the reference. */
+  MF_OPT_FMM_FORCE_ORDER = 16 /* expansion order P of those products (4..9), default 9: one degree
+                               more than the field's default lets the wider aperture meet 1e-5
+                               with fewer near pairs.  Not in the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -335,8 +339,9 @@ typedef struct mf_fmm mf_fmm;
 /* targets may be NULL (nt ignored): the targets are the sources.  order is
  * P as the reference counts it (4..8), theta the acceptance aperture of the
  * field product, leaf_min the mean particles per leaf box.  The Hessian
- * product uses the aperture min(theta, 0.32), as the handles' force does
- * (MF_OPT_FMM_FORCE_THETA): its lists are built on its first call. */
+ * product uses the aperture min(theta, 0.36) and the order 9, as the
+ * handles' force does (MF_OPT_FMM_FORCE_THETA, MF_OPT_FMM_FORCE_ORDER): its
+ * lists are built on its first call. */
 mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, int64_t nt, float h, int32_t order,
                         double theta, int32_t leaf_min, int32_t device, mf_fmm** out);
 mf_status mf_fmm_destroy(mf_fmm* f);

@@ -500,6 +500,11 @@ class Engine final : public EngineBase {
         fmm_cfg_.theta_force = v;
         fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;
+      case MF_OPT_FMM_FORCE_ORDER:
+        if (v < 4 || v > 9 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm force order must be 4..9");
+        fmm_cfg_.order_force = int(v);
+        fmmf_dirty_ = ext_fmm_dirty_ = true;
+        return MF_OK;
       case MF_OPT_FMM_LEAF:
         if (v < 1 || v > 4096) return fail(MF_ERR_INVALID_ARG, "fmm leaf size must be 1..4096");
         fmm_cfg_.leaf_min = int(v);
@@ -540,6 +545,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_ORDER: *v = fmm_cfg_.order; return MF_OK;
       case MF_OPT_FMM_THETA: *v = fmm_cfg_.theta; return MF_OK;
       case MF_OPT_FMM_FORCE_THETA: *v = fmm_cfg_.theta_force; return MF_OK;
+      case MF_OPT_FMM_FORCE_ORDER: *v = fmm_cfg_.force_order(); return MF_OK;
       case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
       case MF_OPT_AUTOTUNE: *v = double(int(tune_)); return MF_OK;
       case MF_OPT_PAIR_SYMMETRIC: *v = double(sym_mode_); return MF_OK;
@@ -953,9 +959,10 @@ class Engine final : public EngineBase {
         if (!leaf_set_) ce.leaf_min = kExtLeafMin;
         MF_TRY(ext_fmm_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, ce, st_));
         ctr_.kernel_launches += 17;
-        if (fmm_cfg_.force_theta() < fmm_cfg_.theta) {
+        if (fmm_cfg_.force_tree()) {
           FmmConfig ct = ce;
           ct.theta = fmm_cfg_.force_theta();
+          ct.order = fmm_cfg_.force_order();
           MF_TRY(ext_fmmt_.build(sp, n_ext_, pos4(), np_, double(ext_h_), bbox, ct, st_));
           ctr_.kernel_launches += 17;
         }
@@ -980,7 +987,7 @@ class Engine final : public EngineBase {
       t.corr4 = corr;
       for (int k = 0; k < 9; ++k) t.out[k] = rext(k);
       t.err = scr_.err.template as<int32_t>();
-      Fmm& ft = fmm_cfg_.force_theta() < fmm_cfg_.theta ? ext_fmmt_ : ext_fmm_;
+      Fmm& ft = fmm_cfg_.force_tree() ? ext_fmmt_ : ext_fmm_;
       MF_TRY(ft.product(2, sp, sm, t, plan_ext_tensor_.host[0], st_, nullptr));
       ctr_.kernel_launches += ext_fmm_.launches_per_product() + ft.launches_per_product() + 2;
     }
@@ -1002,7 +1009,7 @@ class Engine final : public EngineBase {
   // aperture is the field's, else fmmf_ built at the smaller one.
   mf_status ensure_fmm_force(Fmm** out) {
     if constexpr (kF32) {
-      if (fmm_cfg_.force_theta() >= fmm_cfg_.theta) {
+      if (!fmm_cfg_.force_tree()) {
         MF_TRY(ensure_fmm());
         *out = &fmm_;
         return MF_OK;
@@ -1011,6 +1018,7 @@ class Engine final : public EngineBase {
       if (fmmf_dirty_) {
         FmmConfig ct = fmm_cfg_;
         ct.theta = fmm_cfg_.force_theta();
+        ct.order = fmm_cfg_.force_order();
         MF_TRY(fmmf_.build(pos4(), np_, nullptr, 0, h_, cells_.bbox(0), ct, st_));
         ctr_.kernel_launches += 8;
         fmmf_dirty_ = false;

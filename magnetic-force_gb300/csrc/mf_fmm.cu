@@ -43,7 +43,7 @@
 namespace mfgb {
 namespace {
 
-constexpr int kMaxDegree = 7;  // P = 8
+constexpr int kMaxDegree = 8;  // P = 9
 constexpr int kMaxLevel = 10;
 
 // Multi-indices in graded order: degree n, then s = y + z, then z.
@@ -208,7 +208,8 @@ __global__ void k_fmm_m2l_stats(FmmLevel lv, const int32_t* __restrict__ occ, co
 // ---------------------------------------------------------------------------
 // Upward pass
 // ---------------------------------------------------------------------------
-// Leaf multipoles, one CTA per box, one thread per coefficient alpha:
+// Leaf multipoles, one CTA per box, one thread per coefficient alpha (two for
+// degree 8, whose 164 coefficients outnumber the threads):
 //   M_alpha = (-1)^|alpha| sum_j sum_k m_jk u_j^(alpha - e_k) / (alpha - e_k)!,
 // u_j = (y_j - centre) / edge.
 template <int Q>
@@ -217,23 +218,33 @@ __global__ void __launch_bounds__(128) k_fmm_p2m(FmmLevel lv, const int32_t* __r
                                                  const float4* __restrict__ pos4, const float4* __restrict__ mom4,
                                                  float* __restrict__ M, const double* __restrict__ done) {
   constexpr int NC = ncoef(Q) - 1;
+  constexpr int KPT = (NC + 127) / 128;  // coefficients per thread
   constexpr int W = 3 * Q + 3;  // powers u^i/i! (i < Q) per axis, then the dipole
   if (done && *done != 0.0) return;
   __shared__ float s_p[128][W + 1];
   const int tid = threadIdx.x;
-  const bool act = tid < NC;
-  int ax = 0, ay = 0, az = 0;
-  if (act) {
-    const char4 e = c_mi[tid + 1];
-    ax = e.x;
-    ay = e.y;
-    az = e.z;
+  bool act[KPT];
+  int ax[KPT], ay[KPT], az[KPT];
+  float sign[KPT];
+#pragma unroll
+  for (int r = 0; r < KPT; ++r) {
+    const int k = tid + 128 * r;
+    act[r] = k < NC;
+    ax[r] = ay[r] = az[r] = 0;
+    if (act[r]) {
+      const char4 e = c_mi[k + 1];
+      ax[r] = e.x;
+      ay[r] = e.y;
+      az[r] = e.z;
+    }
+    sign[r] = ((ax[r] + ay[r] + az[r]) & 1) ? -1.f : 1.f;
   }
-  const float sign = ((ax + ay + az) & 1) ? -1.f : 1.f;
   const float inv_s = 1.f / lv.side;
   for (int64_t c = blockIdx.x; c < lv.nbox; c += gridDim.x) {
     const int32_t n = cnt[c];
-    float acc = 0.f;
+    float acc[KPT];
+#pragma unroll
+    for (int r = 0; r < KPT; ++r) acc[r] = 0.f;
     if (n > 0) {
       const int ix = int(c % lv.nx), iy = int((c / lv.nx) % lv.ny), iz = int(c / (int64_t(lv.nx) * lv.ny));
       const float cx = lv.ox + (float(ix) + 0.5f) * lv.side;
@@ -262,19 +273,24 @@ __global__ void __launch_bounds__(128) k_fmm_p2m(FmmLevel lv, const int32_t* __r
           s_p[tid][3 * Q + 2] = m.z;
         }
         __syncthreads();
-        if (act) {
-          for (int j = 0; j < nj; ++j) {
-            const float* q = s_p[j];
-            float t = 0.f;
-            if (ax > 0) t += q[3 * Q] * q[ax - 1] * q[Q + ay] * q[2 * Q + az];
-            if (ay > 0) t += q[3 * Q + 1] * q[ax] * q[Q + ay - 1] * q[2 * Q + az];
-            if (az > 0) t += q[3 * Q + 2] * q[ax] * q[Q + ay] * q[2 * Q + az - 1];
-            acc += t;
+#pragma unroll
+        for (int r = 0; r < KPT; ++r) {
+          if (act[r]) {
+            for (int j = 0; j < nj; ++j) {
+              const float* q = s_p[j];
+              float t = 0.f;
+              if (ax[r] > 0) t += q[3 * Q] * q[ax[r] - 1] * q[Q + ay[r]] * q[2 * Q + az[r]];
+              if (ay[r] > 0) t += q[3 * Q + 1] * q[ax[r]] * q[Q + ay[r] - 1] * q[2 * Q + az[r]];
+              if (az[r] > 0) t += q[3 * Q + 2] * q[ax[r]] * q[Q + ay[r]] * q[2 * Q + az[r] - 1];
+              acc[r] += t;
+            }
           }
         }
       }
     }
-    if (act) M[int64_t(tid) * lv.nbox + c] = sign * acc;
+#pragma unroll
+    for (int r = 0; r < KPT; ++r)
+      if (act[r]) M[int64_t(tid + 128 * r) * lv.nbox + c] = sign[r] * acc[r];
   }
 }
 
@@ -1079,7 +1095,7 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
   if (tpos4 && nt <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no targets");
   separate_ = tpos4 != nullptr;
   nt_ = separate_ ? nt : n;
-  if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 8]");
+  if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 9]");
   if (!(cfg.theta > 0.0 && cfg.theta <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm: theta must be in (0, 1]");
   if (cfg.leaf_min < 1) return fail(MF_ERR_INVALID_ARG, "fmm: leaf_min must be >= 1");
   cfg_ = cfg;
@@ -1414,6 +1430,7 @@ mf_status Fmm::product(int kind, const float4* pos4, const float4* smom, const A
     case 5: return product_q<5>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     case 6: return product_q<6>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     case 7: return product_q<7>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 8: return product_q<8>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
   }
 }
@@ -1466,6 +1483,21 @@ struct M2LVariants<7> {
     else k_fmm_m2l<7, 1, 3><<<g, 128, 0, st>>>(p);
     k_fmm_m2l<7, 4, 7><<<g, 128, 0, st>>>(p);
     *n += 2;
+  }
+};
+template <>
+struct M2LVariants<8> {
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (hess) {
+      k_fmm_m2l<8, 2, 3><<<g, 128, 0, st>>>(p);
+      k_fmm_m2l<8, 4, 5><<<g, 128, 0, st>>>(p);
+      k_fmm_m2l<8, 6, 8><<<g, 128, 0, st>>>(p);
+    } else {
+      k_fmm_m2l<8, 1, 2><<<g, 128, 0, st>>>(p);
+      k_fmm_m2l<8, 3, 4><<<g, 128, 0, st>>>(p);
+      k_fmm_m2l<8, 5, 8><<<g, 128, 0, st>>>(p);
+    }
+    *n += 3;
   }
 };
 // One CTA of 128 threads per leaf box, 256-source stages, also for small
@@ -1774,10 +1806,11 @@ mf_status mf_fmm_hessian(mf_fmm* f, const float* charges, float* results9) {
     for (int k = 0; k < 9; ++k) a.out[k] = x.out9.as<float>() + size_t(k) * size_t(x.nt);
     a.err = x.scr.err.as<int32_t>();
     Fmm* fh = &x.fmm;
-    if (x.cfg.force_theta() < x.cfg.theta) {
+    if (x.cfg.force_tree()) {
       if (!x.fmmh_built) {
         FmmConfig ct = x.cfg;
         ct.theta = x.cfg.force_theta();
+        ct.order = x.cfg.force_order();
         MF_TRY(x.fmmh.build(x.spos.as<float4>(), x.ns, x.same ? nullptr : x.tpos.as<float4>(), x.nt, x.h, x.bbox, ct,
                             x.st));
         x.fmmh_built = true;
@@ -1817,7 +1850,7 @@ mf_status mf_fmm_get_stats(mf_fmm* f, mf_fmm_stats* out) {
     if (x.fmmh_built) {
       out->force_p2p_pairs = x.fmmh.stats().p2p_pairs;
       out->force_m2l_per_product = x.fmmh.stats().m2l_per_product;
-    } else if (x.cfg.force_theta() >= x.cfg.theta) {
+    } else if (!x.cfg.force_tree()) {
       out->force_p2p_pairs = s.p2p_pairs;
       out->force_m2l_per_product = s.m2l_per_product;
     }

@@ -405,14 +405,24 @@ struct FmmConfig {
   // small net force, so the same truncation error is ~40x larger relative to
   // the result.  Measured against FP64 direct sums at P = 8 on a cylinder of
   // 1,048,576 particles: 1.3e-4 at 0.5, 3.1e-5 at 0.42, 9.3e-6 at 0.36,
-  // 7.6e-6 at 0.34, 4.7e-6 at 0.32, 4.0e-6 at 0.3 (field at 0.5: 3.3e-6); on
-  // the same cylinder's shape at 262,144 particles 1.3e-5 at 0.34, 6.6e-6 at
-  // 0.32 and 4.5e-6 at 0.3; spheres of 150,000-262,144 particles 2.1e-6 at
-  // 0.32.  0.32 holds every one of these within 1e-5 with a margin of 1.5x,
-  // and takes 66 against 75 ms per force product at 1,048,576 particles.
-  // The force uses min(theta, this).
-  double theta_force = 0.32;
+  // 4.7e-6 at 0.32, 4.0e-6 at 0.3 (field at 0.5: 3.3e-6).  At the default
+  // force order P = 9: 1.6e-5 at 0.44, 7.0e-6 at 0.4, 4.8e-6 at 0.36 on that
+  // cylinder; 1.6e-5 at 0.4 and 6.9e-6 at 0.36 on its shape at 262,144
+  // particles; spheres of 150,000-262,144 particles 2.0e-6 at 0.36.  0.36
+  // holds every one of these within 1e-5 with a margin of 1.4x.  The force
+  // uses min(theta, this).
+  double theta_force = 0.36;
   double force_theta() const { return theta_force < theta ? theta_force : theta; }
+  // Expansion order of the Kelvin force and force-tensor products (0: the
+  // field's).  One degree more than the field lets the force take a wider
+  // aperture for the same error, so fewer near pairs: at P = 9 and 0.36 the
+  // force error is 4.8e-6 on the 1,048,576-particle cylinder (P = 8 needs
+  // 0.32 for 4.7e-6) and 6.9e-6 on its 262,144-particle shape (6.6e-6), and
+  // a force product takes 51 against 66 ms at 1,048,576 particles.
+  int order_force = 9;
+  int force_order() const { return order_force > 0 ? order_force : order; }
+  // Whether the force products need lists or expansions of their own.
+  bool force_tree() const { return force_theta() < theta || force_order() != order; }
 };
 
 // One level of the uniform box grid (level 0 is one box holding the scene).

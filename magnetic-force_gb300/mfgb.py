@@ -40,7 +40,8 @@ Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyfor
      "dHextdx": 5, "dHextdy": 6, "dHextdz": 7, "velocity": 8}
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
        "crit_size": 6, "check_interval": 7, "kernel_timing": 8, "fmm": 9, "fmm_order": 10, "fmm_theta": 11,
-       "fmm_leaf": 12, "autotune": 13, "pair_symmetric": 14, "fmm_force_theta": 15}
+       "fmm_leaf": 12, "autotune": 13, "pair_symmetric": 14, "fmm_force_theta": 15,
+       "fmm_force_order": 16}
 FMM_AUTO, FMM_ON, FMM_OFF = 0, 1, 2
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
