@@ -97,7 +97,7 @@ typedef enum mf_option {
                                force above 131,072; all-pairs below), 1 always the FMM,
                                2 always all-pairs.  FP64 handles are all-pairs. */
   MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
-                               (terms of degree n < P): 4..8, default 8.  The reference's
+                               (terms of degree n < P): 4..9, default 8.  The reference's
                                default is 6 (magnetic_force.cu:661); at 6 the field here is
                                3e-5 from FP64 direct sums, at 8 2-3e-6. */
   MF_OPT_FMM_THETA = 11,    /* multipole acceptance aperture of the field products, default 0.5
@@ -337,7 +337,7 @@ mf_status mf_debug_stage_wait_limit(int64_t limit);
 /* ---------------------------------------------------------------------- */
 typedef struct mf_fmm mf_fmm;
 /* targets may be NULL (nt ignored): the targets are the sources.  order is
- * P as the reference counts it (4..8), theta the acceptance aperture of the
+ * P as the reference counts it (4..9), theta the acceptance aperture of the
  * field product, leaf_min the mean particles per leaf box.  The Hessian
  * product uses the aperture min(theta, 0.36) and the order 9, as the
  * handles' force does (MF_OPT_FMM_FORCE_THETA, MF_OPT_FMM_FORCE_ORDER): its

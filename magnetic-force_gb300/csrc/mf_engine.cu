@@ -486,7 +486,7 @@ class Engine final : public EngineBase {
         return MF_OK;
       }
       case MF_OPT_FMM_ORDER:
-        if (v < 4 || v > 8 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..8");
+        if (v < 4 || v > 9 || v != std::floor(v)) return fail(MF_ERR_INVALID_ARG, "fmm order must be 4..9");
         fmm_cfg_.order = int(v);
         fmm_dirty_ = fmmf_dirty_ = ext_fmm_dirty_ = true;
         return MF_OK;

@@ -151,8 +151,9 @@ def test_auto_mode_threshold(mf):
 
 def test_bad_fmm_options(mf, sphere40k):
     s = solver(mf, sphere40k)
-    for key, v in (("fmm", 3), ("fmm_order", 3), ("fmm_order", 9), ("fmm_theta", 0.0), ("fmm_theta", 1.5),
-                   ("fmm_leaf", 0), ("fmm_force_theta", 0.0), ("fmm_force_theta", 1.01)):
+    for key, v in (("fmm", 3), ("fmm_order", 3), ("fmm_order", 10), ("fmm_theta", 0.0), ("fmm_theta", 1.5),
+                   ("fmm_leaf", 0), ("fmm_force_theta", 0.0), ("fmm_force_theta", 1.01), ("fmm_force_order", 3),
+                   ("fmm_force_order", 10), ("fmm_force_order", 8.5)):
         with pytest.raises(mf.MFError):
             s.set_option(key, v)
 
