@@ -29,6 +29,9 @@ Printed (rank 0, one JSON line):
              time; a Poisson stream of scenes of 1,024..262,144 particles
              served with continuous batching against the same arrivals one
              request at a time (pairs/s and p50/p99 step and request latency)
+  fmm_1048576  the 1,048,576-particle cylinder through the FMM (the fmm1m
+             workload, a few steps): effective pairs/s, step latency, product
+             times and the force's error against the FP64 oracle
   cpu_baseline  the CPU restatement of the reference's pair kernels (FP32,
              OpenMP over all host cores) on a bounded sample of the same step
 
@@ -390,10 +393,13 @@ def run_ours(args, rank, world, local):
     s.close()
 
     # the spec comparison: batched and served against plain
-    batched = served = None
+    batched = served = fmm = None
     if not args.no_compare and n == 65536:
         batched = measure_batch(args, rank, world, local, steps=args.compare_steps, plain_passes=1)
         served = measure_served(args, rank, world, local)
+        # config 3 (1,048,576 particles through the FMM), a few steps
+        fs, _, _, fmm = fmm_measure(args, rank, world, local, steps=args.compare_steps, warmup=3)
+        fs.close()
 
     if rank == 0:
         out = {
@@ -410,6 +416,7 @@ def run_ours(args, rank, world, local):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "errors": errors, "clocks": clk,
             "batched_vs_plain": summarize_batch(batched) if batched else None,
             "served_vs_plain": summarize_served(served) if served else None,
+            "fmm_1048576": summarize_fmm(fmm) if fmm else None,
             "autotune": mfgb.autotune_report(),
         }
         print(json.dumps(out), flush=True)
@@ -910,21 +917,24 @@ def run_served_plain(reqs, arrivals, args, local):
                     "replayed on the measured service times"}
 
 
-def run_fmm(args, rank, world, local):
-    """Config 3: N = 1,048,576 jittered-lattice cylinder (r = 0.3, height 1,
-    h = 2 spacings, chi = 1.5, H0 = (0,0,1)) through the FMM (P = 8, theta =
-    0.5 for the field products and 0.3 for the Kelvin force, leaf boxes of
-    >= 64 particles).  A step is one timestep as in the
-    headline workload.  value counts effective pairs (N^2 per product, the FMM
-    convention); executed near-field pairs are reported beside it.  Errors:
-    against the FP64 oracle on 2,048 seeded targets (CPU) and against the FP32
-    all-pairs direct kernel on a seeded 65,536-target subsample (GPU)."""
+FMM_FORCE_ORDER, FMM_FORCE_THETA = 9, 0.36  # the handle's defaults for the Kelvin force products
+
+
+def fmm_measure(args, rank, world, local, steps, warmup, n=1 << 20):
+    """Config 3 on one GPU: N = 1,048,576 jittered-lattice cylinder (r = 0.3,
+    height 1, h = 2 spacings, chi = 1.5, H0 = (0,0,1)) through the FMM: field
+    products at P = 8 and theta 0.5, the Kelvin force at its own P = 9 and
+    theta 0.36 (the handle's defaults), leaf boxes of >= 12 particles on
+    average.  A step is one timestep as in the headline workload; effective
+    pairs count N^2 per product (the FMM convention).  Returns the handle (still
+    open), the scene and the measured summary; errors are sampled on rank 0
+    against the FP64 oracle at 2,048 seeded targets (CPU)."""
     import torch
     import mfgb
     import scenes
 
     torch.cuda.set_device(local)
-    sc = scenes.config_fmm_1m(args.n if args.n != 65536 else 1 << 20)
+    sc = scenes.config_fmm_1m(n)
     n = sc.n
     s = mfgb.Solver(n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos, device=local)
     s.set_option("solver", mfgb.SOLVER_CG)
@@ -937,7 +947,7 @@ def run_fmm(args, rank, world, local):
     cold_iters, cold_res = s.solve(500)
     torch.cuda.synchronize()
     cold_ms = (time.perf_counter() - t0) * 1e3
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         s.advance(args.dt, 500)
     torch.cuda.synchronize()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -947,7 +957,7 @@ def run_fmm(args, rank, world, local):
     torch.cuda.synchronize()
     clocks.start()
     step_ms, iters = [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -959,6 +969,7 @@ def run_fmm(args, rank, world, local):
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
+    del flush
     ctr = s.counters()
     st = s.fmm_stats()
     ks = {k: s.kernel_stats(k) for k in ("field", "force", "fmm_near_field", "fmm_near_force", "fmm_far")}
@@ -966,7 +977,7 @@ def run_fmm(args, rank, world, local):
     t_max = allreduce_max(total_ms, world)
     pairs = allreduce_sum(ctr["field_pairs"] + ctr["force_pairs"], world)
     value = pairs / (t_max * 1e-3)
-    executed = (st["field_products"] + st["force_products"]) * st["p2p_pairs"]
+    executed = st["field_products"] * st["p2p_pairs"] + st["force_products"] * st["force_p2p_pairs"]
 
     peak, _, _ = fp32_peak(clk.get("sm_max_mhz"))
     probe = mfgb.probe_fp32_peak()
@@ -985,19 +996,16 @@ def run_fmm(args, rank, world, local):
                           "tflops": flop / (k["total_ms"] * 1e-3) / 1e12}
     far = ks["fmm_far"]
     dom = max(kern, key=lambda k: kern[k]["total_ms"])
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath) and n == 1 << 20:
-        traffic = json.load(open(tpath)).get(f"fmm_p2p_{'force' if dom.endswith('force') else 'field'}_fp32_{n}")
     roofline = {"bound": "fp32", "achieved": round(kern[dom]["tflops"], 3), "peak": round(peak, 3),
-                "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": traffic,
+                "unit": "TFLOP/s", "frac": round(kern[dom]["tflops"] / peak, 4), "traffic": None,
                 "kernel": ("k_fmm_near_sym + k_fmm_p2p<force>" if kern[dom].get("once_per_box_pair")
                            else f"k_fmm_p2p<{'force' if dom.endswith('force') else 'field'}>"),
                 "peak_source": "SMs x 128 FP32 lanes x 2 FLOP x max SM clock (nvidia-smi clocks.max.sm)",
                 "probe_tflops": round(probe, 3),
                 "kernels": kern,
                 "far_field": {"launches": far["launches"], "total_ms": round(far["total_ms"], 4),
-                              "m2l_per_product": st["m2l_per_product"]},
+                              "m2l_per_product": st["m2l_per_product"],
+                              "force_m2l_per_product": st["force_m2l_per_product"]},
                 "products_ms": {"field": ks["field"]["total_ms"] / max(ks["field"]["launches"], 1),
                                 "force": ks["force"]["total_ms"] / max(ks["force"]["launches"], 1)},
                 "note": "near-field kernels: executed pairs x minimal far-form FLOP (32 field, 53 force), or, "
@@ -1007,6 +1015,42 @@ def run_fmm(args, rank, world, local):
     if rank == 0:
         errors = sample_errors(s, sc, k=2048)
         errors["oracle"] = "FP64 CPU oracle sums over all N at 2,048 seeded targets"
+    summary = {
+        "metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": t_max / steps,
+        "config": {"workload": f"fmm_fp32_{n}: jittered lattice cylinder r=0.3 height 1, N={n}, "
+                               f"h=2*spacing={sc.h:.5f}, chi=1.5, H0=(0,0,1), FMM field P={args.fmm_order} "
+                               f"theta=0.5, force P={FMM_FORCE_ORDER} theta={FMM_FORCE_THETA}, leaf>=12, "
+                               f"dt={args.dt}, CG rel tol {args.rel_tol:g}",
+                   "N": n, "step": "one timestep: octree rebuild, warm-started CG solve (FMM products), "
+                                   "Kelvin force (FMM), symplectic Euler",
+                   "l2": "flushed before every timed step (256 MiB write, not timed)",
+                   "parallelism": f"replicas x{world}", "pairs": "effective (N^2 per product)"},
+        "field_pairs": ctr["field_pairs"], "force_pairs": ctr["force_pairs"],
+        "executed_near_pairs": executed, "fmm": st,
+        "solve_iters_per_step": iters, "step_ms": [round(v, 4) for v in step_ms],
+        "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
+        "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
+        "gpu_launches": ctr["kernel_launches"], "roofline": roofline, "errors": errors, "clocks": clk,
+    }
+    return s, sc, ctr, summary
+
+
+def run_fmm(args, rank, world, local):
+    """The fmm1m workload (config 3) as its own line: fmm_measure plus a
+    65,536-target check against the FP32 all-pairs direct kernels, the
+    end-to-end rate and the CPU baseline."""
+    import torch
+    import mfgb
+
+    s, sc, ctr, out = fmm_measure(args, rank, world, local, args.steps, args.warmup,
+                                  n=args.n if args.n != 65536 else 1 << 20)
+    n = sc.n
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath) and n == 1 << 20:
+        dom = out["roofline"]["kernel"]
+        key = "fmm_p2p_force" if "force" in dom else "fmm_p2p_field"
+        out["roofline"]["traffic"] = json.load(open(tpath)).get(f"{key}_fp32_{n}")
+    if rank == 0:
         # 65,536 seeded targets against the FP32 all-pairs direct kernels
         rng = np.random.default_rng(65536)
         idx = np.sort(rng.choice(n, size=min(65536, n), replace=False))
@@ -1014,17 +1058,15 @@ def run_fmm(args, rank, world, local):
         M = torch.from_numpy(s.M).cuda()
         b = s.total_B_over_mu0[idx].astype(np.float64)
         hext = s.Hext[idx].astype(np.float64)
-        c = sc.volume * sc.chi / (1 + sc.chi)
         G = mfgb.direct_field(pos[idx], pos, M, sc.h).double().cpu().numpy()
         r = b - hext - G  # fixed point b = Hext + G(c b), with M = c b
         T = mfgb.direct_force_tensor(pos[idx], pos, M, sc.h).double().cpu().numpy().reshape(-1, 3, 3)
         Fd = np.einsum("icr,ic->ir", T, M[idx].double().cpu().numpy())
         F = s.magnetic_bodyforce[idx].astype(np.float64)
-        errors["subsample_65536"] = {
+        out["errors"]["subsample_65536"] = {
             "fixed_point_rel_residual": float(np.linalg.norm(r) / np.linalg.norm(hext)),
             "force_rel_l2": float(np.linalg.norm(F - Fd) / np.linalg.norm(Fd)),
             "against": "FP32 all-pairs direct kernels (mf_direct_field / mf_direct_force_tensor)"}
-        del c
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(s, sc, args, world)
@@ -1037,28 +1079,27 @@ def run_fmm(args, rank, world, local):
                "sample": sample + "; value = the timed step's effective field/force pairs at these direct rates "
                                   "(the CPU evaluates them all-pairs)"}
     if rank == 0:
-        out = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic: seeded jittered-lattice cylinder (the reference ships no dataset)",
-            "config": {"workload": f"fmm_fp32_{n}: jittered lattice cylinder r=0.3 height 1, N={n}, "
-                                   f"h=2*spacing={sc.h:.5f}, chi=1.5, H0=(0,0,1), FMM P={args.fmm_order} "
-                                   f"theta=0.5 (force 0.3) leaf>=12, dt={args.dt}, CG rel tol {args.rel_tol:g}",
-                       "N": n, "step": "one timestep: octree rebuild, warm-started CG solve (FMM products), "
-                                       "Kelvin force (FMM), symplectic Euler",
-                       "l2": "flushed before every timed step (256 MiB write, not timed)",
-                       "parallelism": f"replicas x{world}", "pairs": "effective (N^2 per product)"},
-            "field_pairs": ctr["field_pairs"], "force_pairs": ctr["force_pairs"],
-            "executed_near_pairs": executed, "fmm": st,
-            "solve_iters_per_step": iters, "step_ms": [round(v, 4) for v in step_ms],
-            "p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
-            "cold_solve": {"iters": cold_iters, "rel_res": cold_res, "ms": round(cold_ms, 3)},
-            "gpu_launches": ctr["kernel_launches"], "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "errors": errors, "clocks": clk,
-        }
-        print(json.dumps(out), flush=True)
+        line = {"metric": METRIC, "value": out["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": out["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic: seeded jittered-lattice cylinder (the reference ships no dataset)"}
+        line.update({k: v for k, v in out.items() if k not in line})
+        line["cpu_baseline"] = cpu
+        line["e2e"] = e2e
+        print(json.dumps(line), flush=True)
     s.close()
+
+
+def summarize_fmm(out):
+    """The config-3 figures carried in the default line."""
+    r = out["roofline"]
+    e = out["errors"] or {}
+    return {"workload": out["config"]["workload"], "value": out["value"], "unit": out["unit"],
+            "ms_per_step": out["ms_per_step"], "p50_step_ms": out["p50_step_ms"], "p99_step_ms": out["p99_step_ms"],
+            "products_ms": r["products_ms"], "executed_near_pairs": out["executed_near_pairs"],
+            "roofline": {k: r[k] for k in ("kernel", "achieved", "peak", "unit", "frac")},
+            "errors": {k: e.get(k) for k in ("fixed_point_rel_residual", "force_rel_l2", "oracle", "sample")},
+            "solve_iters_per_step": out["solve_iters_per_step"], "clocks": out["clocks"]}
 
 
 def main():
