@@ -1048,7 +1048,8 @@ def run_fmm(args, rank, world, local):
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath) and n == 1 << 20:
         dom = out["roofline"]["kernel"]
-        key = "fmm_p2p_force" if "force" in dom else "fmm_p2p_field"
+        key = ("fmm_near_sym_force" if "near_sym" in dom else "fmm_p2p_force" if "force" in dom
+               else "fmm_p2p_field")
         out["roofline"]["traffic"] = json.load(open(tpath)).get(f"{key}_fp32_{n}")
     if rank == 0:
         # 65,536 seeded targets against the FP32 all-pairs direct kernels
