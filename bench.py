@@ -917,14 +917,14 @@ def run_served_plain(reqs, arrivals, args, local):
                     "replayed on the measured service times"}
 
 
-FMM_FORCE_ORDER, FMM_FORCE_THETA = 9, 0.36  # the handle's defaults for the Kelvin force products
+FMM_FORCE_ORDER, FMM_FORCE_THETA = 10, 0.44  # the handle's defaults for the Kelvin force products
 
 
 def fmm_measure(args, rank, world, local, steps, warmup, n=1 << 20):
     """Config 3 on one GPU: N = 1,048,576 jittered-lattice cylinder (r = 0.3,
     height 1, h = 2 spacings, chi = 1.5, H0 = (0,0,1)) through the FMM: field
-    products at P = 8 and theta 0.5, the Kelvin force at its own P = 9 and
-    theta 0.36 (the handle's defaults), leaf boxes of >= 12 particles on
+    products at P = 8 and theta 0.5, the Kelvin force at its own P = 10 and
+    theta 0.44 (the handle's defaults), leaf boxes of >= 12 particles on
     average.  A step is one timestep as in the headline workload; effective
     pairs count N^2 per product (the FMM convention).  Returns the handle (still
     open), the scene and the measured summary; errors are sampled on rank 0

@@ -118,15 +118,15 @@ typedef enum mf_option {
                                pair with 2, and with 1 from 1,048,576 particles on.  Not in
                                the reference. */
   MF_OPT_FMM_FORCE_THETA = 15,/* aperture of the Kelvin force (and the external gradient tensor)
-                               products on the FMM path, default 0.36; they use the smaller of
+                               products on the FMM path, default 0.44; they use the smaller of
                                this and MF_OPT_FMM_THETA.  The force takes the Hessian of the
                                local expansion, whose error relative to the small net force
                                of a magnetised body is ~40x the field's: 1.3e-4 at 0.5 and
-                               P = 8, 4.8e-6 at 0.36 and P = 9 (1,048,576 particles).  Not in
+                               P = 8, 6.6e-6 at 0.44 and P = 10 (1,048,576 particles).  Not in
                                the reference. */
-  MF_OPT_FMM_FORCE_ORDER = 16 /* expansion order P of those products (4..9), default 9: one degree
-                               more than the field's default lets the wider aperture meet 1e-5
-                               with fewer near pairs.  Not in the reference. */
+  MF_OPT_FMM_FORCE_ORDER = 16 /* expansion order P of those products (4..10), default 10: two
+                               degrees more than the field's default let the wider aperture
+                               meet 1e-5 with fewer near pairs.  Not in the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -339,7 +339,7 @@ typedef struct mf_fmm mf_fmm;
 /* targets may be NULL (nt ignored): the targets are the sources.  order is
  * P as the reference counts it (4..9), theta the acceptance aperture of the
  * field product, leaf_min the mean particles per leaf box.  The Hessian
- * product uses the aperture min(theta, 0.36) and the order 9, as the
+ * product uses the aperture min(theta, 0.44) and the order 10, as the
  * handles' force does (MF_OPT_FMM_FORCE_THETA, MF_OPT_FMM_FORCE_ORDER): its
  * lists are built on its first call. */
 mf_status mf_fmm_create(const float* sources, int64_t ns, const float* targets, int64_t nt, float h, int32_t order,

@@ -43,7 +43,8 @@
 namespace mfgb {
 namespace {
 
-constexpr int kMaxDegree = 8;  // P = 9
+constexpr int kMaxDegree = 9;  // P = 10 (the field products stop at degree 8)
+constexpr int kMaxFieldDegree = 8;
 constexpr int kMaxLevel = 10;
 
 // Multi-indices in graded order: degree n, then s = y + z, then z.
@@ -1095,7 +1096,7 @@ mf_status Fmm::build(const float4* pos4, int64_t n, const float4* tpos4, int64_t
   if (tpos4 && nt <= 0) return fail(MF_ERR_INVALID_ARG, "fmm: no targets");
   separate_ = tpos4 != nullptr;
   nt_ = separate_ ? nt : n;
-  if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 9]");
+  if (cfg.order < 4 || cfg.order > kMaxDegree + 1) return fail(MF_ERR_INVALID_ARG, "fmm: order must be in [4, 10]");
   if (!(cfg.theta > 0.0 && cfg.theta <= 1.0)) return fail(MF_ERR_INVALID_ARG, "fmm: theta must be in (0, 1]");
   if (cfg.leaf_min < 1) return fail(MF_ERR_INVALID_ARG, "fmm: leaf_min must be >= 1");
   cfg_ = cfg;
@@ -1431,6 +1432,9 @@ mf_status Fmm::product(int kind, const float4* pos4, const float4* smom, const A
     case 6: return product_q<6>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     case 7: return product_q<7>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     case 8: return product_q<8>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
+    case 9:
+      if (kind == 0) return fail(MF_ERR_INVALID_ARG, "fmm: order 10 is for the force products only");
+      return product_q<9>(kind, pos4, smom, a, sc, st, done, marks, sym_near);
     default: return fail(MF_ERR_INVALID_ARG, "fmm: unsupported degree");
   }
 }
@@ -1498,6 +1502,18 @@ struct M2LVariants<8> {
       k_fmm_m2l<8, 5, 8><<<g, 128, 0, st>>>(p);
     }
     *n += 3;
+  }
+};
+template <>
+struct M2LVariants<9> {
+  // The force products only (Fmm::product refuses a field product at degree 9).
+  static void launch(const M2LArgs& p, unsigned g, cudaStream_t st, int* n, bool hess) {
+    if (!hess) return;
+    k_fmm_m2l<9, 2, 3><<<g, 128, 0, st>>>(p);
+    k_fmm_m2l<9, 4, 5><<<g, 128, 0, st>>>(p);
+    k_fmm_m2l<9, 6, 7><<<g, 128, 0, st>>>(p);
+    k_fmm_m2l<9, 8, 9><<<g, 128, 0, st>>>(p);
+    *n += 4;
   }
 };
 // One CTA of 128 threads per leaf box, 256-source stages, also for small
@@ -1611,7 +1627,7 @@ mf_status Fmm::product_q(int kind, const float4* pos4, const float4* smom, const
   else if (kind == 2)
     launch_p2p<Q, 2, false>(unsigned(leaf.nbox), st, pp, a, sc);
   else
-    launch_p2p<Q, 0, false>(unsigned(leaf.nbox), st, pp, a, sc);
+    if constexpr (Q <= kMaxFieldDegree) launch_p2p<Q, 0, false>(unsigned(leaf.nbox), st, pp, a, sc);
   ++nl;
   if (marks) MF_CUDA_TRY(cudaEventRecord(marks[3], st));
   launches_ = nl;

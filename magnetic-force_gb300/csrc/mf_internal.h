@@ -411,7 +411,7 @@ struct FmmConfig {
   // particles; spheres of 150,000-262,144 particles 2.0e-6 at 0.36.  0.36
   // holds every one of these within 1e-5 with a margin of 1.4x.  The force
   // uses min(theta, this).
-  double theta_force = 0.36;
+  double theta_force = 0.44;
   double force_theta() const { return theta_force < theta ? theta_force : theta; }
   // Expansion order of the Kelvin force and force-tensor products (0: the
   // field's).  One degree more than the field lets the force take a wider
@@ -419,7 +419,7 @@ struct FmmConfig {
   // force error is 4.8e-6 on the 1,048,576-particle cylinder (P = 8 needs
   // 0.32 for 4.7e-6) and 6.9e-6 on its 262,144-particle shape (6.6e-6), and
   // a force product takes 51 against 66 ms at 1,048,576 particles.
-  int order_force = 9;
+  int order_force = 10;
   int force_order() const { return order_force > 0 ? order_force : order; }
   // Whether the force products need lists or expansions of their own.
   bool force_tree() const { return force_theta() < theta || force_order() != order; }

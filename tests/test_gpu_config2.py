@@ -61,14 +61,15 @@ def test_allpairs_solution_matches_oracle(mf, config2, rel_tol):
 
 def test_fmm_solution_matches_oracle(mf, config2):
     # Both products through the FMM at the defaults (P = 8; field aperture
-    # 0.5, force aperture 0.36, P = 9) on the same scene.
+    # 0.5, force aperture 0.44, P = 10) on the same scene.
     z = config2
     c = float(z["volume"]) * float(z["chi"]) / (1.0 + float(z["chi"]))
     s = solved(mf, z, 1e-7, fmm=mf.FMM_ON)
     st = s.fmm_stats()
     assert st["active"] == 1 and st["force_active"] == 1 and st["degree"] == 7
-    assert st["theta"] == 0.5 and abs(st["force_theta"] - 0.36) < 1e-12
-    assert st["force_p2p_pairs"] > st["p2p_pairs"]
+    assert st["theta"] == 0.5 and abs(st["force_theta"] - 0.44) < 1e-12
+    # the force's own, wider near lists (equal where the leaf boxes make them so)
+    assert st["force_p2p_pairs"] >= st["p2p_pairs"] and s.get_option("fmm_force_order") == 10
     eb = rel(s.total_B_over_mu0, z["b"])
     em = rel(s.M, c * z["b"].astype(np.float64))
     ef = rel(s.magnetic_bodyforce, z["F"])
