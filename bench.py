@@ -833,7 +833,7 @@ def measure_served(args, rank, world, local):
         "pairs": pairs, "budget_bytes": 120e9, "clocks": clk, "plain": plain,
         "note": "N <= 65,536: all-pairs batch (executed pairs); N > 65,536: own solver handle on its own host "
                 "thread and stream, field products through the FMM (P=8, effective pairs), the force all-pairs "
-                "up to 131,072 particles and through the FMM above; 20 timesteps per request, <= 4 CG "
+                "up to 90,000 particles and through the FMM above; 20 timesteps per request, <= 4 CG "
                 "iterations per step; step latency: per request timestep (batch members: their tick until the "
                 "step was done on the device; others: each timestep on their thread); tick: serving-loop "
                 "ticks in which the batch took a timestep",

@@ -94,7 +94,7 @@ typedef enum mf_option {
                                whole) with CUDA events (mf_get_kernel_stats) */
   MF_OPT_FMM = 9,           /* field and force products of FP32 handles: 0 auto (field
                                products through the FMM above 65,536 particles, the Kelvin
-                               force above 131,072; all-pairs below), 1 always the FMM,
+                               force above 90,000; all-pairs below), 1 always the FMM,
                                2 always all-pairs.  FP64 handles are all-pairs. */
   MF_OPT_FMM_ORDER = 10,    /* expansion order P counted as the reference counts it
                                (terms of degree n < P): 4..9, default 8.  The reference's

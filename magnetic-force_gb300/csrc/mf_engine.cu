@@ -181,13 +181,13 @@ struct EngineBase {
 // Particle counts above which FP32 handles take the FMM by default: the
 // field products above kFmmAutoMin, the Kelvin force above kFmmForceAutoMin.
 // The force's near field is wider (FmmConfig::theta_force), so in a compact
-// scene of up to ~130k particles it covers most of the scene, and the
-// all-pairs product once per unordered pair is as fast and exact to FP32
-// rounding (all-pairs / FMM force ms, cylinder r = 0.3 and sphere r = 0.4:
-// 6.5 / 8.4-8.8 at 98,304, 11.4 / 10.9-11.0 at 131,072, 17.5 / 14.3-16.3 at
-// 163,840, 24.8 / 17.0-17.2 at 196,608).
+// scene of up to ~90k particles it covers most of the scene, and the
+// all-pairs product once per unordered pair is faster and exact to FP32
+// rounding (all-pairs / FMM force ms at the force's P = 10 and 0.44,
+// cylinder r = 0.3 and sphere r = 0.4: 3.3 / 4.0-5.9 at 70,000, 6.5 /
+// 5.2-6.4 at 98,304, 11.4 / 6.2-7.1 at 131,072).
 constexpr int64_t kFmmAutoMin = 65536;
-constexpr int64_t kFmmForceAutoMin = 131072;
+constexpr int64_t kFmmForceAutoMin = 90000;
 // Leaf size of the external dipoles' trees unless the caller sets one.
 constexpr int kExtLeafMin = 64;
 // The external dipoles' gradient tensor (sources scattered around the body,

@@ -134,7 +134,7 @@ def test_advance_rebuilds_tree(mf, cylinder100k):
 
 def test_auto_mode_threshold(mf):
     # Field products through the FMM above 65,536 particles, the Kelvin force
-    # above 262,144 (below, its wider near field covers most of the scene).
+    # above 90,000 (below, its wider near field covers most of the scene).
     import scenes
     small = scenes.uniform_cube(65536, seed=9, volume=1e-6, chi=1.0)
     big = scenes.uniform_cube(65537, seed=9, volume=1e-6, chi=1.0)
