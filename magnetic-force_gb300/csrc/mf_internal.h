@@ -120,11 +120,11 @@ constexpr int64_t kBatchPackedForceMin = 4096;
 // (0.206 against 0.213 ms).
 constexpr int64_t kSymDirectMin = 32768;
 // FMM handles: the force's near field once per unordered box pair from this
-// size on.  With the force's aperture of 0.3 (its half stencil ~4x the
-// partial-sum planes of 0.5), force products on the r = 0.3 cylinder took
-// 84.0 against 90.2 ms for every ordered pair at 1,048,576 particles, but
-// 188.6 against 128.8 at 524,288 (leaf boxes of ~330 particles there) and
-// 49.3 against 35.3 at 262,144.
+// size on.  Measured when the force's aperture was 0.3 (its half stencil ~4x
+// the partial-sum planes of 0.5): force products on the r = 0.3 cylinder
+// took 84.0 against 90.2 ms for every ordered pair at 1,048,576 particles,
+// but 188.6 against 128.8 at 524,288 (leaf boxes of ~330 particles there)
+// and 49.3 against 35.3 at 262,144.
 constexpr int64_t kSymNearMin = 1048576;
 
 template <class Real, Body B>
@@ -403,22 +403,20 @@ struct FmmConfig {
   // Hessian of the local expansion: it converges one degree later than the
   // field, and inside a magnetised body the far boxes' Hessians cancel to a
   // small net force, so the same truncation error is ~40x larger relative to
-  // the result.  Measured against FP64 direct sums at P = 8 on a cylinder of
-  // 1,048,576 particles: 1.3e-4 at 0.5, 3.1e-5 at 0.42, 9.3e-6 at 0.36,
-  // 4.7e-6 at 0.32, 4.0e-6 at 0.3 (field at 0.5: 3.3e-6).  At the default
-  // force order P = 9: 1.6e-5 at 0.44, 7.0e-6 at 0.4, 4.8e-6 at 0.36 on that
-  // cylinder; 1.6e-5 at 0.4 and 6.9e-6 at 0.36 on its shape at 262,144
-  // particles; spheres of 150,000-262,144 particles 2.0e-6 at 0.36.  0.36
-  // holds every one of these within 1e-5 with a margin of 1.4x.  The force
-  // uses min(theta, this).
+  // the result.  Measured against FP64 direct sums on a cylinder of 1,048,576
+  // particles: at P = 8, 1.3e-4 at 0.5, 9.3e-6 at 0.36, 4.7e-6 at 0.32 (field
+  // at 0.5: 3.3e-6); at P = 9, 4.8e-6 at 0.36; at P = 10, 2.2e-5 at 0.48,
+  // 6.6e-6 at 0.44, 3.6e-6 at 0.4.  On the same cylinder's shape at 262,144
+  // particles P = 10 gives 1.2e-5 at 0.48 and 6.4e-6 at 0.44, on spheres of
+  // 150,000-262,144 particles 2.9-3.6e-6 at 0.44.  0.44 holds every one of
+  // these within 1e-5 with a margin of 1.5x.  The force uses min(theta, this).
   double theta_force = 0.44;
   double force_theta() const { return theta_force < theta ? theta_force : theta; }
   // Expansion order of the Kelvin force and force-tensor products (0: the
-  // field's).  One degree more than the field lets the force take a wider
-  // aperture for the same error, so fewer near pairs: at P = 9 and 0.36 the
-  // force error is 4.8e-6 on the 1,048,576-particle cylinder (P = 8 needs
-  // 0.32 for 4.7e-6) and 6.9e-6 on its 262,144-particle shape (6.6e-6), and
-  // a force product takes 51 against 66 ms at 1,048,576 particles.
+  // field's).  Orders above the field's let the force take a wider aperture
+  // for the same error, so fewer near pairs: at the 1,048,576-particle
+  // cylinder the force product takes 66 ms at P = 8 and 0.32, 51 at P = 9 and
+  // 0.36, 34 at P = 10 and 0.44, all within 7e-6 of the oracle.
   int order_force = 10;
   int force_order() const { return order_force > 0 ? order_force : order; }
   // Whether the force products need lists or expansions of their own.
