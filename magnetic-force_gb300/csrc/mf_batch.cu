@@ -640,13 +640,14 @@ class Server {
   // scratch.  FMM request: a solver handle's vectors, published arrays, cell
   // list and octree.
   static double need_bytes(int64_t n) {
-    // FMM requests: the handle's state and trees, ~1.2 KB per particle of
+    // FMM requests: the handle's state and trees, 1.5 KB per particle of
     // near-field partial sums where the force's near field runs once per box
-    // pair, and, where the force is the all-pairs product once per unordered
+    // pair ((1 + 125 half-stencil offsets) x 3 floats at the force's aperture
+    // 0.44), and, where the force is the all-pairs product once per unordered
     // pair, its block sums (12 KB per ordered pair of 1,024-particle blocks).
     if (n > kServeFmmMin) {
       const double nb = std::ceil(double(n) / 1024.0);
-      return double(n) * (720.0 + 1200.0) + 12288.0 * nb * nb + 64.0 * 1024 * 1024;
+      return double(n) * (720.0 + 1536.0) + 12288.0 * nb * nb + 64.0 * 1024 * 1024;
     }
     return double(n) * 320.0 + 4.0 * 1024 * 1024;
   }
