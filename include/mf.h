@@ -124,9 +124,17 @@ typedef enum mf_option {
                                of a magnetised body is ~40x the field's: 1.3e-4 at 0.5 and
                                P = 8, 6.6e-6 at 0.44 and P = 10 (1,048,576 particles).  Not in
                                the reference. */
-  MF_OPT_FMM_FORCE_ORDER = 16 /* expansion order P of those products (4..10), default 10: two
+  MF_OPT_FMM_FORCE_ORDER = 16,/* expansion order P of those products (4..10), default 10: two
                                degrees more than the field's default let the wider aperture
                                meet 1e-5 with fewer near pairs.  Not in the reference. */
+  MF_OPT_FUSED_PRODUCTS = 17 /* FP32 handles whose field and force both run once per unordered
+                               pair: the solve's first residual product also forms the
+                               Kelvin force of the same magnetization in the same launch,
+                               used by mf_eval_force if the solve then needs no iteration
+                               (the warm start stands, so M is unchanged) and discarded
+                               otherwise.  0 never, 1 after a solve whose warm start stood
+                               (default), 2 every solve.  Results equal the separate
+                               products' to FP32 rounding.  Not in the reference. */
 } mf_option;
 
 /* Construction parameters: the reference's CtorParam (magnetic_force.cuh:39-76). */
@@ -234,7 +242,9 @@ typedef enum mf_kernel_kind {
   MF_K_TENSOR = 2,          /* external gradient tensor */
   MF_K_FMM_NEAR_FIELD = 3,  /* the FMM near-field kernel of field products; pairs = executed near pairs */
   MF_K_FMM_NEAR_FORCE = 4,  /* the FMM near-field kernel of force products */
-  MF_K_FMM_FAR = 5          /* the FMM far-field stages (gather, P2M, M2M, M2L, L2L); pairs = M2L translations */
+  MF_K_FMM_FAR = 5,         /* the FMM far-field stages (gather, P2M, M2M, M2L, L2L); pairs = M2L translations */
+  MF_K_FIELD_FORCE = 6      /* field and force in one launch (MF_OPT_FUSED_PRODUCTS); pairs = both
+                               products' pairs, evals = unordered pairs */
 } mf_kernel_kind;
 typedef struct mf_kernel_stats {
   int64_t launches;

@@ -281,6 +281,7 @@ class Engine final : public EngineBase {
 
   // ---- setHext -------------------------------------------------------------
   mf_status set_external(const float* H0, const float* sp, const float* sm, int64_t ns, float hext) override {
+    ff_ready_ = false;
     if (ns < 0) return fail(MF_ERR_INVALID_ARG, "n_src < 0");
     if (ns > 0 && (!sp || !sm)) return fail(MF_ERR_INVALID_ARG, "external sources are NULL");
     if (H0)
@@ -359,6 +360,7 @@ class Engine final : public EngineBase {
   mf_status solve(int64_t niter, int64_t* iters, double* err) override {
     if (niter < 0) return fail(MF_ERR_INVALID_ARG, "niter < 0");
     history_.clear();
+    ff_ready_ = false;
     MF_TRY(eval_hext());
     mf_status st = (solver_ == MF_SOLVER_CG) ? solve_cg(niter, iters, err) : solve_nlcg(niter, iters, err);
     if (st != MF_OK && st != MF_ERR_NOT_CONVERGED) return st;
@@ -370,6 +372,7 @@ class Engine final : public EngineBase {
   // ---- evaluate_fitted_near_foece ----------------------------------------------
   mf_status eval_force() override {
     MF_TRY(publish_b());  // M = c b (magnetic_force.cu:899, :915)
+    if (ff_ready_) return force_from_fused();
     if (use_fmm_force()) {
       MF_TRY(fmm_product(true, plan_force_, mom4(), nullptr, nullptr, nullptr, nullptr));
       ctr_.force_passes += 1;
@@ -449,6 +452,7 @@ class Engine final : public EngineBase {
 
   mf_status set_option(int key, double v) override {
     if (!std::isfinite(v)) return fail(MF_ERR_INVALID_ARG, "option value must be finite");
+    ff_ready_ = false;
     switch (key) {
       case MF_OPT_TOLERANCE: tolerance_ = v; return MF_OK;
       case MF_OPT_MAX_ITERATION:
@@ -532,6 +536,10 @@ class Engine final : public EngineBase {
           MF_TRY(build_plans());
         }
         return MF_OK;
+      case MF_OPT_FUSED_PRODUCTS:
+        if (v != 0.0 && v != 1.0 && v != 2.0) return fail(MF_ERR_INVALID_ARG, "fused_products must be 0, 1 or 2");
+        fused_mode_ = int(v);
+        return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -556,6 +564,7 @@ class Engine final : public EngineBase {
       case MF_OPT_FMM_LEAF: *v = fmm_cfg_.leaf_min; return MF_OK;
       case MF_OPT_AUTOTUNE: *v = double(int(tune_)); return MF_OK;
       case MF_OPT_PAIR_SYMMETRIC: *v = double(sym_mode_); return MF_OK;
+      case MF_OPT_FUSED_PRODUCTS: *v = double(fused_mode_); return MF_OK;
       default: return fail(MF_ERR_INVALID_ARG, "unknown option key");
     }
   }
@@ -600,6 +609,15 @@ class Engine final : public EngineBase {
   int64_t fmm_field_products_ = 0, fmm_force_products_ = 0;
   bool plans_ready_ = false;
   bool rext_zero_ = true;
+  // The field and the force of one b in one launch (run_symff), for a solve
+  // whose warm start is expected to stand: plan_ff_ is the residual's plan in
+  // the fused kernel's blocks, ff_sum_ the force's pair sums it keeps.
+  Plan<Real> plan_ff_;
+  DevBuf ff_sum_;
+  bool ff_plan_ = false;   // plan_ff_ is built (both products once per unordered pair)
+  bool ff_hint_ = false;   // the last solve's warm start stood (no iteration)
+  bool ff_ready_ = false;  // ff_sum_ holds the pair sums of the current b
+  int fused_mode_ = 1;     // MF_OPT_FUSED_PRODUCTS
 
   R4* v4(int id) const { return vec4_[id].template as<R4>(); }
   R4* pos4() const { return v4(V_POS); }
@@ -730,6 +748,18 @@ class Engine final : public EngineBase {
     MF_TRY(build_plan<Real>(fb, {s}, plan_cgq_, fshape));
     s = base;
     MF_TRY(build_plan<Real>(gb, {s}, plan_force_, gshape));
+    ff_plan_ = ff_ready_ = false;
+    if constexpr (kF32) {
+      if (plan_resid_.shape == kShapeSym && plan_force_.shape == kShapeSym && fb == Body::FieldF2 &&
+          gb == Body::ForceF2) {
+        SceneSpec r = base;
+        r.scale = c;
+        r.coef_add = 1.0;
+        r.coef_add2 = -1.0;
+        MF_TRY(build_symff_plan({r}, plan_ff_));
+        ff_plan_ = true;
+      }
+    }
     MF_TRY(build_plan<Real>(fb, {base}, plan_apply_, fshape));  // G(m) alone
     MF_TRY(build_ext_plans());
     plans_ready_ = true;
@@ -887,7 +917,7 @@ class Engine final : public EngineBase {
     cudaEvent_t start = nullptr, stop = nullptr;
   };
   std::vector<TimedLaunch> timed_;
-  static constexpr int kKinds = MF_K_FMM_FAR + 1;
+  static constexpr int kKinds = MF_K_FIELD_FORCE + 1;
   mf_kernel_stats agg_[kKinds] = {};
   bool timing_ = false;
 
@@ -919,6 +949,7 @@ class Engine final : public EngineBase {
     return MF_OK;
   }
   void positions_changed() {
+    ff_ready_ = false;
     if constexpr (kF32) {
       to_pairs(pos4(), pos2_.template as<float4>(), np_, st_);
       ++ctr_.kernel_launches;
@@ -1154,12 +1185,17 @@ class Engine final : public EngineBase {
     k_init_row<<<1, 32, 0, st_>>>(scal_.template as<double>(), 0.0, 0.0);
     MF_CUDA_TRY(cudaGetLastError());
     // start()
-    MF_TRY(field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B)));
+    bool fused = false;
+    MF_TRY(first_residual(&fused));
     MF_TRY(reduce(NlErr<R4>{v4(V_R)}));
     double err = 0;
     MF_TRY(read_scalars(&err, S_ERR, 1));
     history_.push_back(err);
-    if (!(std::sqrt(err * inv_np) < tolerance_)) {
+    // The warm start stands: b is unchanged, and the fused launch kept its force.
+    const bool stood = std::sqrt(err * inv_np) < tolerance_;
+    ff_ready_ = fused && stood;
+    ff_hint_ = stood;
+    if (!stood) {
       MF_TRY(field(plan_grad_, v4(V_R), v4(V_G), v4(V_R), nullptr));
       MF_TRY(reduce(NlDirection<Real, R4>{v4(V_G), v4(V_DOLD), v4(V_D), true}));
       MF_TRY(alpha_and_step());
@@ -1188,6 +1224,85 @@ class Engine final : public EngineBase {
     return MF_OK;
   }
 
+  // The solve's first residual r = c G(b) + Hext - b.  Where both products
+  // run once per unordered pair and the last solve's warm start stood (or
+  // always, MF_OPT_FUSED_PRODUCTS 2), the force of the same b comes from the
+  // same launch; it is used if this solve's warm start stands too (b then is
+  // the magnetization the force is asked for), and discarded otherwise.
+  mf_status first_residual(bool* fused) {
+    *fused = false;
+    if constexpr (kF32) {
+      if (ff_plan_ && fused_mode_ != 0 && (fused_mode_ == 2 || ff_hint_) && !naive_ && !use_fmm_field() &&
+          !use_fmm_force()) {
+        MF_TRY(field_force_fused());
+        *fused = true;
+        return MF_OK;
+      }
+    }
+    return field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B));
+  }
+
+  mf_status field_force_fused() {
+    if constexpr (kF32) {
+      LaunchIO<Real> io;
+      io.tpos = pos4();
+      MF_TRY(prepare_packed(v4(V_B), false, io));  // the field's correction; b in pair layout
+      io.out4 = v4(V_R);
+      io.add4 = hext4();
+      io.add4b = v4(V_B);
+      size_t pd = 0;
+      symff_needs(plan_ff_, &pd);
+      MF_TRY(scr_.ensure(pd, 0));
+      MF_TRY(ff_sum_.reserve(size_t(3 * np_) * sizeof(double)));
+      TimedLaunch t;
+      if (timing_) {
+        t.body = MF_K_FIELD_FORCE;
+        t.pairs = plan_resid_.pairs + plan_force_.pairs;
+        t.evals = plan_ff_.evals;
+        MF_CUDA_TRY(cudaEventCreate(&t.start));
+        MF_CUDA_TRY(cudaEventCreate(&t.stop));
+        MF_CUDA_TRY(cudaEventRecord(t.start, st_));
+      }
+      MF_TRY(run_symff(plan_ff_, io, scr_.partials.template as<double>(), ff_sum_.template as<double>(),
+                       scr_.err.template as<int32_t>(), st_));
+      if (timing_) {
+        MF_CUDA_TRY(cudaEventRecord(t.stop, st_));
+        timed_.push_back(t);
+      }
+      ctr_.kernel_launches += 2;
+      ctr_.field_products += 1;
+      ctr_.field_pairs += plan_resid_.pairs;
+    }
+    return MF_OK;
+  }
+
+  // The force of M = c b from the pair sums the fused launch kept for b:
+  // the force's correction for M, then its epilogue on the sums scaled by
+  // c^2 (c as publish_b rounds it).
+  mf_status force_from_fused() {
+    ff_ready_ = false;
+    if constexpr (kF32) {
+      MF_TRY(ensure_cells());
+      MF_TRY(cells_.force_correction(pos4(), mom4(), corr_.template as<float4>(), st_));
+      LaunchIO<Real> io;
+      io.tpos = pos4();
+      io.tmom = mom4();
+      io.corr4 = corr_.template as<float4>();
+      for (int k = 0; k < 3; ++k) io.out[k] = pubr(MF_Q_FORCE, k);
+      if (!rext_zero_)
+        for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
+      io.naive_quirks = naive_ ? 1 : 0;
+      const double c = double(Real(c_coef()));
+      MF_TRY(run_sym_force_from_sums(plan_force_, io, ff_sum_.template as<double>(), c * c,
+                                     scr_.err.template as<int32_t>(), st_));
+      ctr_.kernel_launches += 2;
+      ctr_.force_passes += 1;
+      ctr_.force_pairs += plan_force_.pairs;
+      MF_TRY(scr_.check(st_));
+    }
+    return MF_OK;
+  }
+
   // calc_alpha (magnetic_force.cu:1287-1302), then b += alpha d (:1037, :1092).
   mf_status alpha_and_step() {
     MF_TRY(field(plan_dd_, v4(V_D), v4(V_DD), v4(V_D), nullptr));
@@ -1203,7 +1318,8 @@ class Engine final : public EngineBase {
     k_init_row<<<1, 32, 0, st_>>>(scal_.template as<double>(), rel_tol_, double(cap));
     MF_CUDA_TRY(cudaGetLastError());
     double* done = scal_.template as<double>() + S_DONE;
-    MF_TRY(field(plan_resid_, v4(V_B), v4(V_R), hext4(), v4(V_B)));
+    bool fused = false;
+    MF_TRY(first_residual(&fused));
     MF_TRY(reduce(CgStart<R4>{v4(V_R), v4(V_P), hext4()}));
     double row[kScal];
     MF_TRY(read_scalars(row, 0, kScal));
@@ -1232,6 +1348,9 @@ class Engine final : public EngineBase {
         }
       }
     }
+    // No iteration ran: b is the warm start, whose force the fused launch kept.
+    ff_ready_ = fused && executed == 0;
+    ff_hint_ = executed == 0 && row[S_RELRES] < rel_tol_;
     if (iters_out) *iters_out = executed;
     if (err_out) *err_out = row[S_RELRES];
     history_.push_back(row[S_RELRES]);

@@ -258,6 +258,22 @@ void sym_needs(const Plan<float>& plan, size_t* partial_doubles);
 mf_status run_sym(const Plan<float>& plan, const LaunchIO<float>& io, double* partials, int32_t* err,
                   cudaStream_t st);
 
+// The field and the Kelvin force of the same dipoles once per unordered pair
+// in one launch (mf_sympair.cu).  The plan is a packed field plan (its
+// epilogue coefficients) cut into the fused kernel's own blocks; io is the
+// field's (pair-layout sources and targets, correction, addends).  The
+// field's epilogue is applied; the force's pair sums, for those dipoles and
+// not yet corrected or scaled, go to gsum[3 n] (FP64).
+// run_sym_force_from_sums then applies the force's epilogue (a force plan's
+// scenes, io with the force's dipoles M, correction and outputs) to gsum
+// scaled by c2 = c^2, for dipoles M = c times those of the fused launch.
+mf_status build_symff_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan);
+void symff_needs(const Plan<float>& plan, size_t* partial_doubles);
+mf_status run_symff(const Plan<float>& plan, const LaunchIO<float>& io, double* partials, double* gsum,
+                    int32_t* err, cudaStream_t st);
+mf_status run_sym_force_from_sums(const Plan<float>& plan, const LaunchIO<float>& io, const double* gsum, double c2,
+                                  int32_t* err, cudaStream_t st);
+
 // Scratch sizes a plan needs.
 template <class Real>
 void plan_scratch_needs(const Plan<Real>& plan, size_t* partial_doubles, size_t* n_counters);

@@ -85,6 +85,52 @@ __device__ __forceinline__ void sym_field_pair2(float2 tx, float2 ty, float2 tz,
     src[2] = f2_fma(tmz, beta, f2_fma(dz, tt, src[2]));
   }
 
+// Field and Kelvin force of one pair item together, for a product of both
+// over the same dipoles: the separation, r^2 and the two dots d.m_s, d.m_t
+// are formed once (54 packed operations per target and item against 30 + 36
+// apart).  Each term is the one sym_field_pair2 / sym_force_pair2 forms,
+// operation for operation: the field clamped at its near radius (nf2), the
+// force at its own (ng2).
+__device__ __forceinline__ void sym_field_force_pair2(float2 tx, float2 ty, float2 tz, float2 tmx, float2 tmy,
+                                                      float2 tmz, const PairItems::Item& it, float nf2, float ng2,
+                                                      float2* accf, float2* accg, float2* srcf, float2* srcg) {
+  const float2 dx = f2_sub(tx, it.x), dy = f2_sub(ty, it.y), dz = f2_sub(tz, it.z);
+  const float2 r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx)));
+  const float2 ds = f2_fma(dz, it.mz, f2_fma(dy, it.my, f2_mul(dx, it.mx)));
+  const float2 dm = f2_fma(dz, tmz, f2_fma(dy, tmy, f2_mul(dx, tmx)));
+  {
+    const float2 ri = clamp_rsqrt2(r2, nf2);
+    const float2 ri2 = f2_mul(ri, ri);
+    const float2 beta = f2_mul(ri2, ri);
+    const float2 a3 = f2_mul(beta, f2_mul(ri2, f2_dup(-3.f)));
+    const float2 ts = f2_mul(ds, a3);
+    const float2 tt = f2_mul(dm, a3);
+    accf[0] = f2_fma(it.mx, beta, f2_fma(dx, ts, accf[0]));
+    accf[1] = f2_fma(it.my, beta, f2_fma(dy, ts, accf[1]));
+    accf[2] = f2_fma(it.mz, beta, f2_fma(dz, ts, accf[2]));
+    srcf[0] = f2_fma(tmx, beta, f2_fma(dx, tt, srcf[0]));
+    srcf[1] = f2_fma(tmy, beta, f2_fma(dy, tt, srcf[1]));
+    srcf[2] = f2_fma(tmz, beta, f2_fma(dz, tt, srcf[2]));
+  }
+  {
+    const float2 ri = clamp_rsqrt2(r2, ng2);
+    const float2 ri2 = f2_mul(ri, ri);
+    const float2 ri5 = f2_mul(f2_mul(ri2, ri2), ri);
+    const float2 sm = f2_fma(it.mz, tmz, f2_fma(it.my, tmy, f2_mul(it.mx, tmx)));
+    const float2 e = f2_mul(f2_mul(ri2, f2_dup(-5.f)), ds);
+    const float2 w = f2_fma(e, dm, sm);
+    const float2 g0 = f2_fma(dx, w, f2_fma(tmx, ds, f2_mul(it.mx, dm)));
+    const float2 g1 = f2_fma(dy, w, f2_fma(tmy, ds, f2_mul(it.my, dm)));
+    const float2 g2 = f2_fma(dz, w, f2_fma(tmz, ds, f2_mul(it.mz, dm)));
+    accg[0] = f2_fma(ri5, g0, accg[0]);
+    accg[1] = f2_fma(ri5, g1, accg[1]);
+    accg[2] = f2_fma(ri5, g2, accg[2]);
+    srcg[0] = f2_fma(ri5, g0, srcg[0]);
+    srcg[1] = f2_fma(ri5, g1, srcg[1]);
+    srcg[2] = f2_fma(ri5, g2, srcg[2]);
+  }
+}
+
 // s + x with the rounding error of the add carried in e: Knuth's TwoSum
 // (The Art of Computer Programming, vol. 2, 4.2.2), exact in round-to-
 // nearest without any ordering of |s| and |x|.

@@ -41,7 +41,7 @@ Q = {"positions": 0, "M": 1, "total_B_over_mu0": 2, "Hext": 3, "magnetic_bodyfor
 OPT = {"tolerance": 0, "max_iteration": 1, "naive": 2, "solver": 3, "rel_tol": 4, "cg_max_iter": 5,
        "crit_size": 6, "check_interval": 7, "kernel_timing": 8, "fmm": 9, "fmm_order": 10, "fmm_theta": 11,
        "fmm_leaf": 12, "autotune": 13, "pair_symmetric": 14, "fmm_force_theta": 15,
-       "fmm_force_order": 16}
+       "fmm_force_order": 16, "fused_products": 17}
 FMM_AUTO, FMM_ON, FMM_OFF = 0, 1, 2
 SOLVER_NLCG, SOLVER_CG = 0, 1
 
@@ -82,7 +82,8 @@ class mf_fmm_stats(ctypes.Structure):
                 ("force_p2p_pairs", ctypes.c_double), ("force_m2l_per_product", ctypes.c_double)]
 
 
-KERNEL = {"field": 0, "force": 1, "tensor": 2, "fmm_near_field": 3, "fmm_near_force": 4, "fmm_far": 5}
+KERNEL = {"field": 0, "force": 1, "tensor": 2, "fmm_near_field": 3, "fmm_near_force": 4, "fmm_far": 5,
+          "field_force": 6}
 
 _lib = None
 

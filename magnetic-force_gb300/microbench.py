@@ -41,6 +41,14 @@ autotuner) with the handle's event timing: G(m) through mf_apply_field and
 the force through mf_eval_force.  This is the launch shape the solver and
 the bench use.
 
+    python magnetic-force_gb300/microbench.py --kernel engine_step --n 65536 --reps 5 --fused 1
+
+``engine_step`` runs warm solves and forces of a Solver handle (CG, the
+positions unchanged, so every solve keeps its warm start): with --fused 1 or 2
+the solve's residual and the force come from one launch (k_sym_ff), with
+--fused 0 from the separate products.  It prints the device ms per step of
+each kernel kind from the handle's event timing.
+
 Every mode brackets its measured repetitions with the CUDA profiler range
 (cudaProfilerStart / cudaProfilerStop), so an Nsight Compute capture given
 ``--profile-from-start off`` sees those launches only, not the warm-up or
@@ -62,12 +70,14 @@ FLOP = {"field": 32.0, "force": 53.0, "tensor": 53.0}
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", default="field", choices=["field", "force", "tensor", "all", "fmm_field", "fmm_force", "fmm_step", "batch",
-                                                      "engine_field", "engine_force"])
+                                                      "engine_field", "engine_force", "engine_step"])
     ap.add_argument("--n", type=int, default=65536)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--pair-symmetric", type=int, default=-1,
                     help="fmm_* / engine_*: MF_OPT_PAIR_SYMMETRIC of the handle (-1: its default)")
+    ap.add_argument("--fused", type=int, default=-1,
+                    help="engine_step: MF_OPT_FUSED_PRODUCTS of the handle (-1: its default)")
     ap.add_argument("--density-of", type=int, default=0,
                     help="fmm_*: keep the particle spacing of the cylinder of this many particles (r 0.3, "
                          "height 1) and scale its radius and height to --n particles (0: r 0.3, height 1)")
@@ -81,6 +91,8 @@ def main():
 
     if args.kernel.startswith("fmm"):
         return fmm(args, np, torch, mfgb, scenes)
+    if args.kernel == "engine_step":
+        return engine_step(args, np, torch, mfgb, scenes)
     if args.kernel.startswith("engine"):
         return engine(args, np, torch, mfgb, scenes)
     if args.kernel == "batch":
@@ -228,6 +240,43 @@ def engine(args, np, torch, mfgb, scenes):
     print(json.dumps({"kernel": args.kernel, "n": sc.n, "kernel_ms": ms, "pairs_per_s": pairs / (ms * 1e-3),
                       "symmetric": sym, "tflops": flop / (ms * 1e-3) / 1e12,
                       "autotune": mfgb.autotune_report()}), flush=True)
+
+
+def engine_step(args, np, torch, mfgb, scenes):
+    sc = scenes.jittered_lattice(args.n, "sphere", radius=0.5, chi=2.0, seed=1)
+    s = mfgb.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
+    s.set_option("fmm", mfgb.FMM_OFF)
+    s.set_option("solver", mfgb.SOLVER_CG)
+    if args.pair_symmetric >= 0:
+        s.set_option("pair_symmetric", args.pair_symmetric)
+    if args.fused >= 0:
+        s.set_option("fused_products", args.fused)
+    s.solve(500)
+    s.evaluate_fitted_near_foece()
+    for _ in range(args.warmup):
+        s.solve(500)
+        s.evaluate_fitted_near_foece()
+    s.set_option("kernel_timing", 1)
+    s.reset_counters()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    iters = []
+    for _ in range(args.reps):
+        iters.append(s.solve(500)[0])
+        s.evaluate_fitted_near_foece()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    out = {"kernel": args.kernel, "n": sc.n, "fused": s.get_option("fused_products"), "iters": iters}
+    total = 0.0
+    for kind, fpe in (("field", 49.0), ("force", 55.0), ("field_force", 86.0)):
+        st = s.kernel_stats(kind)
+        if st["launches"]:
+            ms = st["total_ms"] / args.reps
+            total += ms
+            out[kind] = {"launches": st["launches"], "ms_per_step": ms,
+                         "tflops": fpe * st["evals"] / (st["total_ms"] * 1e-3) / 1e12}
+    out["pair_ms_per_step"] = total
+    print(json.dumps(out), flush=True)
 
 
 if __name__ == "__main__":

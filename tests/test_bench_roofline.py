@@ -43,6 +43,21 @@ def test_ordered_and_unordered_counts(bench):
     assert r["kernels"]["field"]["body_bound"] == pytest.approx(64.0 / 76.0, abs=1e-4)
 
 
+def test_field_and_force_in_one_launch(bench):
+    # Steps whose solve keeps its warm start: one fused launch per step, the
+    # shared terms counted once (86 FLOP per unordered pair).
+    n, peak = 65536, 80.5
+    kff = stats(n, 4.5, 10, True)
+    kff["pairs"] *= 2  # both products' pairs
+    none = {"launches": 0, "total_ms": 0.0, "pairs": 0.0, "evals": 0.0}
+    r = bench.pair_roofline(none, none, peak, n, kff=kff)
+    assert r["kernel"] == "k_sym_ff<field+force>"
+    want = 86.0 * n * (n - 1) / 2 / 4.5e-3 / 1e12
+    assert r["achieved"] == pytest.approx(want, abs=1e-3)
+    assert r["kernels"]["field_force"]["body_bound"] == pytest.approx(172.0 / 216.0, abs=1e-4)
+    assert set(r["kernels"]) == {"field_force"}
+
+
 def test_traffic_only_at_the_profiled_size(bench):
     r = bench.pair_roofline(stats(32768, 1.0, 1, True), stats(32768, 1.0, 1, True), 73.0, 32768)
     assert r["traffic"] is None

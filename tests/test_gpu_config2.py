@@ -75,3 +75,25 @@ def test_fmm_solution_matches_oracle(mf, config2):
     ef = rel(s.magnetic_bodyforce, z["F"])
     assert eb < 1e-5 and em < 1e-5 and ef < 1e-5, (eb, em, ef)
     s.close()
+
+
+def test_fused_step_matches_oracle(mf, config2):
+    # Warm steps at the full size: once the warm start stands, the solve's
+    # residual and the Kelvin force come from one launch (field and force
+    # once per unordered pair); the state and force still match the oracle.
+    z = config2
+    c = float(z["volume"]) * float(z["chi"]) / (1.0 + float(z["chi"]))
+    s = solved(mf, z, 1e-6)
+    f_sep = s.magnetic_bodyforce.copy()
+    s.set_option("kernel_timing", 1)
+    for _ in range(2):
+        it, rr = s.solve(500)
+        assert it == 0 and rr < 1e-6
+    s.evaluate_fitted_near_foece()
+    assert s.kernel_stats("field_force")["launches"] == 1 and s.kernel_stats("force")["launches"] == 0
+    ef = rel(s.magnetic_bodyforce, z["F"])
+    assert rel(s.magnetic_bodyforce, f_sep) < 2e-6
+    eb = rel(s.total_B_over_mu0, z["b"])
+    em = rel(s.M, c * z["b"].astype(np.float64))
+    assert eb < 1e-5 and em < 1e-5 and ef < 1e-5, (eb, em, ef)
+    s.close()
