@@ -370,14 +370,21 @@ __global__ void k_sym_finish(const AllPairsArgs<float> a, const float* __restric
 // field's epilogue as k_sym_finish<false> applies it; the force sums (for
 // dipoles b, not yet scaled to M = c b) are kept per particle in FP64 and
 // applied by k_sym_force_from_sums once the solve has confirmed that b did
-// not change.  Blocks hold kFfTPT targets per thread: the two bodies' sums
-// take twice the registers of one.
+// not change.  Blocks of 1,024 particles (128 threads x 8 targets) as in
+// k_sym; the two bodies' sums take twice the registers of one, so the kernel
+// runs at 255 registers with a few bytes spilled, and the source sums of a
+// tile are reduced in four phases (a phase's per-warp buffer fits the static
+// shared memory).
 // ---------------------------------------------------------------------------
-constexpr int kFfTPB = 128, kFfTPT = 4, kFfStages = 2, kFfMinBlocks = 3;
+// Measured at N = 65,536 / 131,072 (ms per fused launch with its finish;
+// targets per thread, CTAs per SM, phases): 4, 3, 2 (166 registers) 4.90 /
+// 18.54; 6, 2, 2 (242) 4.63 / 17.93; 8, 2, 4 (255, 124 bytes of spills)
+// 4.54 / 18.05.  The separate products take 5.36 / 21.37.
+constexpr int kFfTPB = 128, kFfTPT = 8, kFfStages = 2, kFfMinBlocks = 2;
 constexpr int kFfTB = kFfTPB * kFfTPT;
 constexpr int kFfWarps = kFfTPB / 32;
 constexpr size_t kFfSmem = size_t(kFfStages) * 2 * kFfTB * sizeof(float4);
-constexpr int kFfSplit = 2;
+constexpr int kFfSplit = 4;  // phases per tile: the per-warp source sums of one phase fit the static smem
 constexpr int kFfNH = kFfTB / 2 / kFfSplit;  // pair items per phase
 // Per item, 12 source sums: field x, y, z then force x, y, z, each for the
 // item's two sources.  Row stride 13 (odd): one item's 12 lane writes, and
