@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MF_ABI_VERSION 3
+#define MF_ABI_VERSION 4
 
 typedef enum mf_status {
   MF_OK = 0,

@@ -15,7 +15,7 @@ def test_exports_every_declared_symbol(mf):
 
 def test_abi_version_and_strings(mf):
     lib = mf.load()
-    assert lib.mf_abi_version() == 3
+    assert lib.mf_abi_version() == 4
     assert lib.mf_status_string(0) == b"MF_OK"
     assert lib.mf_status_string(5) == b"MF_ERR_TIMEOUT"
 
