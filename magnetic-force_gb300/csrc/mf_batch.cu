@@ -43,6 +43,21 @@ __global__ void k_batch_init_rows(double* scal, int n, double tol, double maxit,
   if (blockIdx.x == 0 && threadIdx.x == 0) *done_count = 0;
 }
 
+// After a solve: a packed-force scene whose solve made no CG update kept its
+// b, so its force comes from the sums the fused residual launch kept
+// (kept[s] = 1); the others take their own force product (kept[s] = 0).
+// kept_count counts the first kind: the force product does nothing when
+// every scene kept its b.
+__global__ void k_batch_mark_kept(const double* __restrict__ scal, const int32_t* __restrict__ ids, int n_ids,
+                                  double* __restrict__ kept, int32_t* __restrict__ kept_count) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_ids; j += gridDim.x * blockDim.x) {
+    const int s = ids[j];
+    const bool k = scal[int64_t(s) * kScal + S_ITERS] == 0.0;
+    kept[s] = k ? 1.0 : 0.0;
+    if (k) atomicAdd(kept_count, 1);
+  }
+}
+
 // M = c b per scene (the dipoles of the force pass).
 struct BPublish {
   static constexpr int kN = 0;
@@ -261,6 +276,30 @@ class Batch {
       }
     }
 
+    // The packed scenes' residual and force in one launch where both run once
+    // per unordered pair (MF_FUSED_PRODUCTS=0 never): plan_ff_ covers the
+    // packed field scenes; the force sums of those below the packed force
+    // threshold are not used.
+    ff_ = ff_valid_ = false;
+    n_ff_ids_ = 0;
+    if (default_fused_mode() != 0 && plan_resid_[1].n_scenes && plan_force_[1].n_scenes &&
+        plan_resid_[1].shape == kShapeSym && plan_force_[1].shape == kShapeSym) {
+      MF_TRY(build_symff_plan(resid[1], plan_ff_));
+      size_t pd = 0;
+      symff_needs(plan_ff_, &pd);
+      MF_TRY(scr_.ensure(pd, 0));
+      MF_TRY(ff_sum_.reserve_grow(size_t(3 * n_alloc_) * sizeof(double)));
+      std::vector<int32_t> ids;
+      for (const SceneDesc<float>& x : plan_force_[1].host) ids.push_back(x.flag_index);
+      MF_TRY(ff_ids_.reserve_grow(ids.size() * sizeof(int32_t)));
+      MF_CUDA_TRY(cudaMemcpy(ff_ids_.ptr, ids.data(), ids.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+      MF_TRY(kept_.reserve_grow(size_t(n) * sizeof(double)));
+      MF_CUDA_TRY(cudaMemsetAsync(kept_.ptr, 0, size_t(n) * sizeof(double), st_));
+      MF_TRY(kept_count_.reserve_grow(16));
+      n_ff_ids_ = int(ids.size());
+      ff_ = true;
+    }
+
     std::vector<CellSceneSpec> cs;
     for (const SI& si : sc_) cs.push_back(CellSceneSpec{si.off, si.n, si.h});
     MF_TRY(cells_.build(pos4_.as<float4>(), cs, st_, /*margin_h=*/2.0));
@@ -296,7 +335,9 @@ class Batch {
                     std::make_pair(&corr_, &o.corr_), std::make_pair(&fs_, &o.fs_),
                     std::make_pair(&scal_, &o.scal_), std::make_pair(&ranges_, &o.ranges_),
                     std::make_pair(&red_part_, &o.red_part_), std::make_pair(&red_tickets_, &o.red_tickets_),
-                    std::make_pair(&done_count_, &o.done_count_)})
+                    std::make_pair(&done_count_, &o.done_count_), std::make_pair(&ff_sum_, &o.ff_sum_),
+                    std::make_pair(&ff_ids_, &o.ff_ids_), std::make_pair(&kept_, &o.kept_),
+                    std::make_pair(&kept_count_, &o.kept_count_)})
       *pr.first = std::move(*pr.second);
     scr_ = std::move(o.scr_);
     cells_ = std::move(o.cells_);
@@ -308,6 +349,9 @@ class Batch {
         pr.first->host.clear();
       }
     }
+    plan_ff_ = std::move(o.plan_ff_);
+    plan_ff_.n_scenes = 0;
+    plan_ff_.host.clear();
 
   }
   int scenes() const { return int(sc_.size()); }
@@ -315,12 +359,13 @@ class Batch {
   // ---- solve -----------------------------------------------------------------
   mf_status solve(int64_t max_iter, double tol, bool host_checks) {
     const int n = scenes();
+    ff_valid_ = false;
     k_batch_init_rows<<<(n + 127) / 128, 128, 0, st_>>>(scal_.as<double>(), n, tol, double(max_iter),
                                                         done_count_.as<int32_t>());
     MF_CUDA_TRY(cudaGetLastError());
     ++ctr_.kernel_launches;
-    // r = c G b + Hext - b
-    MF_TRY(field(plan_resid_, b4_.as<float4>(), r4_.as<float4>(), hext4_.as<float4>(), b4_.as<float4>(), false));
+    // r = c G b + Hext - b (with the packed scenes' force of b, where fused)
+    MF_TRY(field(plan_resid_, b4_.as<float4>(), r4_.as<float4>(), hext4_.as<float4>(), b4_.as<float4>(), false, ff_));
     MF_TRY(reduce(CgStart<float4>{r4_.as<float4>(), p4_.as<float4>(), hext4_.as<float4>(), done_count_.as<int32_t>()}));
     ++solves_;
     for (int64_t it = 0; it < max_iter; ++it) {
@@ -336,6 +381,7 @@ class Batch {
       }
     }
     MF_TRY(reduce(BPublish{b4_.as<float4>(), mom4_.as<float4>()}));
+    ff_valid_ = ff_;
     return MF_OK;
   }
 
@@ -358,8 +404,27 @@ class Batch {
       io.spos = pos2_.as<float4>();
       io.smom = mom2_.as<float4>();
       io.corr4 = corr_.as<float4>();
-      MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
-      ctr_.kernel_launches += plan_force_[1].shape == kShapeSym ? 4 : 3;
+      if (ff_ && ff_valid_) {
+        // Scenes whose solve kept b: the force from the fused launch's sums;
+        // the others (skipped by the first) through their force product.
+        MF_CUDA_TRY(cudaMemsetAsync(kept_count_.ptr, 0, sizeof(int32_t), st_));
+        k_batch_mark_kept<<<(n_ff_ids_ + 127) / 128, 128, 0, st_>>>(scal_.as<double>(), ff_ids_.as<int32_t>(),
+                                                                     n_ff_ids_, kept_.as<double>(),
+                                                                     kept_count_.as<int32_t>());
+        MF_CUDA_TRY(cudaGetLastError());
+        LaunchIO<float> g = io;
+        g.done_flags = kept_.as<double>();
+        g.done_stride = 1;
+        g.done_count = kept_count_.as<int32_t>();
+        g.done_total = n_ff_ids_;
+        MF_TRY(run_plan<float>(plan_force_[1], g, scr_, st_));
+        MF_TRY(run_sym_force_from_sums(plan_force_[1], io, ff_sum_.as<double>(), 0.0, kept_.as<double>(),
+                                       scal_.as<double>(), kScal, S_CONST_C, scr_.err.as<int32_t>(), st_));
+        ctr_.kernel_launches += 6;
+      } else {
+        MF_TRY(run_plan<float>(plan_force_[1], io, scr_, st_));
+        ctr_.kernel_launches += plan_force_[1].shape == kShapeSym ? 4 : 3;
+      }
     }
     ctr_.force_passes += 1;
     ctr_.force_pairs += pairs_;
@@ -371,6 +436,7 @@ class Batch {
     MF_TRY(eval_force());
     const float* F = fs_.as<float>();
     MF_TRY(reduce(BIntegrate{F, F + n_alloc_, F + 2 * n_alloc_, vel4_.as<float4>(), pos4_.as<float4>(), float(dt)}));
+    ff_valid_ = false;  // the kept sums belong to the old positions
     MF_TRY(cells_.rebin(pos4_.as<float4>(), st_));
     to_pairs(pos4_.as<float4>(), pos2_.as<float4>(), n_alloc_, st_);
     MF_CUDA_TRY(cudaGetLastError());
@@ -521,7 +587,7 @@ class Batch {
   };
 
   mf_status field(const Plan<float>* plans, const float4* src_mom, float4* out4, const float4* add4,
-                  const float4* add4b, bool skip_done) {
+                  const float4* add4b, bool skip_done, bool fused = false) {
     const int n = scenes();
     const int32_t* dc = skip_done ? done_count_.as<int32_t>() : nullptr;
     LaunchIO<float> io;
@@ -549,8 +615,13 @@ class Batch {
       io.spos = pos2_.as<float4>();
       io.smom = mom2_.as<float4>();
       io.corr4 = corr_.as<float4>();
-      MF_TRY(run_plan<float>(plans[1], io, scr_, st_));
-      ctr_.kernel_launches += plans[1].shape == kShapeSym ? 4 : 3;
+      if (fused) {
+        MF_TRY(run_symff(plan_ff_, io, scr_.partials.as<double>(), ff_sum_.as<double>(), scr_.err.as<int32_t>(), st_));
+        ctr_.kernel_launches += 4;
+      } else {
+        MF_TRY(run_plan<float>(plans[1], io, scr_, st_));
+        ctr_.kernel_launches += plans[1].shape == kShapeSym ? 4 : 3;
+      }
     }
     return MF_OK;
   }
@@ -581,6 +652,14 @@ class Batch {
   DevBuf pos4_, pos2_, vel4_, b4_, r4_, p4_, q4_, hext4_, mom4_, mom2_, corr_, fs_;
   DevBuf scal_, ranges_, red_part_, red_tickets_, done_count_;
   Plan<float> plan_resid_[2], plan_cgq_[2], plan_force_[2];  // [0] exact branches, [1] packed
+  // The packed scenes' residual and force in one launch (run_symff): its
+  // plan, the force sums it keeps (for b), the packed force scenes and their
+  // kept flags (k_batch_mark_kept).  ff_valid_: the kept sums are those of
+  // the current b and positions.
+  Plan<float> plan_ff_;
+  DevBuf ff_sum_, ff_ids_, kept_, kept_count_;
+  int n_ff_ids_ = 0;
+  bool ff_ = false, ff_valid_ = false;
   Tune tune_ = Tune::OnMiss;
   int sym_mode_ = default_sym_mode();  // pair-symmetric products: 0 never, 1 tuned, 2 always
   Scratch scr_;

@@ -617,7 +617,7 @@ class Engine final : public EngineBase {
   bool ff_plan_ = false;   // plan_ff_ is built (both products once per unordered pair)
   bool ff_hint_ = false;   // the last solve's warm start stood (no iteration)
   bool ff_ready_ = false;  // ff_sum_ holds the pair sums of the current b
-  int fused_mode_ = 1;     // MF_OPT_FUSED_PRODUCTS
+  int fused_mode_ = default_fused_mode();  // MF_OPT_FUSED_PRODUCTS
 
   R4* v4(int id) const { return vec4_[id].template as<R4>(); }
   R4* pos4() const { return v4(V_POS); }
@@ -1293,7 +1293,7 @@ class Engine final : public EngineBase {
         for (int k = 0; k < 9; ++k) io.rext[k] = rext(k);
       io.naive_quirks = naive_ ? 1 : 0;
       const double c = double(Real(c_coef()));
-      MF_TRY(run_sym_force_from_sums(plan_force_, io, ff_sum_.template as<double>(), c * c,
+      MF_TRY(run_sym_force_from_sums(plan_force_, io, ff_sum_.template as<double>(), c * c, nullptr, nullptr, 0, 0,
                                      scr_.err.template as<int32_t>(), st_));
       ctr_.kernel_launches += 2;
       ctr_.force_passes += 1;

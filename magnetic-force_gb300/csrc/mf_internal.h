@@ -266,13 +266,20 @@ mf_status run_sym(const Plan<float>& plan, const LaunchIO<float>& io, double* pa
 // not yet corrected or scaled, go to gsum[3 n] (FP64).
 // run_sym_force_from_sums then applies the force's epilogue (a force plan's
 // scenes, io with the force's dipoles M, correction and outputs) to gsum
-// scaled by c2 = c^2, for dipoles M = c times those of the fused launch.
+// scaled by c^2, for dipoles M = c times those of the fused launch: c^2 = c2
+// for every scene, or, where rows is given, c = float(rows[flag_index *
+// row_stride + c_index]) per scene; where kept is given, only the scenes
+// whose kept[flag_index] is non-zero are written.
 mf_status build_symff_plan(const std::vector<SceneSpec>& specs, Plan<float>& plan);
 void symff_needs(const Plan<float>& plan, size_t* partial_doubles);
 mf_status run_symff(const Plan<float>& plan, const LaunchIO<float>& io, double* partials, double* gsum,
                     int32_t* err, cudaStream_t st);
 mf_status run_sym_force_from_sums(const Plan<float>& plan, const LaunchIO<float>& io, const double* gsum, double c2,
-                                  int32_t* err, cudaStream_t st);
+                                  const double* kept, const double* rows, int row_stride, int c_index, int32_t* err,
+                                  cudaStream_t st);
+// Default of MF_OPT_FUSED_PRODUCTS for new handles, and whether batches fuse
+// (MF_FUSED_PRODUCTS=0|1|2 in the environment; 1 when unset).
+int default_fused_mode();
 
 // Scratch sizes a plan needs.
 template <class Real>

@@ -202,9 +202,9 @@ __global__ void __launch_bounds__(kSymTPB) k_sym(const AllPairsArgs<float> a, fl
       k_fail = k;
       break;
     }
-    // A stopped scene's sums are not written (block-uniform).  Force products
-    // carry no stop flags; the check is compiled out of that kernel.
-    if (kForce || !scene_done(a, sc)) {
+    // A stopped scene's sums are not written (block-uniform).  A force
+    // product's flags mark the scenes whose force comes from kept sums.
+    if (!scene_done(a, sc)) {
       const bool sym = I != J;
       const int64_t rem = sc.ns - int64_t(J) * TB;
       const int cnt = int(rem < TB ? rem : TB);
@@ -622,7 +622,8 @@ __global__ void k_sym_ff_finish(const AllPairsArgs<float> a, const float* __rest
 // the external gradient term and the scene's scale, as k_sym_finish<true>
 // applies them.  a carries the force plan's scenes and the dipoles M.
 __global__ void k_sym_force_from_sums(const AllPairsArgs<float> a, const double* __restrict__ gsum, double c2,
-                                      int64_t g0, int64_t n_span) {
+                                      const double* __restrict__ kept, const double* __restrict__ rows,
+                                      int row_stride, int c_index, int64_t g0, int64_t n_span) {
   for (int64_t g = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < n_span;
        g += int64_t(gridDim.x) * blockDim.x) {
     const int64_t gi = g0 + g;
@@ -634,7 +635,13 @@ __global__ void k_sym_force_from_sums(const AllPairsArgs<float> a, const double*
     }
     const SceneDesc<float>& sc = a.scenes[lo];
     if (gi - sc.t_off >= sc.nt) continue;
-    const double v[3] = {gsum[3 * gi] * c2, gsum[3 * gi + 1] * c2, gsum[3 * gi + 2] * c2};
+    if (kept && kept[sc.flag_index] == 0.0) continue;  // this scene's force comes from its own product
+    double cc = c2;
+    if (rows) {
+      const double c = double(float(rows[int64_t(sc.flag_index) * row_stride + c_index]));
+      cc = c * c;
+    }
+    const double v[3] = {gsum[3 * gi] * cc, gsum[3 * gi + 1] * cc, gsum[3 * gi + 2] * cc};
     const float4 m = a.tmom[gi];
     force_epilogue<float>(a, sc, gi, double(m.x), double(m.y), double(m.z), v);
   }
@@ -831,14 +838,23 @@ mf_status run_symff(const Plan<float>& plan, const LaunchIO<float>& io, double* 
   return MF_OK;
 }
 
+int default_fused_mode() {
+  static const int mode = [] {
+    const char* e = getenv("MF_FUSED_PRODUCTS");
+    return (e && (e[0] == '0' || e[0] == '2') && e[1] == 0) ? e[0] - '0' : 1;
+  }();
+  return mode;
+}
+
 mf_status run_sym_force_from_sums(const Plan<float>& plan, const LaunchIO<float>& io, const double* gsum, double c2,
-                                  int32_t* err, cudaStream_t st) {
+                                  const double* kept, const double* rows, int row_stride, int c_index, int32_t* err,
+                                  cudaStream_t st) {
   if (plan.host.empty()) return MF_OK;
   const AllPairsArgs<float> a = sym_args(plan, io, err);
   const int64_t g0 = plan.host.front().t_off;
   const int64_t n_span = plan.host.back().t_off + plan.host.back().nt - g0;
   const int64_t fb = std::min<int64_t>((n_span + 255) / 256, 8192);
-  k_sym_force_from_sums<<<unsigned(fb), 256, 0, st>>>(a, gsum, c2, g0, n_span);
+  k_sym_force_from_sums<<<unsigned(fb), 256, 0, st>>>(a, gsum, c2, kept, rows, row_stride, c_index, g0, n_span);
   MF_CUDA_TRY(cudaGetLastError());
   return MF_OK;
 }

@@ -117,10 +117,13 @@ def test_packed_products_once_per_pair_in_batch(mf, tmp_path):
     # Scenes of the packed field and force paths in a child process with
     # MF_PAIR_SYMMETRIC=2 and MF_AUTOTUNE=0 (both read once per process): the
     # batch evaluates every field and force product once per unordered pair,
-    # the CG's per-scene stop flags included -- a force product is 4
-    # launches: pair records, near-field correction, pair kernel,
-    # per-particle finish.  Each scene matches the same scene solved alone,
-    # and graph-captured steps match plain steps bit for bit.
+    # the CG's per-scene stop flags included -- a force product after a solve
+    # is 6 launches: the marks of the scenes whose solve kept b (their force
+    # comes from the solve's fused residual launch; none after this cold
+    # solve), pair records, near-field correction, pair kernel, per-particle
+    # finish, the force from the kept sums.  Each scene matches the same
+    # scene solved alone, and graph-captured steps match plain steps bit for
+    # bit.
     import os
     import subprocess
     import sys
@@ -130,7 +133,7 @@ def test_packed_products_once_per_pair_in_batch(mf, tmp_path):
     env = dict(os.environ, MF_AUTOTUNE="0", MF_PAIR_SYMMETRIC="2")
     subprocess.run([sys.executable, "-c", CHILD, path, here, pkg], env=env, check=True, timeout=600)
     got = np.load(path)
-    assert int(got["launches"]) == 4
+    assert int(got["launches"]) == 6
     assert bool(got["graph_equal"])
     for k, sc in enumerate(mixed_scenes(seed=41, sizes=(4097, 6000, 9001))):
         s = mf.Solver(sc.n, sc.h, sc.h, sc.volume, sc.chi, sc.H0, None, None, sc.pos)
