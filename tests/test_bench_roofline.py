@@ -56,6 +56,10 @@ def test_field_and_force_in_one_launch(bench):
     assert r["achieved"] == pytest.approx(want, abs=1e-3)
     assert r["kernels"]["field_force"]["body_bound"] == pytest.approx(172.0 / 216.0, abs=1e-4)
     assert set(r["kernels"]) == {"field_force"}
+    # the same launch at the two products' own counts (49 + 55)
+    assert r["kernels"]["field_force"]["tflops_at_product_counts"] == pytest.approx(want * 104.0 / 86.0)
+    # the profiled DRAM bytes of this launch at this size
+    assert r["traffic"] == 43090688
 
 
 def test_traffic_only_at_the_profiled_size(bench):
