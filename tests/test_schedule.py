@@ -300,3 +300,73 @@ def test_fmm_half_stencil_planes():
                     if b != (ax, ay, az) and inside(*b) and b in occupied:
                         full.add(frozenset([(ax, ay, az), b]))
         assert pairs == full
+
+
+# ---------------------------------------------------------------------------
+# The warp reduce-scatter of the source sums (mf_sym.cuh warp_reduce_scatter)
+# and the per-warp phase buffer of the fused field-and-force launch
+# (mf_sympair.cu k_sym_ff): which lane ends with which sum, and which slot
+# each value is stored at and read back from.
+# ---------------------------------------------------------------------------
+def warp_reduce_scatter(v):
+    """Lane-by-lane model of the device's shuffle tree over v[32][NV]."""
+    w = np.array(v, dtype=np.float64)
+    nv = w.shape[1]
+    b, n = 16, nv
+    while n > 1:
+        new = w.copy()
+        for lane in range(32):
+            hi = bool(lane & b)
+            p = lane ^ b
+            phi = bool(p & b)
+            for q in range(n // 2):
+                keep = w[lane, q + n // 2] if hi else w[lane, q]
+                got = w[p, q] if phi else w[p, q + n // 2]  # the partner's `send`
+                new[lane, q] = keep + got
+        w = new
+        n //= 2
+        b >>= 1
+    while b >= 1:
+        w[:, 0] = w[:, 0] + w[np.arange(32) ^ b, 0]
+        b >>= 1
+    return w[:, 0]
+
+
+def test_warp_reduce_scatter_lanes():
+    rng = np.random.default_rng(9)
+    for nv in (8, 16, 32):
+        v = rng.normal(size=(32, nv))
+        got = warp_reduce_scatter(v)
+        per = 32 // nv
+        for lane in range(32):
+            assert abs(got[lane] - v[:, lane // per].sum()) < 1e-12, (nv, lane)
+
+
+def test_fused_phase_buffer_slots():
+    # k_sym_ff: per pair item 12 values (field x, y, z then force x, y, z, each
+    # for the item's two sources: value 2c + s and 6 + 2c + s) in a 16-value
+    # reduce-scatter, so value k sits in lanes 2k and 2k + 1 and the even lane
+    # stores it at row stride 13.  At the phase's end thread r reads source
+    # 2 (r >> 1) + (r & 1) of the phase.  Every (item, value) slot is written
+    # once and read once, by the thread of its own source and component.
+    TB, SPLIT, ROW = 1024, 4, 13
+    NH = TB // 2 // SPLIT
+    written, read = {}, {}
+    for j in range(NH):
+        for lane in range(32):
+            kv = lane >> 1
+            if lane & 1 == 0 and kv < 12:
+                slot = j * ROW + kv
+                assert slot not in written
+                written[slot] = (j, kv)
+    assert len(written) == 12 * NH and max(written) < NH * ROW
+    for r in range(2 * NH):
+        j, s = r >> 1, r & 1
+        for c in range(3):
+            for base, prod in ((0, "field"), (6, "force")):
+                slot = j * ROW + base + 2 * c + s
+                assert slot not in read
+                read[slot] = (prod, 2 * j + s, c)
+                # the value stored there is that source's component of that product
+                assert written[slot] == (j, base + 2 * c + s)
+    assert set(read) == set(written)
